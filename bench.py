@@ -1,0 +1,389 @@
+"""Benchmark: beams/s of the collapsed-cone dose engine on GB300.
+
+Workload (one "step"): a batch of --beams beams on the heterogeneous 128^3
+slab phantom (0.25 cm voxels: water, lung slab 0.25 g/cc at depth 5-12 cm,
+bone slab 1.85 g/cc at 14-16 cm, 20 random cuboid inserts of 0.2-2.0
+g/cc), 5 x 5 cm^2 jaw field, gantry uniform in [0, 360), seeded synthetic
+inputs.  Every beam runs the whole path: blocking -> radiological depth ->
+fluence -> TERMA -> collapsed-cone dose (float32 dose and accumulation).
+
+  value       beams/s with inputs resident in HBM (batched, one persistent
+              cone launch per step), L2 flushed (256 MiB write) between steps
+  e2e         beams/s through the C ABI with pinned host buffers: density and
+              block-map H2D plus dose D2H inside the timed region
+  roofline    cone-gather kernel: algorithmic HBM bytes (TERMA read + dose
+              write per beam) per launch over its CUDA-event time, against
+              the measured HBM peak; "onchip" gives the same kernel's
+              voxel-direction updates/s against its shared-memory ceiling
+  cpu_baseline / --impl reference
+              the CPU oracle (C++ FP64 restatement of the reference path,
+              OpenMP over every host core) on whole beams of the workload
+
+Multi-GPU (torchrun): beams are independent, so each rank runs its own
+batches (weak scaling, no data-path collective); the step time is the
+maximum over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+
+METRIC = ("beams/s @128³ batched vs plain-GPU vs CPU at ≤0.5% Dmax; HBM GB/s; "
+          "p50/p99 ms")
+SETTINGS = {
+    'sPri': 0.90924, 'sAnn': 2.887e-3, 'zAnn': 4.0, 'rInner': 0.2, 'rOuter': 1.4,
+    'zExp': 12.5, 'sExp': 8.289e-3, 'kExp': 0.4816, 'softRatio': 0.0025,
+    'softLimit': 20, 'hornRatio': 0.0065, 'fluenceResampling': 3,
+    'energy_weights': {"0.5": 0.08196, "1.0": 0.12385, "1.5": 0.10605, "2.0": 0.08307,
+                       "2.5": 0.05881, "3.0": 0.03911, "3.5": 0.02131, "4.0": 0.02426,
+                       "4.5": 0.0, "5.0": 0.00881, "5.5": 0.0, "6.0": 0.00498},
+}
+
+
+# ----------------------------------------------------------- distribution --
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def dist_init(backend):
+    import torch.distributed as dist
+    world, rank, _ = dist_env()
+    if world > 1 and not dist.is_initialized():
+        dist.init_process_group(backend=backend, rank=rank, world_size=world)
+    return world, rank
+
+
+def barrier():
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
+def max_over_ranks(x, device=None):
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def beam_seed(rank, index):
+    """Per-rank, per-beam seed: ranks draw disjoint beams (weak scaling)."""
+    return 1_000_003 * (rank + 1) + index
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([p.strip() for p in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = [float(s[0]) for s in self.samples if s and s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if len(s) > 1 and s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 3 + i and s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+# --------------------------------------------------------------- workload --
+def workload(n, spacing, seed=0):
+    from conehead_gb300.phantoms import slab_phantom
+    return slab_phantom(n, spacing, seed=seed)
+
+
+def make_beam(seed, field):
+    from conehead_gb300.phantoms import random_beam
+    return random_beam(np.random.default_rng(seed), field=field)
+
+
+def cpu_oracle_beams(phantom, beams, threads=None):
+    """Time the FP64 oracle on whole beams; returns (beams/s, cores, seconds)."""
+    from oracle import oracle
+    oracle.build()
+    t0 = time.perf_counter()
+    for src, blk in beams:
+        oracle.calculate(src, blk, phantom, SETTINGS, oracle.MODE_F64)
+    dt = time.perf_counter() - t0
+    return len(beams) / dt, oracle.num_threads(), dt
+
+
+def run_reference(args):
+    """--impl reference: the CPU oracle of the reference path, rank 0 only."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    ph = workload(args.grid, args.spacing)
+    beams = [make_beam(beam_seed(0, i), args.field) for i in range(args.warmup + args.steps)]
+    from oracle import oracle
+    oracle.build()
+    for src, blk in beams[:args.warmup]:
+        oracle.calculate(src, blk, ph, SETTINGS, oracle.MODE_F64)
+    v, cores, dt = cpu_oracle_beams(ph, beams[args.warmup:])
+    sample = (f"{args.steps} whole beams ({args.grid}^3, {args.field:g}x{args.field:g} cm, "
+              f"random gantry), FP64 oracle, OpenMP")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "beams/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config(args, beams_per_step=1),
+        "cpu_baseline": {"value": v, "unit": "beams/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "beams/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+    return 0
+
+
+def config(args, beams_per_step=None):
+    return {"workload": f"heterogeneous slab phantom {args.grid}^3 @ {args.spacing:g} cm, "
+                        f"{args.field:g}x{args.field:g} cm2 field, gantry U[0,360), 6 MV, 12x48 cones",
+            "grid": args.grid, "spacing_cm": args.spacing, "field_cm": args.field,
+            "beams_per_step": beams_per_step if beams_per_step is not None else args.beams,
+            "l2": "flushed between timed steps (256 MiB write)", "seed": 0}
+
+
+def percentile(xs, q):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    k = (len(xs) - 1) * q
+    lo, hi = int(np.floor(k)), int(np.ceil(k))
+    return xs[lo] + (xs[hi] - xs[lo]) * (k - lo)
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist_init("nccl")
+    from conehead_gb300.conehead import engine
+    eng = engine(local)
+    eng.set_kernel(SETTINGS["energy_weights"])
+    ph = workload(args.grid, args.spacing)
+    N = int(np.prod(ph.size))
+    rho = eng.upload_densities(ph.densities)
+    B = args.beams
+    total = (args.warmup + args.steps) * B
+    beams = [make_beam(beam_seed(rank, i), args.field) for i in range(total)]
+    dblocks = [eng.upload_block(blk.block_values) for _, blk in beams]
+    doses = [torch.empty(ph.size, dtype=torch.float32, device=dev) for _ in range(B)]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream(dev)
+
+    def step_jobs(s):
+        return [eng.job(ph, rho, beams[s * B + i][0], dblocks[s * B + i], SETTINGS, dose=doses[i])
+                for i in range(B)]
+
+    # ---- device-resident batched steps
+    for s in range(args.warmup):
+        eng.run_batch(step_jobs(s))
+    eng.sync()
+    stats = []
+    step_ms = []
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    for s in range(args.warmup, args.warmup + args.steps):
+        jobs = step_jobs(s)
+        flush.fill_(float(s))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        eng.run_batch(jobs)
+        e1.record(st)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        stats.append(eng.stats())
+    torch.cuda.synchronize(dev)
+    barrier()
+    clk = clocks.stop()
+    eng.sync()
+    local_s = sum(step_ms) / 1000.0
+    job_s = max_over_ranks(local_s, dev)
+    value = world * args.steps * B / job_s
+
+    # ---- cone kernel roofline (CUDA events around the gather launch, same stream)
+    cone_ms = statistics.mean(x["ms_cone"] for x in stats)
+    updates = statistics.mean(x["updates"] for x in stats)
+    alg_bytes = B * 2 * 4 * N                     # TERMA read + dose write per beam
+    peaks = {}
+    pk_path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(pk_path):
+        peaks = json.load(open(pk_path))
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg_bytes / (cone_ms * 1e-3) / 1e9
+    traffic = None
+    tr_path = os.path.join(HERE, "profiles", "cone_gather_traffic.json")
+    if os.path.exists(tr_path):
+        tr = json.load(open(tr_path))
+        traffic = tr.get("bytes_per_beam", 0) * B if tr.get("bytes_per_beam") else None
+    props = torch.cuda.get_device_properties(dev)
+    sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    lds_ceiling = props.multi_processor_count * 32 * sm_mhz * 1e6     # one 4-byte LDS lane per update
+    onchip = {"metric": "voxel-direction updates/s", "achieved": updates / (cone_ms * 1e-3),
+              "peak": lds_ceiling, "frac": updates / (cone_ms * 1e-3) / lds_ceiling,
+              "peak_basis": "SMs x 32 shared-memory lanes/clk x median SM clock"}
+
+    # ---- e2e through the C ABI with pinned host buffers
+    e2e = None
+    if rank == 0 or True:
+        h_rho = torch.from_numpy(np.ascontiguousarray(ph.densities)).pin_memory()
+        h_blocks = [torch.from_numpy(np.ascontiguousarray(db.crop.cpu().numpy())).pin_memory()
+                    for db in dblocks[:B]]
+        h_doses = [torch.empty(ph.size, dtype=torch.float32).pin_memory() for _ in range(B)]
+        d_rho = torch.empty_like(rho)
+        d_blocks = [torch.empty_like(db.crop) for db in dblocks[:B]]
+        from conehead_gb300.engine import DeviceBlock
+        e2e_ms = []
+        for s in range(args.warmup + args.steps):
+            flush.fill_(float(s))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            d_rho.copy_(h_rho, non_blocking=True)
+            jobs = []
+            for i in range(B):
+                d_blocks[i].copy_(h_blocks[i], non_blocking=True)
+                db = dblocks[i]
+                jobs.append(eng.job(ph, d_rho, beams[i][0], DeviceBlock(d_blocks[i], db.r0, db.c0, db.full_shape),
+                                    SETTINGS, dose=doses[i]))
+            eng.run_batch(jobs)
+            for i in range(B):
+                h_doses[i].copy_(doses[i], non_blocking=True)
+            e1.record(st)
+            e1.synchronize()
+            if s >= args.warmup:
+                e2e_ms.append(e0.elapsed_time(e1))
+        eng.sync()
+        e2e_s = max_over_ranks(sum(e2e_ms) / 1000.0, dev)
+        h2d = h_rho.numel() * 4 + sum(h.numel() * 4 for h in h_blocks)
+        e2e = {"value": world * args.steps * B / e2e_s, "unit": "beams/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(B * N * 4)}
+
+    # ---- extras: single-beam latency, plain scatter path, CPU baseline (rank 0)
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        lat = []
+        for i in range(args.latency_beams):
+            job = eng.job(ph, rho, beams[i][0], dblocks[i], SETTINGS, dose=doses[0])
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            eng.run(job)
+            eng.sync()
+            lat.append(1000.0 * (time.perf_counter() - t0))
+        extras["single_beam_latency_ms"] = {"p50": percentile(lat, 0.5), "p99": percentile(lat, 0.99),
+                                            "n": len(lat)}
+        extras["single_beam_beams_per_s"] = 1000.0 / statistics.mean(lat)
+        pl = []
+        for i in range(args.plain_beams):
+            job = eng.job(ph, rho, beams[i][0], dblocks[i], SETTINGS, dose=doses[0])
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            eng.run(job, scatter=True)
+            eng.sync()
+            pl.append(time.perf_counter() - t0)
+        extras["plain_gpu_beams_per_s"] = len(pl) / sum(pl)
+        extras["plain_gpu_path"] = "prologue + per-voxel scatter with float32 atomics, one beam per launch"
+        if not args.no_cpu:
+            cv, cores, dt = cpu_oracle_beams(ph, beams[:args.cpu_beams])
+            extras["cpu_baseline"] = {
+                "value": cv, "unit": "beams/s", "cores": cores, "kind": "port",
+                "sample": f"{args.cpu_beams} whole beam(s) of the workload, FP64 oracle "
+                          f"(C++ restatement of conehead's GPU path), OpenMP, {dt:.1f} s"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "beams/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * job_s / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded slab phantom and beams; no dataset)",
+            "config": config(args),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": traffic,
+                         "kernel": "cone_gather_kernel",
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"},
+            "onchip": onchip,
+            "cone_ms_per_step": cone_ms,
+            "updates_per_step": updates,
+            "e2e": e2e,
+            "clocks": clk,
+            "gpu_launches": args.steps * (B + 3),
+        }
+        line.update(extras)
+        print(json.dumps(line))
+    barrier()
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--beams", type=int, default=16, help="beams per step")
+    ap.add_argument("--grid", type=int, default=128)
+    ap.add_argument("--spacing", type=float, default=0.25)
+    ap.add_argument("--field", type=float, default=5.0)
+    ap.add_argument("--latency-beams", type=int, default=20)
+    ap.add_argument("--plain-beams", type=int, default=2)
+    ap.add_argument("--cpu-beams", type=int, default=2)
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args(argv)
+    args.warmup = max(3, args.warmup)      # at least three untimed warm-up steps
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,744 @@
+// Host side of the C ABI declared in include/conehead_gb300.h: plans,
+// stencil preparation, scratch management and launch sequencing.
+//
+// A plan owns the kernel tables, the per-spacing direction stencils and a
+// grow-only scratch arena (TERMA volumes, tile ranges, per-beam launch
+// records).  Caller buffers (densities, block maps, dose) are never
+// allocated or freed here.  Calls are stream ordered and asynchronous;
+// device-side failures (bounded waits that expired, rays parallel to the
+// blocking plane) are reported by ch_plan_sync / ch_plan_stats.
+
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "ch_internal.cuh"
+
+using namespace ch;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+ch_status fail(ch_status st, const std::string& msg) {
+  g_last_error = msg;
+  return st;
+}
+
+#define CH_CUDA(call)                                                                  \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess)                                                             \
+      return fail(e_ == cudaErrorMemoryAllocation ? CH_ERR_OOM : CH_ERR_DEVICE,        \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                 \
+  } while (0)
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <typename T>
+  T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  });
+  return fn;
+}
+
+inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
+
+}  // namespace
+
+struct StencilSet {
+  bool valid = false;
+  float spacing[3] = {0, 0, 0};
+  int cap[3] = {0, 0, 0};
+  int n_dirs = 0;            // unique walks
+  int n_raw = 0;             // theta x phi
+  size_t total_taps = 0;
+  DevBuf tap_base, tap_len, taps, offs, tvals, chunk_base, n_chunks, chunk_start, dirs;
+  DevBuf raw_dirs;           // float [n_theta*n_phi][3] as the device computed them
+};
+
+struct ch_plan {
+  int device = 0;
+  int n_sm = 0;
+  bool have_kernel = false;
+  int n_phi = 0, n_r = 0, n_theta = 0;
+  DevBuf K, theta, phi;
+  StencilSet st;
+  // scratch
+  DevBuf T, aabb, counters, ranges, cone_beams, range_beams;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaStream_t last_stream = nullptr;
+  ch_stats stats{};
+  bool stats_pending = false;
+  bool timed = false;
+  ~ch_plan() {
+    for (DevBuf* b : {&K, &theta, &phi, &T, &aabb, &counters, &ranges, &cone_beams, &range_beams, &st.tap_base,
+                      &st.tap_len, &st.taps, &st.offs, &st.tvals, &st.chunk_base, &st.n_chunks, &st.chunk_start,
+                      &st.dirs, &st.raw_dirs})
+      b->release();
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+};
+
+namespace {
+
+// ------------------------------------------------------------ stencils --
+ch_status build_stencils(ch_plan* P, const float* spacing, const int* cap, cudaStream_t s) {
+  StencilSet& S = P->st;
+  const int n_raw = P->n_theta * P->n_phi;
+  const int max_len = cap[0] + cap[1] + cap[2] + 2;
+  DevBuf off, tv, dk, len;
+  CH_CUDA(off.ensure((size_t)n_raw * max_len * sizeof(short4)));
+  CH_CUDA(tv.ensure((size_t)n_raw * max_len * sizeof(float)));
+  CH_CUDA(dk.ensure((size_t)n_raw * max_len * sizeof(float)));
+  CH_CUDA(len.ensure((size_t)n_raw * sizeof(int)));
+  CH_CUDA(S.raw_dirs.ensure((size_t)n_raw * 3 * sizeof(float)));
+  launch_stencil(P->theta.as<float>(), P->n_theta, P->phi.as<float>(), P->n_phi, P->K.as<double>(), P->n_r,
+                 spacing, cap, max_len, off.as<short4>(), tv.as<float>(), dk.as<float>(), len.as<int>(),
+                 S.raw_dirs.as<float>(), s);
+  CH_CUDA(cudaGetLastError());
+  std::vector<short4> h_off((size_t)n_raw * max_len);
+  std::vector<float> h_t((size_t)n_raw * max_len), h_dk((size_t)n_raw * max_len), h_dir((size_t)n_raw * 3);
+  std::vector<int> h_len(n_raw);
+  CH_CUDA(cudaMemcpyAsync(h_off.data(), off.p, h_off.size() * sizeof(short4), cudaMemcpyDeviceToHost, s));
+  CH_CUDA(cudaMemcpyAsync(h_t.data(), tv.p, h_t.size() * sizeof(float), cudaMemcpyDeviceToHost, s));
+  CH_CUDA(cudaMemcpyAsync(h_dk.data(), dk.p, h_dk.size() * sizeof(float), cudaMemcpyDeviceToHost, s));
+  CH_CUDA(cudaMemcpyAsync(h_len.data(), len.p, h_len.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+  CH_CUDA(cudaMemcpyAsync(h_dir.data(), S.raw_dirs.p, h_dir.size() * sizeof(float), cudaMemcpyDeviceToHost, s));
+  CH_CUDA(cudaStreamSynchronize(s));
+  off.release();
+  tv.release();
+  dk.release();
+  len.release();
+
+  // merge identical walks (the 12 phi = 180 deg directions are one walk)
+  struct Key {
+    std::vector<short4> o;
+    std::vector<float> w;
+    bool operator<(const Key& k) const {
+      if (o.size() != k.o.size()) return o.size() < k.o.size();
+      int c = std::memcmp(o.data(), k.o.data(), o.size() * sizeof(short4));
+      if (c) return c < 0;
+      return std::memcmp(w.data(), k.w.data(), w.size() * sizeof(float)) < 0;
+    }
+  };
+  std::map<Key, int> seen;
+  std::vector<int> uniq_first, mult;
+  for (int d = 0; d < n_raw; ++d) {
+    const int L = h_len[d];
+    if (L <= 0) continue;
+    Key k;
+    k.o.assign(h_off.begin() + (size_t)d * max_len, h_off.begin() + (size_t)d * max_len + L);
+    k.w.assign(h_dk.begin() + (size_t)d * max_len, h_dk.begin() + (size_t)d * max_len + L);
+    auto it = seen.find(k);
+    if (it == seen.end()) {
+      seen.emplace(std::move(k), (int)uniq_first.size());
+      uniq_first.push_back(d);
+      mult.push_back(1);
+    } else {
+      mult[it->second] += 1;
+    }
+  }
+  const int U = (int)uniq_first.size();
+  std::vector<int> tap_base(U), tap_len(U), chunk_base(U), n_chunks(U), chunk_start;
+  std::vector<int2> taps;
+  std::vector<short4> offs;
+  std::vector<float> tvals, dirs((size_t)U * 3);
+  for (int u = 0; u < U; ++u) {
+    const int d = uniq_first[u], L = h_len[d];
+    const short4* o = &h_off[(size_t)d * max_len];
+    tap_base[u] = (int)taps.size();
+    tap_len[u] = L;
+    for (int k = 0; k < 3; ++k) dirs[(size_t)u * 3 + k] = h_dir[(size_t)d * 3 + k];
+    for (int m = 0; m < L; ++m) {
+      const int toff = ((int)o[m].x * WY + (int)o[m].y) * WZ + (int)o[m].z;
+      const float w = h_dk[(size_t)d * max_len + m] * (float)mult[u];
+      int wb;
+      std::memcpy(&wb, &w, 4);
+      taps.push_back(make_int2(toff, wb));
+      offs.push_back(o[m]);
+      tvals.push_back(h_t[(size_t)d * max_len + m]);
+    }
+    // greedy chunks: the sources of a chunk must fit the window spans
+    chunk_base[u] = (int)chunk_start.size();
+    int a = 0;
+    while (a < L) {
+      int b = a;
+      while (b + 1 < L && std::abs(o[b + 1].x - o[a].x) <= SPAN_X && std::abs(o[b + 1].y - o[a].y) <= SPAN_Y &&
+             std::abs(o[b + 1].z - o[a].z) <= SPAN_Z)
+        ++b;
+      chunk_start.push_back(a);
+      a = b + 1;
+    }
+    n_chunks[u] = (int)chunk_start.size() - chunk_base[u];
+  }
+  auto up = [&](DevBuf& b, const void* h, size_t n) -> cudaError_t {
+    cudaError_t e = b.ensure(std::max<size_t>(n, 16));
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(b.p, h, n, cudaMemcpyHostToDevice, s);
+  };
+  CH_CUDA(up(S.tap_base, tap_base.data(), tap_base.size() * sizeof(int)));
+  CH_CUDA(up(S.tap_len, tap_len.data(), tap_len.size() * sizeof(int)));
+  CH_CUDA(up(S.taps, taps.data(), taps.size() * sizeof(int2)));
+  CH_CUDA(up(S.offs, offs.data(), offs.size() * sizeof(short4)));
+  CH_CUDA(up(S.tvals, tvals.data(), tvals.size() * sizeof(float)));
+  CH_CUDA(up(S.chunk_base, chunk_base.data(), chunk_base.size() * sizeof(int)));
+  CH_CUDA(up(S.n_chunks, n_chunks.data(), n_chunks.size() * sizeof(int)));
+  CH_CUDA(up(S.chunk_start, chunk_start.data(), chunk_start.size() * sizeof(int)));
+  CH_CUDA(up(S.dirs, dirs.data(), dirs.size() * sizeof(float)));
+  CH_CUDA(cudaStreamSynchronize(s));
+  S.valid = true;
+  S.n_dirs = U;
+  S.n_raw = n_raw;
+  S.total_taps = taps.size();
+  for (int k = 0; k < 3; ++k) {
+    S.spacing[k] = spacing[k];
+    S.cap[k] = cap[k];
+  }
+  return CH_OK;
+}
+
+ch_status ensure_stencils(ch_plan* P, const float* spacing, const int* dims, cudaStream_t s) {
+  StencilSet& S = P->st;
+  bool ok = S.valid;
+  for (int k = 0; k < 3 && ok; ++k)
+    ok = S.spacing[k] == spacing[k] && S.cap[k] >= dims[k];
+  if (ok) return CH_OK;
+  int cap[3];
+  for (int k = 0; k < 3; ++k) cap[k] = std::max(dims[k], S.valid && S.spacing[k] == spacing[k] ? S.cap[k] : 0);
+  return build_stencils(P, spacing, cap, s);
+}
+
+ConeDirs cone_dirs(const ch_plan* P) {
+  const StencilSet& S = P->st;
+  ConeDirs D;
+  D.n_dirs = S.n_dirs;
+  D.tap_base = S.tap_base.as<int>();
+  D.tap_len = S.tap_len.as<int>();
+  D.taps = S.taps.as<int2>();
+  D.offs = S.offs.as<short4>();
+  D.tvals = S.tvals.as<float>();
+  D.chunk_base = S.chunk_base.as<int>();
+  D.n_chunks = S.n_chunks.as<int>();
+  D.chunk_start = S.chunk_start.as<int>();
+  D.dirs = S.dirs.as<float>();
+  return D;
+}
+
+// --------------------------------------------------------- validation --
+ch_status check_grid(const ch_grid* g) {
+  if (!g) return fail(CH_ERR_INVALID_ARG, "grid is NULL");
+  for (int k = 0; k < 3; ++k) {
+    if (g->n[k] <= 0 || g->n[k] > 4096) return fail(CH_ERR_INVALID_ARG, "grid dimension out of range (1..4096)");
+    if (!(g->spacing[k] > 0.0f) || !std::isfinite(g->spacing[k]))
+      return fail(CH_ERR_INVALID_ARG, "grid spacing must be positive");
+    if (!std::isfinite(g->origin[k])) return fail(CH_ERR_INVALID_ARG, "grid origin must be finite");
+  }
+  return CH_OK;
+}
+
+ch_status check_beam(const ch_beam* b) {
+  if (!b) return fail(CH_ERR_INVALID_ARG, "beam is NULL");
+  if (!b->block || b->block_rows <= 0 || b->block_cols <= 0)
+    return fail(CH_ERR_INVALID_ARG, "beam block map missing");
+  if (b->full_rows < b->block_r0 + b->block_rows || b->full_cols < b->block_c0 + b->block_cols ||
+      b->block_r0 < 0 || b->block_c0 < 0)
+    return fail(CH_ERR_INVALID_ARG, "block crop lies outside the full map");
+  const double nn = b->vy[0] * b->vy[0] + b->vy[1] * b->vy[1] + b->vy[2] * b->vy[2];
+  if (!(nn > 0.0)) return fail(CH_ERR_INVALID_ARG, "beam v_y is zero");
+  return CH_OK;
+}
+
+ch_status check_settings(const ch_settings* s) {
+  if (!s) return fail(CH_ERR_INVALID_ARG, "settings is NULL");
+  if (s->samples < 1 || s->samples > 16) return fail(CH_ERR_INVALID_ARG, "fluenceResampling out of range (1..16)");
+  if (s->n_energy < 0 || s->n_energy > CH_MAX_ENERGY) return fail(CH_ERR_INVALID_ARG, "too many energy bins");
+  return CH_OK;
+}
+
+// ------------------------------------------------------ beam prep --
+BeamDev make_beam(const ch_beam& in, const ch_grid& g) {
+  BeamDev b{};
+  for (int k = 0; k < 3; ++k) {
+    b.src[k] = in.src[k];
+    b.vy[k] = in.vy[k];
+    b.m0[k] = in.xform[k];
+    b.m2[k] = in.xform[6 + k];
+    b.srcf[k] = (float)in.src[k];
+    b.vyf[k] = (float)in.vy[k];
+    b.m0f[k] = (float)in.xform[k];
+    b.m2f[k] = (float)in.xform[6 + k];
+  }
+  // v_y . w with w = float32(src), reference evaluation order
+  const double w0 = b.srcf[0], w1 = b.srcf[1], w2 = b.srcf[2];
+  b.vyw = (b.vy[0] * w0 + b.vy[1] * w1) + b.vy[2] * w2;
+  b.vywf = (b.vyf[0] * b.srcf[0] + b.vyf[1] * b.srcf[1]) + b.vyf[2] * b.srcf[2];
+  b.geom_f32 = in.geom_f32;
+  const double nS = b.vy[0] * b.src[0] + b.vy[1] * b.src[1] + b.vy[2] * b.src[2];
+  const double m0S = b.m0[0] * b.src[0] + b.m0[1] * b.src[1] + b.m0[2] * b.src[2];
+  const double m2S = b.m2[0] * b.src[0] + b.m2[1] * b.src[1] + b.m2[2] * b.src[2];
+  b.a_nS = (float)nS;
+  b.a_m0S = (float)m0S;
+  b.a_m2S = (float)m2S;
+  b.a_K = (float)(-b.vyw);
+  b.a_c0 = (float)(b.m0[0] * w0 + b.m0[1] * w1 + b.m0[2] * w2);
+  b.a_c2 = (float)(b.m2[0] * w0 + b.m2[1] * w1 + b.m2[2] * w2);
+  // map rows [r0, r1] are read for x in [(r0 - 1999)/100, (r1 - 1998)/100);
+  // cell 0 wraps to the last row, i.e. x in [-20, -19.99)
+  const int r0 = in.block_r0, r1 = in.block_r0 + in.block_rows - 1;
+  const int c0 = in.block_c0, c1 = in.block_c0 + in.block_cols - 1;
+  double xlo = (r0 - 1999) / 100.0, xhi = (r1 - 1998) / 100.0;
+  double zlo = (c0 - 1999) / 100.0, zhi = (c1 - 1998) / 100.0;
+  if (r1 == in.full_rows - 1) xlo = std::min(xlo, -20.0);
+  if (c1 == in.full_cols - 1) zlo = std::min(zlo, -20.0);
+  b.cx_lo = (float)std::max(xlo, -20.0);
+  b.cx_hi = (float)std::min(xhi, 20.0);
+  b.cz_lo = (float)std::max(zlo, -20.0);
+  b.cz_hi = (float)std::min(zhi, 20.0);
+  const float smax = std::max(g.spacing[0], std::max(g.spacing[1], g.spacing[2]));
+  b.cull_margin_k = 1.25f * 0.8660254f * smax;
+  b.cull_enable = (-nS > 0.0 && b.cx_lo <= b.cx_hi && b.cz_lo <= b.cz_hi) ? 1 : 0;
+  b.block = in.block;
+  b.brows = in.block_rows;
+  b.bcols = in.block_cols;
+  b.br0 = in.block_r0;
+  b.bc0 = in.block_c0;
+  b.full_rows = in.full_rows;
+  b.full_cols = in.full_cols;
+  b.sad = in.sad;
+  b.sad_f32 = in.sad_f32;
+  return b;
+}
+
+SettingsDev make_settings(const ch_settings& s) {
+  SettingsDev d{};
+  d.sPri = (float)s.sPri;
+  d.sAnn = (float)s.sAnn;
+  d.zAnn = (float)s.zAnn;
+  d.rInner = (float)s.rInner;
+  d.rOuter = (float)s.rOuter;
+  d.zExp = (float)s.zExp;
+  d.sExp = (float)s.sExp;
+  d.kExp = (float)s.kExp;
+  d.softRatio = (float)s.softRatio;
+  d.softLimit = (float)s.softLimit;
+  d.hornRatio = (float)s.hornRatio;
+  d.samples = s.samples;
+  d.n_energy = s.n_energy;
+  for (int i = 0; i < s.n_energy; ++i) {
+    d.E[i] = s.E[i];
+    d.w[i] = s.w[i];
+    d.mu[i] = s.mu[i];
+  }
+  return d;
+}
+
+// Frustum planes a.(p - S) <= e bounding every voxel centre whose samples
+// can project into the open block region (widened by half a voxel).
+void make_planes(const ch_beam& in, const ch_grid& g, const BeamDev& b, RangeBeam& R) {
+  R.n_planes = 0;
+  const double* n = in.vy;
+  const double* S = in.src;
+  const double D = -(n[0] * S[0] + n[1] * S[1] + n[2] * S[2]);
+  if (!(D > 0.0)) return;
+  // every grid point (widened by a voxel) must lie in front of the source
+  for (int c = 0; c < 8; ++c) {
+    double p[3];
+    for (int k = 0; k < 3; ++k) {
+      const int hi = (c >> k) & 1;
+      p[k] = (double)g.origin[k] + (hi ? (g.n[k] - 0.5) * g.spacing[k] : -1.5 * g.spacing[k]);
+    }
+    const double depth = n[0] * (p[0] - S[0]) + n[1] * (p[1] - S[1]) + n[2] * (p[2] - S[2]);
+    if (!(depth > 0.05 * D)) return;
+  }
+  const double m0S = b.m0[0] * S[0] + b.m0[1] * S[1] + b.m0[2] * S[2];
+  const double m2S = b.m2[0] * S[0] + b.m2[1] * S[1] + b.m2[2] * S[2];
+  const double pad = 0.02;  // cm, covers cell-edge and float32 slack
+  struct Pl { double a[3]; };
+  std::vector<Pl> pls;
+  auto add = [&](const double* m, double sgn, double X, double mS) {
+    Pl p;
+    // sgn = +1: x_b >= X  ->  ((X - mS) n - D m) . r <= 0
+    // sgn = -1: x_b <= X  ->  (D m - (X - mS) n) . r <= 0
+    for (int k = 0; k < 3; ++k) p.a[k] = sgn * ((X - mS) * n[k] - D * m[k]);
+    pls.push_back(p);
+  };
+  add(b.m0, +1.0, b.cx_lo - pad, m0S);
+  add(b.m0, -1.0, b.cx_hi + pad, m0S);
+  add(b.m2, +1.0, b.cz_lo - pad, m2S);
+  add(b.m2, -1.0, b.cz_hi + pad, m2S);
+  for (size_t j = 0; j < pls.size() && j < 4; ++j) {
+    double e = 0.0, aos = 0.0, scale = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      e += std::fabs(pls[j].a[k]) * g.spacing[k] * 0.5;
+      aos += pls[j].a[k] * ((double)g.origin[k] - S[k]);
+      scale = std::max(scale, std::fabs(pls[j].a[k]));
+    }
+    if (!(scale > 0.0)) continue;
+    // normalise so float32 in the range kernel keeps its precision
+    for (int k = 0; k < 3; ++k) R.pa[R.n_planes][k] = (float)(pls[j].a[k] / scale);
+    R.pk0[R.n_planes] = (float)((aos - e) / scale - 1e-3);
+    ++R.n_planes;
+  }
+}
+
+struct BeamJob {
+  GridDev g;
+  BeamDev b;
+  SettingsDev s;
+  const float* rho;
+  float* dose;
+  size_t t_off;        // float offset in the T arena
+  size_t r_off;        // uint32 offset in the ranges arena
+  int ntile[3];
+  int n_tiles;
+  int n_units;
+  ch_grid grid;
+  ch_beam beam;
+};
+
+ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, const int* swap_xy,
+              const ch_beam* beams, const ch_settings* settings, float* const* dose, const ch_intermediates* inter,
+              bool scatter, cudaStream_t s) {
+  if (!P) return fail(CH_ERR_INVALID_ARG, "plan is NULL");
+  if (!P->have_kernel) return fail(CH_ERR_NO_KERNEL, "ch_plan_set_kernel has not been called");
+  if (n <= 0) return fail(CH_ERR_INVALID_ARG, "no beams");
+  CH_CUDA(cudaSetDevice(P->device));
+  std::vector<BeamJob> jobs(n);
+  int dims[3] = {0, 0, 0};
+  for (int i = 0; i < n; ++i) {
+    ch_status st;
+    if ((st = check_grid(&grids[i])) != CH_OK) return st;
+    if ((st = check_beam(&beams[i])) != CH_OK) return st;
+    if ((st = check_settings(&settings[i])) != CH_OK) return st;
+    if (!rho || !rho[i] || !dose || !dose[i]) return fail(CH_ERR_INVALID_ARG, "density or dose pointer is NULL");
+    const int sw = swap_xy ? swap_xy[i] : 0;
+    if (sw && grids[i].n[0] != grids[i].n[1])
+      return fail(CH_ERR_INVALID_ARG, "swap_xy needs a square x/y grid");
+    for (int k = 0; k < 3; ++k) {
+      if (grids[i].spacing[k] != grids[0].spacing[k])
+        return fail(CH_ERR_INVALID_ARG, "all beams of one call must share the voxel spacing");
+      dims[k] = std::max(dims[k], grids[i].n[k]);
+    }
+  }
+  ch_status st = ensure_stencils(P, grids[0].spacing, dims, s);
+  if (st != CH_OK) return st;
+  const int U = P->st.n_dirs;
+  const int n_groups = (U + DIR_GROUP - 1) / DIR_GROUP;
+  size_t t_total = 0, r_total = 0;
+  int total_units = 0, max_tiles = 0;
+  for (int i = 0; i < n; ++i) {
+    BeamJob& J = jobs[i];
+    J.grid = grids[i];
+    J.beam = beams[i];
+    for (int k = 0; k < 3; ++k) {
+      J.g.n[k] = grids[i].n[k];
+      J.g.origin[k] = grids[i].origin[k];
+      J.g.spacing[k] = grids[i].spacing[k];
+    }
+    J.g.zp = round_up(grids[i].n[2], 4);
+    J.g.swap_xy = swap_xy ? swap_xy[i] : 0;
+    J.b = make_beam(beams[i], grids[i]);
+    J.s = make_settings(settings[i]);
+    J.rho = rho[i];
+    J.dose = dose[i];
+    J.t_off = t_total;
+    t_total += (size_t)J.g.n[0] * J.g.n[1] * J.g.zp;
+    t_total = (t_total + 63) / 64 * 64;
+    J.ntile[0] = (J.g.n[0] + TX - 1) / TX;
+    J.ntile[1] = (J.g.n[1] + TY - 1) / TY;
+    J.ntile[2] = (J.g.n[2] + TZ - 1) / TZ;
+    J.n_tiles = J.ntile[0] * J.ntile[1] * J.ntile[2];
+    J.n_units = J.n_tiles * n_groups;
+    J.r_off = r_total;
+    r_total += (size_t)J.n_tiles * U;
+    total_units += J.n_units;
+    max_tiles = std::max(max_tiles, J.n_tiles);
+  }
+  CH_CUDA(P->T.ensure(t_total * sizeof(float)));
+  CH_CUDA(P->aabb.ensure((size_t)n * 8 * sizeof(int)));
+  CH_CUDA(P->counters.ensure(8 * sizeof(int)));
+  CH_CUDA(P->ranges.ensure(std::max<size_t>(r_total, 1) * sizeof(uint32_t)));
+  CH_CUDA(P->cone_beams.ensure((size_t)n * sizeof(ConeBeam)));
+  CH_CUDA(P->range_beams.ensure((size_t)n * sizeof(RangeBeam)));
+  int* counters = P->counters.as<int>();
+  int* flags = counters + 1;
+  unsigned long long* updates = reinterpret_cast<unsigned long long*>(counters + 2);
+
+  for (auto& e : P->ev)
+    if (!e) CH_CUDA(cudaEventCreate(&e));
+  CH_CUDA(cudaEventRecord(P->ev[0], s));
+  launch_init_scratch(P->aabb.as<int>(), n, counters, s);
+  for (int i = 0; i < n; ++i) {
+    BeamJob& J = jobs[i];
+    Inter in{};
+    int all = 0;
+    if (inter) {
+      in.blocked = inter->blocked;
+      in.d_eff = inter->d_eff;
+      in.oad = inter->oad;
+      in.fluence = inter->fluence;
+      in.f_soften = inter->f_soften;
+      in.f_horn = inter->f_horn;
+      in.terma = inter->terma;
+      all = (in.d_eff || in.oad || in.fluence || in.f_soften || in.f_horn) ? 1 : 0;
+    }
+    launch_prologue(J.rho, J.g, J.b, J.s, P->T.as<float>() + J.t_off, in, all, P->aabb.as<int>() + 8 * i, flags,
+                    s);
+    CH_CUDA(cudaGetLastError());
+  }
+  CH_CUDA(cudaEventRecord(P->ev[1], s));
+  for (int i = 0; i < n; ++i)
+    CH_CUDA(cudaMemsetAsync(jobs[i].dose, 0, (size_t)jobs[i].g.n[0] * jobs[i].g.n[1] * jobs[i].g.n[2] * 4, s));
+  const ConeDirs D = cone_dirs(P);
+  if (scatter) {
+    for (int i = 0; i < n; ++i) {
+      launch_scatter(P->T.as<float>() + jobs[i].t_off, jobs[i].g.n, jobs[i].g.zp, U, D.tap_base, D.tap_len, D.offs,
+                     D.taps, jobs[i].dose, s);
+      CH_CUDA(cudaGetLastError());
+    }
+    CH_CUDA(cudaEventRecord(P->ev[2], s));
+    CH_CUDA(cudaEventRecord(P->ev[3], s));
+    P->stats = ch_stats{};
+    P->stats.n_unique_dirs = U;
+    P->stats_pending = true;
+    P->last_stream = s;
+    return CH_OK;
+  }
+  // per-beam launch records
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled is not available from the driver");
+  std::vector<ConeBeam> cb(n);
+  std::vector<RangeBeam> rb(n);
+  int unit_begin = 0;
+  for (int i = 0; i < n; ++i) {
+    const BeamJob& J = jobs[i];
+    ConeBeam& C = cb[i];
+    std::memset(&C, 0, sizeof(C));
+    cuuint64_t gdim[3] = {(cuuint64_t)J.g.n[2], (cuuint64_t)J.g.n[1], (cuuint64_t)J.g.n[0]};
+    cuuint64_t gstride[2] = {(cuuint64_t)J.g.zp * 4, (cuuint64_t)J.g.zp * J.g.n[1] * 4};
+    cuuint32_t box[3] = {(cuuint32_t)WZ, (cuuint32_t)BOX_Y, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = enc(&C.tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)(P->T.as<float>() + J.t_off), gdim, gstride,
+                     box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    C.dose = J.dose;
+    C.ranges = P->ranges.as<uint32_t>() + J.r_off;
+    for (int k = 0; k < 3; ++k) {
+      C.n[k] = J.g.n[k];
+      C.ntile[k] = J.ntile[k];
+    }
+    C.n_tiles = J.n_tiles;
+    C.unit_begin = unit_begin;
+    C.n_units = J.n_units;
+    unit_begin += J.n_units;
+    RangeBeam& R = rb[i];
+    std::memset(&R, 0, sizeof(R));
+    for (int k = 0; k < 3; ++k) {
+      R.n[k] = J.g.n[k];
+      R.ntile[k] = J.ntile[k];
+      R.origin[k] = J.g.origin[k];
+      R.spacing[k] = J.g.spacing[k];
+    }
+    R.n_tiles = J.n_tiles;
+    make_planes(J.beam, J.grid, J.b, R);
+    R.aabb = P->aabb.as<int>() + 8 * i;
+    R.ranges = P->ranges.as<uint32_t>() + J.r_off;
+  }
+  CH_CUDA(cudaMemcpyAsync(P->cone_beams.p, cb.data(), n * sizeof(ConeBeam), cudaMemcpyHostToDevice, s));
+  CH_CUDA(cudaMemcpyAsync(P->range_beams.p, rb.data(), n * sizeof(RangeBeam), cudaMemcpyHostToDevice, s));
+  launch_range(P->range_beams.as<RangeBeam>(), n, max_tiles, D, s);
+  CH_CUDA(cudaGetLastError());
+  CH_CUDA(cudaEventRecord(P->ev[2], s));
+  launch_gather(P->cone_beams.as<ConeBeam>(), n, D, total_units, P->n_sm, counters, updates, flags, s);
+  CH_CUDA(cudaGetLastError());
+  CH_CUDA(cudaEventRecord(P->ev[3], s));
+  P->stats = ch_stats{};
+  P->stats.n_unique_dirs = U;
+  P->stats.n_units = total_units;
+  P->stats_pending = true;
+  P->last_stream = s;
+  return CH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+ch_status ch_plan_create(ch_plan** plan, int device) {
+  if (!plan) return fail(CH_ERR_INVALID_ARG, "plan out-pointer is NULL");
+  *plan = nullptr;
+  int count = 0;
+  CH_CUDA(cudaGetDeviceCount(&count));
+  if (device < 0 || device >= count) return fail(CH_ERR_INVALID_ARG, "no such CUDA device");
+  CH_CUDA(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  CH_CUDA(cudaGetDeviceProperties(&prop, device));
+  if (prop.major < 10) return fail(CH_ERR_DEVICE, "conehead_gb300 needs a Blackwell (sm_10x) GPU");
+  CH_CUDA(setup_cone_kernel());
+  upload_unit_partials();
+  CH_CUDA(cudaGetLastError());
+  ch_plan* P = new ch_plan();
+  P->device = device;
+  P->n_sm = prop.multiProcessorCount;
+  *plan = P;
+  return CH_OK;
+}
+
+void ch_plan_destroy(ch_plan* plan) {
+  if (!plan) return;
+  cudaSetDevice(plan->device);
+  delete plan;
+}
+
+ch_status ch_plan_set_kernel(ch_plan* P, const ch_kernel* k) {
+  if (!P || !k || !k->cum || !k->theta || !k->phi) return fail(CH_ERR_INVALID_ARG, "kernel tables missing");
+  if (k->n_phi <= 0 || k->n_r < 2 || k->n_theta <= 0 || k->n_phi > 1024 || k->n_theta > 1024)
+    return fail(CH_ERR_INVALID_ARG, "kernel table sizes out of range");
+  if (k->n_r < 5996) return fail(CH_ERR_INVALID_ARG, "kernel table needs 5996 radial samples (0.05..60 cm)");
+  CH_CUDA(cudaSetDevice(P->device));
+  CH_CUDA(P->K.ensure((size_t)k->n_phi * k->n_r * sizeof(double)));
+  CH_CUDA(P->theta.ensure((size_t)k->n_theta * sizeof(float)));
+  CH_CUDA(P->phi.ensure((size_t)k->n_phi * sizeof(float)));
+  CH_CUDA(cudaMemcpy(P->K.p, k->cum, (size_t)k->n_phi * k->n_r * sizeof(double), cudaMemcpyHostToDevice));
+  CH_CUDA(cudaMemcpy(P->theta.p, k->theta, (size_t)k->n_theta * sizeof(float), cudaMemcpyHostToDevice));
+  CH_CUDA(cudaMemcpy(P->phi.p, k->phi, (size_t)k->n_phi * sizeof(float), cudaMemcpyHostToDevice));
+  P->n_phi = k->n_phi;
+  P->n_r = k->n_r;
+  P->n_theta = k->n_theta;
+  P->have_kernel = true;
+  P->st.valid = false;
+  return CH_OK;
+}
+
+ch_status ch_dose(ch_plan* P, const ch_grid* grid, const float* rho, int swap_xy, const ch_beam* beam,
+                  const ch_settings* settings, float* dose, void* stream) {
+  return run(P, 1, grid, &rho, &swap_xy, beam, settings, &dose, nullptr, false, (cudaStream_t)stream);
+}
+
+ch_status ch_dose_ex(ch_plan* P, const ch_grid* grid, const float* rho, int swap_xy, const ch_beam* beam,
+                     const ch_settings* settings, float* dose, const ch_intermediates* inter, void* stream) {
+  return run(P, 1, grid, &rho, &swap_xy, beam, settings, &dose, inter, false, (cudaStream_t)stream);
+}
+
+ch_status ch_dose_batch(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, const int* swap_xy,
+                        const ch_beam* beams, const ch_settings* settings, float* const* dose, void* stream) {
+  if (!grids || !beams || !settings) return fail(CH_ERR_INVALID_ARG, "batch arrays missing");
+  return run(P, n, grids, rho, swap_xy, beams, settings, dose, nullptr, false, (cudaStream_t)stream);
+}
+
+ch_status ch_dose_scatter(ch_plan* P, const ch_grid* grid, const float* rho, int swap_xy, const ch_beam* beam,
+                          const ch_settings* settings, float* dose, void* stream) {
+  return run(P, 1, grid, &rho, &swap_xy, beam, settings, &dose, nullptr, true, (cudaStream_t)stream);
+}
+
+ch_status ch_dda_trace(const ch_grid* grid, int n_rays, const int* starts, const float* dirs, int cap, int* vox,
+                       float* t, int* len, void* stream) {
+  ch_status st = check_grid(grid);
+  if (st != CH_OK) return st;
+  if (n_rays <= 0 || cap < 0 || !starts || !dirs || !len || (cap > 0 && (!vox || !t)))
+    return fail(CH_ERR_INVALID_ARG, "bad DDA trace arguments");
+  launch_dda_trace(grid->n, grid->spacing, n_rays, starts, dirs, cap, vox, t, len, (cudaStream_t)stream);
+  CH_CUDA(cudaGetLastError());
+  return CH_OK;
+}
+
+ch_status ch_cone_directions(ch_plan* P, float* out, void* stream) {
+  if (!P || !out) return fail(CH_ERR_INVALID_ARG, "plan or output is NULL");
+  if (!P->have_kernel) return fail(CH_ERR_NO_KERNEL, "ch_plan_set_kernel has not been called");
+  if (!P->st.valid) {
+    const float sp[3] = {1.0f, 1.0f, 1.0f};
+    const int dims[3] = {2, 2, 2};
+    ch_status st = ensure_stencils(P, sp, dims, (cudaStream_t)stream);
+    if (st != CH_OK) return st;
+  }
+  CH_CUDA(cudaMemcpyAsync(out, P->st.raw_dirs.p, (size_t)P->st.n_raw * 3 * sizeof(float),
+                          cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+  return CH_OK;
+}
+
+ch_status ch_plan_sync(ch_plan* P, void* stream) {
+  if (!P) return fail(CH_ERR_INVALID_ARG, "plan is NULL");
+  CH_CUDA(cudaSetDevice(P->device));
+  CH_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  if (!P->counters.p) return CH_OK;
+  int c[4];
+  CH_CUDA(cudaMemcpy(c, P->counters.p, sizeof(c), cudaMemcpyDeviceToHost));
+  const int flags = c[1];
+  if (flags & FLAG_TIMEOUT) return fail(CH_ERR_TIMEOUT, "a bounded device wait expired in the cone stage");
+  if (flags & FLAG_PARALLEL_RAY) return fail(CH_ERR_PARALLEL_RAY, "no intersection or line is within plane");
+  return CH_OK;
+}
+
+ch_status ch_plan_stats(ch_plan* P, ch_stats* out) {
+  if (!P || !out) return fail(CH_ERR_INVALID_ARG, "plan or output is NULL");
+  CH_CUDA(cudaSetDevice(P->device));
+  if (P->stats_pending) {
+    CH_CUDA(cudaEventSynchronize(P->ev[3]));
+    CH_CUDA(cudaEventElapsedTime(&P->stats.ms_prologue, P->ev[0], P->ev[1]));
+    CH_CUDA(cudaEventElapsedTime(&P->stats.ms_range, P->ev[1], P->ev[2]));
+    CH_CUDA(cudaEventElapsedTime(&P->stats.ms_cone, P->ev[2], P->ev[3]));
+    int c[4];
+    CH_CUDA(cudaMemcpy(c, P->counters.p, sizeof(c), cudaMemcpyDeviceToHost));
+    unsigned long long u;
+    std::memcpy(&u, c + 2, sizeof(u));
+    P->stats.updates = (double)u;
+    P->stats_pending = false;
+  }
+  *out = P->stats;
+  return CH_OK;
+}
+
+const char* ch_status_string(ch_status s) {
+  switch (s) {
+    case CH_OK: return "ok";
+    case CH_ERR_INVALID_ARG: return "invalid argument";
+    case CH_ERR_OOM: return "out of device memory";
+    case CH_ERR_DEVICE: return "CUDA error";
+    case CH_ERR_TIMEOUT: return "device wait timed out";
+    case CH_ERR_PARALLEL_RAY: return "ray parallel to the blocking plane";
+    case CH_ERR_NO_KERNEL: return "kernel tables not set";
+  }
+  return "unknown status";
+}
+
+const char* ch_last_error(void) { return g_last_error.c_str(); }
+
+int ch_version(void) { return 1; }
+
+}  // extern "C"

@@ -1,0 +1,178 @@
+// Internal definitions shared by the conehead_gb300 CUDA sources.
+#pragma once
+
+#include <cstdint>
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "../../include/conehead_gb300.h"
+
+namespace ch {
+
+// ------------------------------------------------------------------ sizes --
+// Cone gather tile: 32 (z, lanes) x 16 (y, per-thread run) x 8 (x, warps).
+constexpr int TZ = 32, TY = 16, TX = 8;
+constexpr int TILE_VOX = TZ * TY * TX;
+// Shared-memory window per pipeline slot; a chunk of taps may span at most
+// SPAN_Z/SPAN_Y/SPAN_X voxels along z/y/x (z also absorbs the 4-float TMA
+// alignment of the window origin).
+constexpr int WZ = 48, WY = 24, WX = 16;
+constexpr int SPAN_Z = WZ - TZ - 3;   // 13
+constexpr int SPAN_Y = WY - TY;       // 8
+constexpr int SPAN_X = WX - TX;       // 8
+constexpr int WIN_FLOATS = WZ * WY * WX;
+constexpr int BOX_Y = 8;              // TMA box: 48 (z) x 8 (y) x 1 (x) floats
+constexpr int BOX_BYTES = WZ * BOX_Y * 4;
+constexpr int N_SLOTS = 2;
+constexpr int CONE_CONSUMER_WARPS = TX;
+constexpr int CONE_THREADS = (CONE_CONSUMER_WARPS + 1) * 32;
+constexpr int DIR_GROUP = 16;         // unique directions per work unit
+
+// Bounded device-side waits (iterations of try_wait / spin).
+constexpr long long WAIT_LIMIT = 1ll << 26;
+
+// device error flags (bit mask in Plan::d_flags[0])
+constexpr int FLAG_TIMEOUT = 1;
+constexpr int FLAG_PARALLEL_RAY = 2;
+constexpr int FLAG_BAD_INDEX = 4;
+
+// ---------------------------------------------------------- beam constants --
+// Everything the per-voxel prologue needs about one beam, prepared on the
+// host (float64 values mirrored from the reference's arrays, float32
+// approximations for the fast blocking test).
+struct BeamDev {
+  // exact mirror inputs
+  double src[3], vy[3], m0[3], m2[3];   // m0/m2: transform rows 0 and 2
+  double vyw;                           // v_y . float32(src), reference order
+  float srcf[3], vyf[3], m0f[3], m2f[3], vywf;  // float32 copies (geom_f32 path)
+  int geom_f32;
+  // fast approximate projection: xb ~ c0 + si * (m0.S - m0.p), si = K / (n.S - n.p)
+  float a_c0, a_c2, a_m0S, a_m2S, a_nS, a_K;
+  // cull box in beam coordinates (cm) for voxel centres (inclusive)
+  float cx_lo, cx_hi, cz_lo, cz_hi;
+  float cull_margin_k;   // margin = k * SAD/depth
+  int cull_enable;
+  // block crop
+  const float* block;
+  int brows, bcols, br0, bc0, full_rows, full_cols;
+  // fluence / TERMA
+  double sad;
+  int sad_f32;
+};
+
+struct SettingsDev {
+  float sPri, sAnn, zAnn, rInner, rOuter, zExp, sExp, kExp;
+  float softRatio, softLimit, hornRatio;
+  int samples;
+  int n_energy;
+  float E[CH_MAX_ENERGY], w[CH_MAX_ENERGY], mu[CH_MAX_ENERGY];
+};
+
+struct GridDev {
+  int n[3];
+  float origin[3];
+  float spacing[3];
+  int zp;             // padded z pitch of the internal TERMA volume
+  int swap_xy;
+};
+
+// ------------------------------------------------------------ exact math --
+// Reference arithmetic without FMA contraction (round after every op).
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float d2f(double a) { return __double2float_rn(a); }
+
+// voxel centre: float32 store of f64(origin) + f64(spacing) * i.  The float64
+// value is exact for any realistic grid, so one fused rounding equals it.
+__device__ __forceinline__ float voxel_centre(float origin, float spacing, int i) {
+  return __fmaf_rn(spacing, (float)i, origin);
+}
+
+// DDA initial t and increment for one axis (reference cuda_dda_3d):
+// t0 = f32(f64(s/2) / f64(|d|)) == fdiv(s/2, |d|) (double rounding through
+// float64 is innocuous for float32 operands), dt = s / |d| in float32.
+__device__ __forceinline__ void dda_axis(float d, float s, int& step, float& t, float& dt) {
+  step = d < 0.0f ? -1 : 1;
+  float a = d < 0.0f ? -d : d;
+  if (a == 0.0f) {
+    t = 1000000000.0f;
+    dt = 1000000000.0f;
+  } else {
+    t = fdiv(s * 0.5f, a);
+    dt = fdiv(s, a);
+  }
+}
+
+__device__ __forceinline__ int dda_pick(const float* t) {
+  return (t[0] < t[1]) ? ((t[0] < t[2]) ? 0 : 2) : ((t[1] < t[2]) ? 1 : 2);
+}
+
+// ----------------------------------------------------- cone stage structs --
+constexpr uint32_t RANGE_EMPTY = 0xffffffffu;
+
+struct __align__(128) ConeBeam {
+  CUtensorMap tmap;       // TERMA volume (dims nz, ny, nx; pitch zp)
+  float* dose;
+  const uint32_t* ranges; // [n_tiles][n_dirs]
+  int n[3];
+  int ntile[3];
+  int n_tiles;
+  int unit_begin;
+  int n_units;
+  int pad[3];
+};
+static_assert(sizeof(ConeBeam) % 128 == 0, "ConeBeam must keep tensor maps aligned");
+
+struct ConeDirs {
+  int n_dirs;
+  const int* tap_base;
+  const int* tap_len;
+  const int2* taps;        // (window offset of O[m], float bits of w[m])
+  const short4* offs;      // O[m] (x, y, z, step axis)
+  const float* tvals;      // exit t of tap m
+  const int* chunk_base;
+  const int* n_chunks;
+  const int* chunk_start;
+  const float* dirs;       // unit direction (x, y, z)
+};
+
+struct RangeBeam {
+  int n[3], ntile[3], n_tiles;
+  float origin[3], spacing[3];
+  int n_planes;
+  float pa[4][3];
+  float pk0[4];
+  const int* aabb;
+  uint32_t* ranges;
+};
+
+struct Inter {
+  double* blocked;
+  float *d_eff, *oad, *fluence, *f_soften, *f_horn, *terma;
+};
+
+// ------------------------------------------------------------ launchers --
+void upload_unit_partials();
+void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const SettingsDev& s, float* T,
+                     const Inter& inter, int all_voxels, int* aabb, int* flags, cudaStream_t st);
+void launch_stencil(const float* theta, int n_theta, const float* phi, int n_phi, const double* K, int n_r,
+                    const float* spacing, const int* cap, int max_len, short4* off, float* t, float* dk,
+                    int* len, float* dirs, cudaStream_t st);
+void launch_dda_trace(const int* n, const float* sp, int n_rays, const int* starts, const float* dirs, int cap,
+                      int* vox, float* t, int* len, cudaStream_t st);
+void launch_scatter(const float* T, const int* n, int zp, int n_dirs, const int* tap_base, const int* tap_len,
+                    const short4* offs, const int2* taps, float* dose, cudaStream_t st);
+size_t cone_smem_bytes();
+cudaError_t setup_cone_kernel();
+void launch_range(const RangeBeam* rbs_dev, int n_beams, int max_tiles, const ConeDirs& D, cudaStream_t st);
+void launch_gather(const ConeBeam* beams_dev, int n_beams, const ConeDirs& D, int total_units, int n_ctas,
+                   int* unit_counter, unsigned long long* updates, int* flags, cudaStream_t st);
+void launch_init_scratch(int* aabb, int n_beams, int* counters, cudaStream_t st);
+
+}  // namespace ch

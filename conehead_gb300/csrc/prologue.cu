@@ -1,0 +1,385 @@
+// Fused beam prologue: voxel blocking -> radiological depth -> off-axis
+// distance -> fluence -> softening/horn -> TERMA, one thread per voxel.
+//
+// Follows conehead/conehead.py:71-120 (cuda_hit_test), :209-254
+// (cuda_d_eff with cuda_dda_3d :123-206), :286-314 (cuda_oad), :320-360
+// (cuda_fluence), :641-655 (softening/horn, host numpy float32) and
+// :364-377 (cuda_terma).  The reference runs these as six launches with a
+// host round trip after each; here they are one pass over the grid that
+// writes only TERMA (plus the intermediates when asked).
+//
+// Exactness: blocked, d_eff, oad, f_soften and f_horn reproduce the
+// reference's rounding bit for bit (float32 with float64 where Numba
+// promotes, no FMA contraction).  Blocking samples are classified with a
+// float32 projection first; a sample whose block cell is ambiguous within
+// the float32 error bound (SAMPLE_DELTA cells) is recomputed with the exact
+// float64 mirror, so GB300's low float64 rate is only paid at field edges.
+// Fluence and TERMA run in float32 (reference: float64 fluence, float32
+// TERMA) and are compared with a tolerance.
+
+#include <cstdio>
+
+#include "ch_internal.cuh"
+
+namespace ch {
+
+constexpr float SAMPLE_DELTA = 0.05f;   // cells (0.1 mm) of float32 slack
+
+// partial sums 0, 1/27, 1/27+1/27, ... accumulated in float64 as the
+// reference does for a block value of exactly 1.0 and 3x3x3 samples
+__constant__ double c_unit_partial[28];
+
+// --------------------------------------------------------- block lookup --
+// cell index i = floor(100 x) (x in cm, beam coordinates); the reference
+// reads block_values[i + 1999] after checking i + 2000 in [0, 3999]; index
+// -1 wraps to the last row/column.
+__device__ __forceinline__ float cell_value(const BeamDev& b, long long fi, long long fk) {
+  long long c0 = fi + 2000, c1 = fk + 2000;
+  if (c0 < 0 || c0 > 3999 || c1 < 0 || c1 > 3999) return 0.0f;
+  long long r = c0 - 1, c = c1 - 1;
+  if (r < 0) r += b.full_rows;
+  if (c < 0) c += b.full_cols;
+  r -= b.br0;
+  c -= b.bc0;
+  if (r < 0 || r >= b.brows || c < 0 || c >= b.bcols) return 0.0f;
+  return __ldg(b.block + r * b.bcols + c);
+}
+
+__device__ __forceinline__ long long floor_cell(float v) {
+  // floor(f32 product) as the reference stores it; NaN -> out of range
+  if (!(v == v)) return 1ll << 40;
+  float f = floorf(v);
+  if (f > 1e12f) return 1ll << 40;
+  if (f < -1e12f) return -(1ll << 40);
+  return (long long)f;
+}
+
+// Exact projection, float64 source arrays (conehead.py:25-47 + :109-116).
+__device__ __forceinline__ bool project_exact_mixed(const BeamDev& b, const float* rd, float& px,
+                                                    float& pz) {
+  const double ndotu =
+      dadd(dadd(dmul(b.vy[0], (double)rd[0]), dmul(b.vy[1], (double)rd[1])), dmul(b.vy[2], (double)rd[2]));
+  if (fabs(ndotu) < 1e-6) return false;
+  const double si = ddiv(-b.vyw, ndotu);
+  float pp[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) pp[k] = d2f(dadd(dadd((double)b.srcf[k], dmul(si, (double)rd[k])), 0.0));
+  px = d2f(dadd(dadd(dmul(b.m0[0], (double)pp[0]), dmul(b.m0[1], (double)pp[1])), dmul(b.m0[2], (double)pp[2])));
+  pz = d2f(dadd(dadd(dmul(b.m2[0], (double)pp[0]), dmul(b.m2[1], (double)pp[1])), dmul(b.m2[2], (double)pp[2])));
+  return true;
+}
+
+// Exact projection, float32 source arrays (all float32 arithmetic).
+__device__ __forceinline__ bool project_exact_f32(const BeamDev& b, const float* rd, float& px,
+                                                  float& pz) {
+  const float ndotu = fadd(fadd(fmul(b.vyf[0], rd[0]), fmul(b.vyf[1], rd[1])), fmul(b.vyf[2], rd[2]));
+  if (fabs((double)ndotu) < 1e-6) return false;
+  const float si = fdiv(-b.vywf, ndotu);
+  float pp[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) pp[k] = fadd(fadd(b.srcf[k], fmul(si, rd[k])), 0.0f);
+  px = fadd(fadd(fmul(b.m0f[0], pp[0]), fmul(b.m0f[1], pp[1])), fmul(b.m0f[2], pp[2]));
+  pz = fadd(fadd(fmul(b.m2f[0], pp[0]), fmul(b.m2f[1], pp[1])), fmul(b.m2f[2], pp[2]));
+  return true;
+}
+
+// reference ray vector source - p, rounded to float32
+__device__ __forceinline__ void ray_to_source(const BeamDev& b, const float* p, float* rd) {
+  if (b.geom_f32) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) rd[k] = fsub(b.srcf[k], p[k]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) rd[k] = d2f(dsub(b.src[k], (double)p[k]));
+  }
+}
+
+__device__ __forceinline__ bool project_exact(const BeamDev& b, const float* rd, float& px, float& pz) {
+  return b.geom_f32 ? project_exact_f32(b, rd, px, pz) : project_exact_mixed(b, rd, px, pz);
+}
+
+// Exact transmission of one sub-sample (reference path end to end).
+__device__ float sample_exact(const BeamDev& b, const GridDev& g, const float* pos, const float* off,
+                              int ix, int iy, int iz, int& bad) {
+  const int ii[3] = {ix, iy, iz};
+  float ps[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    // ((pos - s/2) + off/2) + off*i, exact in float64, one rounding
+    const double v = dadd(dadd(dsub((double)pos[k], (double)g.spacing[k] * 0.5), (double)off[k] * 0.5),
+                          dmul((double)off[k], (double)ii[k]));
+    ps[k] = d2f(v);
+  }
+  float rd[3];
+  ray_to_source(b, ps, rd);
+  float px, pz;
+  if (!project_exact(b, rd, px, pz)) {
+    bad = 1;
+    return 0.0f;
+  }
+  return cell_value(b, floor_cell(fmul(px, 100.0f)), floor_cell(fmul(pz, 100.0f)));
+}
+
+// ------------------------------------------------------------ blocking --
+// Transmission of sub-sample (ix, iy, iz): float32 projection, exact
+// float64 mirror only when the block cell is ambiguous within SAMPLE_DELTA.
+__device__ __forceinline__ float sample_value(const BeamDev& b, const GridDev& g, const float* pos,
+                                              const float* off, const float (*rel)[8], int ix, int iy,
+                                              int iz, int& bad) {
+  const float p0 = pos[0] + rel[0][ix], p1 = pos[1] + rel[1][iy], p2 = pos[2] + rel[2][iz];
+  const float np_ = b.vyf[0] * p0 + b.vyf[1] * p1 + b.vyf[2] * p2;
+  const float m0p = b.m0f[0] * p0 + b.m0f[1] * p1 + b.m0f[2] * p2;
+  const float m2p = b.m2f[0] * p0 + b.m2f[1] * p1 + b.m2f[2] * p2;
+  const float ndr = b.a_nS - np_;
+  // the float32 error bound assumes a magnification SAD/depth below 5; closer
+  // to the source plane (or behind it) take the exact path, which also
+  // reports rays parallel to the blocking plane as the reference does
+  if (!(fabsf(ndr) > 0.2f * fabsf(b.a_K))) return sample_exact(b, g, pos, off, ix, iy, iz, bad);
+  const float si = b.a_K / ndr;
+  const float ux = (b.a_c0 + si * (b.a_m0S - m0p)) * 100.0f;
+  const float uz = (b.a_c2 + si * (b.a_m2S - m2p)) * 100.0f;
+  const long long i0 = floor_cell(ux - SAMPLE_DELTA), i1 = floor_cell(ux + SAMPLE_DELTA);
+  const long long k0 = floor_cell(uz - SAMPLE_DELTA), k1 = floor_cell(uz + SAMPLE_DELTA);
+  float v = cell_value(b, i0, k0);
+  if (i0 != i1 || k0 != k1) {
+    const float v1 = cell_value(b, i1, k0), v2 = cell_value(b, i0, k1), v3 = cell_value(b, i1, k1);
+    if (v1 != v || v2 != v || v3 != v) v = sample_exact(b, g, pos, off, ix, iy, iz, bad);
+  }
+  return v;
+}
+
+// blocked fraction of one voxel (float64, reference accumulation order:
+// acc = acc + v / S^3 over ix, iy, iz)
+__device__ double blocked_fraction(const BeamDev& b, const GridDev& g, int S, const float* pos,
+                                   int& bad) {
+  float off[3], rel[3][8];
+#pragma unroll
+  // f32(f64(s) / S) == fdiv(s, S): double rounding is innocuous for float32 operands
+  for (int k = 0; k < 3; ++k) off[k] = fdiv(g.spacing[k], (float)S);
+  const bool exact_all = b.geom_f32 != 0 || S > 8;
+  if (!exact_all) {
+    for (int k = 0; k < 3; ++k)
+      for (int i = 0; i < S; ++i) rel[k][i] = off[k] * ((float)i + 0.5f) - g.spacing[k] * 0.5f;
+  }
+  if (!exact_all && S == 3) {
+    // jaw maps hold only 0 and 1: then the float64 sum is a table lookup
+    int n_one = 0;
+    bool other = false;
+    for (int ix = 0; ix < 3 && !other; ++ix)
+      for (int iy = 0; iy < 3 && !other; ++iy)
+        for (int iz = 0; iz < 3; ++iz) {
+          const float v = sample_value(b, g, pos, off, rel, ix, iy, iz, bad);
+          if (v == 1.0f) {
+            ++n_one;
+          } else if (v != 0.0f) {
+            other = true;
+            break;
+          }
+        }
+    if (!other) return c_unit_partial[n_one];
+  }
+  double acc = 0.0;
+  const double denom = (double)S * (double)S * (double)S;
+  float last_v = -1.0f;
+  double last_q = 0.0;
+  for (int ix = 0; ix < S; ++ix)
+    for (int iy = 0; iy < S; ++iy)
+      for (int iz = 0; iz < S; ++iz) {
+        const float v = exact_all ? sample_exact(b, g, pos, off, ix, iy, iz, bad)
+                                  : sample_value(b, g, pos, off, rel, ix, iy, iz, bad);
+        if (v != last_v) {
+          last_v = v;
+          last_q = ddiv((double)v, denom);
+        }
+        acc = dadd(acc, last_q);
+      }
+  return acc;
+}
+
+// ------------------------------------------------------------------ DDA --
+__device__ __forceinline__ float rho_at(const float* __restrict__ rho, const GridDev& g, int x, int y,
+                                        int z) {
+  const long long idx = g.swap_xy ? ((long long)y * g.n[0] + x) * g.n[2] + z
+                                  : ((long long)x * g.n[1] + y) * g.n[2] + z;
+  return __ldg(rho + idx);
+}
+
+// radiological depth from voxel (x, y, z) toward the source (cuda_d_eff)
+__device__ float radiological_depth(const float* __restrict__ rho, const GridDev& g, int x, int y, int z,
+                                    const float* rd) {
+  const float mag = __fsqrt_rn(fadd(fadd(fmul(rd[0], rd[0]), fmul(rd[1], rd[1])), fmul(rd[2], rd[2])));
+  int s0, s1, s2;
+  float t0, t1, t2, d0, d1, d2;
+  dda_axis(fdiv(rd[0], mag), g.spacing[0], s0, t0, d0);
+  dda_axis(fdiv(rd[1], mag), g.spacing[1], s1, t1, d1);
+  dda_axis(fdiv(rd[2], mag), g.spacing[2], s2, t2, d2);
+  int cx = x, cy = y, cz = z;
+  float deff = 0.0f, tprev = 0.0f;
+  bool first = true;
+  const int n0 = g.n[0], n1 = g.n[1], n2 = g.n[2];
+  while (cx >= 0 && cx < n0 && cy >= 0 && cy < n1 && cz >= 0 && cz < n2) {
+    const float r = rho_at(rho, g, cx, cy, cz);
+    float tv;
+    if (t0 < t1) {
+      if (t0 < t2) { tv = t0; t0 = fadd(t0, d0); cx += s0; }
+      else { tv = t2; t2 = fadd(t2, d2); cz += s2; }
+    } else {
+      if (t1 < t2) { tv = t1; t1 = fadd(t1, d1); cy += s1; }
+      else { tv = t2; t2 = fadd(t2, d2); cz += s2; }
+    }
+    // the reference accumulates in the returned order: voxel v, exit t_v
+    deff = first ? fadd(deff, fmul(r, tv)) : fadd(deff, fmul(r, fsub(tv, tprev)));
+    first = false;
+    tprev = tv;
+  }
+  return deff;
+}
+
+// -------------------------------------------------------------- kernel --
+__global__ void __launch_bounds__(256) prologue_kernel(
+    const float* __restrict__ rho, GridDev g, BeamDev b, SettingsDev s, float* __restrict__ T,
+    Inter inter, int all_voxels, int* __restrict__ aabb, int* __restrict__ flags) {
+  const long long N = (long long)g.n[0] * g.n[1] * g.n[2];
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = v < N;
+  int x = 0, y = 0, z = 0;
+  float Tv = 0.0f;
+  int bad = 0;
+  if (live) {
+    z = (int)(v % g.n[2]);
+    const long long r = v / g.n[2];
+    y = (int)(r % g.n[1]);
+    x = (int)(r / g.n[1]);
+    float pos[3];
+    pos[0] = voxel_centre(g.origin[0], g.spacing[0], x);
+    pos[1] = voxel_centre(g.origin[1], g.spacing[1], y);
+    pos[2] = voxel_centre(g.origin[2], g.spacing[2], z);
+
+    // ---- cull: voxels whose every sub-sample misses the open block region
+    bool candidate = true;
+    if (b.cull_enable) {
+      const float np_ = b.vyf[0] * pos[0] + b.vyf[1] * pos[1] + b.vyf[2] * pos[2];
+      const float m0p = b.m0f[0] * pos[0] + b.m0f[1] * pos[1] + b.m0f[2] * pos[2];
+      const float m2p = b.m2f[0] * pos[0] + b.m2f[1] * pos[1] + b.m2f[2] * pos[2];
+      const float ndr = b.a_nS - np_;   // n . (S - p) = -depth
+      const float depth = -ndr;
+      if (depth > 0.2f * fabsf(b.a_K)) {
+        const float si = b.a_K / ndr;
+        const float xb = b.a_c0 + si * (b.a_m0S - m0p);
+        const float zb = b.a_c2 + si * (b.a_m2S - m2p);
+        const float lat = fmaxf(fabsf(b.a_m0S - m0p), fabsf(b.a_m2S - m2p)) / depth;
+        const float margin = b.cull_margin_k * fabsf(b.a_K) / depth * (1.0f + lat) + 0.01f;
+        if (xb < b.cx_lo - margin || xb > b.cx_hi + margin || zb < b.cz_lo - margin ||
+            zb > b.cz_hi + margin)
+          candidate = false;
+      }
+    }
+    double blocked = 0.0;
+    if (candidate) blocked = blocked_fraction(b, g, s.samples, pos, bad);
+
+    if (blocked != 0.0 || all_voxels) {
+      float rd[3];
+      ray_to_source(b, pos, rd);
+      // ---- radiological depth (float32, exact mirror)
+      const float deff = radiological_depth(rho, g, x, y, z, rd);
+      // ---- off-axis distance (exact mirror)
+      float px = 0.0f, pz = 0.0f;
+      if (!project_exact(b, rd, px, pz)) bad = 1;
+      const float oad = __fsqrt_rn(fadd(fmul(px, px), fmul(pz, pz)));
+      // ---- fluence (float32 evaluation of the reference's float64 formula)
+      const float mag = __fsqrt_rn(fadd(fadd(fmul(rd[0], rd[0]), fmul(rd[1], rd[1])), fmul(rd[2], rd[2])));
+      const float sad = (float)b.sad;
+      const float ratio = sad / mag;
+      const float fpoint = s.sPri * (ratio * ratio);
+      const float r_ann = oad * s.zAnn / sad;
+      float fann = 0.0f;
+      if (r_ann >= s.rInner && r_ann <= s.rOuter) {
+        const float a = sad - s.zAnn, c = mag - s.zAnn;
+        fann = s.sAnn * (a * a) / (c * c);
+      }
+      const float oadc = oad < 2.0f ? 2.0f : oad;
+      const float r_exp = oadc * s.zExp / sad;
+      const float ae = sad - s.zExp, ce = mag - s.zExp;
+      const float fexp = s.sExp / r_exp * expf(-s.kExp * r_exp) * (ae * ae) / (ce * ce);
+      const float fluence = (float)((double)(fpoint + fann + fexp) * blocked);
+      // ---- softening and horn (reference host numpy, float32)
+      float fs = 1.0f;
+      if (oad < s.softLimit) fs = fdiv(1.0f, fsub(1.0f, fmul(s.softRatio, oad)));
+      const float fh = fadd(1.0f, fmul(oad, s.hornRatio));
+      // ---- TERMA (float32, reference order)
+      float terma = 0.0f;
+      for (int i = 0; i < s.n_energy; ++i) {
+        const float e = expf(fmul(fmul(-s.mu[i], fs), deff));
+        terma = fadd(terma, fmul(fmul(fmul(fmul(fmul(s.w[i], fluence), e), s.E[i]), s.mu[i]), fh));
+      }
+      Tv = d2f(dmul((double)terma, blocked));
+      if (inter.d_eff) inter.d_eff[v] = deff;
+      if (inter.oad) inter.oad[v] = oad;
+      if (inter.fluence) inter.fluence[v] = fluence;
+      if (inter.f_soften) inter.f_soften[v] = fs;
+      if (inter.f_horn) inter.f_horn[v] = fh;
+    } else {
+      if (inter.d_eff) inter.d_eff[v] = 0.0f;
+      if (inter.oad) inter.oad[v] = 0.0f;
+      if (inter.fluence) inter.fluence[v] = 0.0f;
+      if (inter.f_soften) inter.f_soften[v] = 1.0f;
+      if (inter.f_horn) inter.f_horn[v] = 1.0f;
+    }
+    if (inter.blocked) inter.blocked[v] = blocked;
+    if (inter.terma) inter.terma[v] = Tv;
+    T[((long long)x * g.n[1] + y) * g.zp + z] = Tv;
+  }
+  // ---- support box of T != 0 (reference skips T == 0 sources)
+  const bool nz_ = live && Tv != 0.0f;
+  const unsigned m = __ballot_sync(0xffffffffu, nz_);
+  if (m) {
+    int lo0 = nz_ ? x : INT_MAX, hi0 = nz_ ? x : INT_MIN;
+    int lo1 = nz_ ? y : INT_MAX, hi1 = nz_ ? y : INT_MIN;
+    int lo2 = nz_ ? z : INT_MAX, hi2 = nz_ ? z : INT_MIN;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo0 = min(lo0, __shfl_xor_sync(0xffffffffu, lo0, o));
+      hi0 = max(hi0, __shfl_xor_sync(0xffffffffu, hi0, o));
+      lo1 = min(lo1, __shfl_xor_sync(0xffffffffu, lo1, o));
+      hi1 = max(hi1, __shfl_xor_sync(0xffffffffu, hi1, o));
+      lo2 = min(lo2, __shfl_xor_sync(0xffffffffu, lo2, o));
+      hi2 = max(hi2, __shfl_xor_sync(0xffffffffu, hi2, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(aabb + 0, lo0); atomicMax(aabb + 1, hi0);
+      atomicMin(aabb + 2, lo1); atomicMax(aabb + 3, hi1);
+      atomicMin(aabb + 4, lo2); atomicMax(aabb + 5, hi2);
+    }
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flags, FLAG_PARALLEL_RAY);
+}
+
+void upload_unit_partials() {
+  double p[28];
+  p[0] = 0.0;
+  const double q = 1.0 / 27.0;
+  for (int i = 1; i < 28; ++i) p[i] = p[i - 1] + q;
+  cudaMemcpyToSymbol(c_unit_partial, p, sizeof(p));
+}
+
+void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const SettingsDev& s,
+                     float* T, const Inter& inter, int all_voxels, int* aabb, int* flags,
+                     cudaStream_t st) {
+  const long long N = (long long)g.n[0] * g.n[1] * g.n[2];
+  const int threads = 256;
+  const long long blocks = (N + threads - 1) / threads;
+  prologue_kernel<<<(unsigned)blocks, threads, 0, st>>>(rho, g, b, s, T, inter, all_voxels, aabb, flags);
+}
+
+__global__ void init_scratch_kernel(int* aabb, int n_beams, int* counters) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n_beams * 8) aabb[i] = (i % 2 == 0) ? INT_MAX : INT_MIN;
+  if (i < 8) counters[i] = 0;
+}
+
+void launch_init_scratch(int* aabb, int n_beams, int* counters, cudaStream_t st) {
+  const int n = n_beams * 8 > 8 ? n_beams * 8 : 8;
+  init_scratch_kernel<<<(n + 255) / 256, 256, 0, st>>>(aabb, n_beams, counters);
+}
+
+}  // namespace ch

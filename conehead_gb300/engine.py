@@ -1,0 +1,174 @@
+"""Device-resident dose engine over the C ABI.
+
+``DoseEngine`` owns one ``ch_plan`` (kernel tables, direction stencils and
+scratch stay on the GPU between calls) and runs single beams, batches of
+beams and the plain scatter path on torch CUDA tensors.  Host objects use
+the reference's duck-typed attributes (``source.position/v_y/transform/
+sad``, ``block.block_values``, ``phantom.size/origin/spacing/densities``)
+and its ``settings`` dict.
+"""
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native as N
+from .kernel import poly_kernel_tables
+
+
+@dataclass
+class DeviceBlock:
+    """Block map on the device, cropped to its nonzero bounding box."""
+    crop: object          # torch float32 tensor [rows, cols]
+    r0: int
+    c0: int
+    full_shape: tuple
+
+
+@dataclass
+class BeamJob:
+    grid: object          # N.Grid
+    rho: object           # torch float32 tensor, phantom.densities layout
+    swap_xy: int
+    beam: object          # N.Beam
+    settings: object      # N.Settings
+    dose: object          # torch float32 tensor [nx, ny, nz]
+    keep: tuple = ()      # tensors the beam struct points at
+
+
+class DoseEngine:
+    def __init__(self, device=0):
+        import torch
+        if not torch.cuda.is_available():
+            raise RuntimeError("conehead_gb300 needs a CUDA GPU (GB300); no CPU fallback exists")
+        self.torch = torch
+        self.index = int(device)
+        self.device = torch.device("cuda", self.index)
+        self.L = N.lib()
+        plan = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            N.check(self.L.ch_plan_create(ctypes.byref(plan), self.index), "ch_plan_create")
+        self.plan = plan
+        self._kernel_key = None
+
+    def close(self):
+        if getattr(self, "plan", None):
+            self.L.ch_plan_destroy(self.plan)
+            self.plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------ set-up --
+    def stream(self):
+        return ctypes.c_void_p(self.torch.cuda.current_stream(self.device).cuda_stream)
+
+    def set_kernel(self, energy_weights, kernel_dir=None):
+        key = (tuple((k, float(v)) for k, v in energy_weights.items()), kernel_dir)
+        if key == self._kernel_key:
+            return
+        K, thetas, phis = poly_kernel_tables(energy_weights, kernel_dir)
+        K = np.ascontiguousarray(K, dtype=np.float64)
+        thetas = np.ascontiguousarray(thetas, dtype=np.float32)
+        phis = np.ascontiguousarray(phis, dtype=np.float32)
+        k = N.Kernel(K.shape[0], K.shape[1], len(thetas), K.ctypes.data, thetas.ctypes.data,
+                     phis.ctypes.data)
+        N.check(self.L.ch_plan_set_kernel(self.plan, ctypes.byref(k)), "ch_plan_set_kernel")
+        self._kernel_key = key
+
+    def upload_block(self, block_values):
+        crop, r0, c0 = N.block_crop(block_values)
+        t = self.torch.from_numpy(crop).to(self.device)
+        return DeviceBlock(t, r0, c0, tuple(np.shape(block_values)))
+
+    def upload_densities(self, densities):
+        return self.torch.from_numpy(np.ascontiguousarray(densities, dtype=np.float32)).to(self.device)
+
+    def job(self, phantom, rho, source, dblock, settings, swap_xy=None, dose=None):
+        size = [int(n) for n in phantom.size]
+        if swap_xy is None:
+            swap_xy = int(size[0] == size[1])
+        grid = N.grid_struct(size, phantom.origin, phantom.spacing)
+        beam = N.beam_struct(source, dblock.crop.data_ptr(), dblock.crop.shape, dblock.r0, dblock.c0,
+                             dblock.full_shape)
+        s = settings if isinstance(settings, N.Settings) else N.settings_struct(settings)
+        if dose is None:
+            dose = self.torch.empty(size, dtype=self.torch.float32, device=self.device)
+        return BeamJob(grid, rho, int(swap_xy), beam, s, dose, (dblock.crop,))
+
+    # ----------------------------------------------------------- compute --
+    def run(self, job, intermediates=False, scatter=False):
+        """Enqueue one beam; returns the dose tensor (and intermediates)."""
+        torch = self.torch
+        st = self.stream()
+        out = None
+        if scatter:
+            N.check(self.L.ch_dose_scatter(self.plan, ctypes.byref(job.grid), job.rho.data_ptr(), job.swap_xy,
+                                           ctypes.byref(job.beam), ctypes.byref(job.settings),
+                                           job.dose.data_ptr(), st), "ch_dose_scatter")
+        elif intermediates:
+            size = list(job.dose.shape)
+            out = {"blocked": torch.empty(size, dtype=torch.float64, device=self.device)}
+            for k in ("d_eff", "oad", "fluence", "f_soften", "f_horn", "terma"):
+                out[k] = torch.empty(size, dtype=torch.float32, device=self.device)
+            inter = N.Intermediates(*[out[k].data_ptr() for k in
+                                      ("blocked", "d_eff", "oad", "fluence", "f_soften", "f_horn", "terma")])
+            N.check(self.L.ch_dose_ex(self.plan, ctypes.byref(job.grid), job.rho.data_ptr(), job.swap_xy,
+                                      ctypes.byref(job.beam), ctypes.byref(job.settings), job.dose.data_ptr(),
+                                      ctypes.byref(inter), st), "ch_dose_ex")
+        else:
+            N.check(self.L.ch_dose(self.plan, ctypes.byref(job.grid), job.rho.data_ptr(), job.swap_xy,
+                                   ctypes.byref(job.beam), ctypes.byref(job.settings), job.dose.data_ptr(), st),
+                    "ch_dose")
+        return (job.dose, out) if intermediates else job.dose
+
+    def run_batch(self, jobs):
+        """Enqueue many beams in one pass; returns their dose tensors."""
+        n = len(jobs)
+        grids = (N.Grid * n)(*[j.grid for j in jobs])
+        beams = (N.Beam * n)(*[j.beam for j in jobs])
+        sets = (N.Settings * n)(*[j.settings for j in jobs])
+        rho = (ctypes.c_void_p * n)(*[j.rho.data_ptr() for j in jobs])
+        dose = (ctypes.c_void_p * n)(*[j.dose.data_ptr() for j in jobs])
+        swap = (ctypes.c_int * n)(*[j.swap_xy for j in jobs])
+        N.check(self.L.ch_dose_batch(self.plan, n, grids, rho, swap, beams, sets, dose, self.stream()),
+                "ch_dose_batch")
+        return [j.dose for j in jobs]
+
+    def sync(self):
+        N.check(self.L.ch_plan_sync(self.plan, self.stream()), "ch_plan_sync")
+
+    def stats(self):
+        s = N.Stats()
+        N.check(self.L.ch_plan_stats(self.plan, ctypes.byref(s)), "ch_plan_stats")
+        return {k: getattr(s, k) for k, _ in N.Stats._fields_}
+
+    # ------------------------------------------------------- test hooks --
+    def cone_directions(self):
+        import torch
+        n = 12 * 48
+        out = torch.empty((n, 3), dtype=torch.float32, device=self.device)
+        N.check(self.L.ch_cone_directions(self.plan, out.data_ptr(), self.stream()), "ch_cone_directions")
+        self.sync()
+        return out.cpu().numpy()
+
+
+def dda_trace(size, spacing, starts, dirs, cap=1024, device=0):
+    """Device DDA traces (test hook): voxels [n, cap, 3], t [n, cap], lengths [n]."""
+    import torch
+    dev = torch.device("cuda", device)
+    starts = torch.as_tensor(np.ascontiguousarray(starts, dtype=np.int32), device=dev)
+    dirs = torch.as_tensor(np.ascontiguousarray(dirs, dtype=np.float32), device=dev)
+    n = starts.shape[0]
+    vox = torch.zeros((n, cap, 3), dtype=torch.int32, device=dev)
+    tv = torch.zeros((n, cap), dtype=torch.float32, device=dev)
+    ln = torch.zeros((n,), dtype=torch.int32, device=dev)
+    g = N.grid_struct(size, (0, 0, 0), spacing)
+    st = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    N.check(N.lib().ch_dda_trace(ctypes.byref(g), n, starts.data_ptr(), dirs.data_ptr(), cap, vox.data_ptr(),
+                                 tv.data_ptr(), ln.data_ptr(), st), "ch_dda_trace")
+    torch.cuda.synchronize(dev)
+    return vox.cpu().numpy(), tv.cpu().numpy(), ln.cpu().numpy()

@@ -1,0 +1,181 @@
+/*
+ * conehead_gb300 -- C ABI of the GB300 collapsed-cone dose engine.
+ *
+ * Plain C types only: grids, beams and settings are small structs of
+ * numbers; volumes are raw device pointers (float32, C order [x][y][z],
+ * z fastest, exactly the layout of the reference's numpy arrays); the
+ * stream argument is a cudaStream_t passed as void*.  Every call returns a
+ * ch_status; ch_last_error() gives a one-line message for the last failure
+ * on the calling thread.
+ *
+ * Reference interfaces replaced (samuelpeet/conehead):
+ *   ch_dose / ch_dose_ex  <- Conehead.calculate, conehead/conehead.py:522-738
+ *                            (cuda_hit_test :71-120, cuda_d_eff :209-254,
+ *                             cuda_oad :286-314, cuda_fluence :320-360,
+ *                             softening/horn :641-655, cuda_terma :364-377,
+ *                             cuda_dose :385-488)
+ *   ch_plan_set_kernel    <- the polyenergetic kernel build,
+ *                            conehead/conehead.py:685-706 (host tables in,
+ *                            per-direction stencils built on the device)
+ *   ch_dose_batch         <- a loop of Conehead.calculate calls, one launch
+ *   ch_dose_scatter       <- cuda_dose's per-voxel scatter with float32
+ *                            atomics, conehead/conehead.py:385-488 (kept as
+ *                            the plain one-beam-per-launch GPU path)
+ *   ch_dda_trace          <- cuda_dda_3d, conehead/conehead.py:123-206
+ *                            (test hook for bit-exact DDA sequences)
+ */
+#ifndef CONEHEAD_GB300_H
+#define CONEHEAD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CH_MAX_ENERGY 32
+
+typedef enum {
+  CH_OK = 0,
+  CH_ERR_INVALID_ARG = 1,   /* bad sizes, null pointers, unsupported layout */
+  CH_ERR_OOM = 2,           /* device allocation failed */
+  CH_ERR_DEVICE = 3,        /* CUDA runtime error */
+  CH_ERR_TIMEOUT = 4,       /* a bounded device-side wait gave up */
+  CH_ERR_PARALLEL_RAY = 5,  /* a ray is parallel to the blocking plane
+                               (the reference raises RuntimeError) */
+  CH_ERR_NO_KERNEL = 6      /* ch_plan_set_kernel was not called */
+} ch_status;
+
+/* Dose grid: voxel centres at origin + spacing * index (cm). */
+typedef struct {
+  int n[3];
+  float origin[3];
+  float spacing[3];
+} ch_grid;
+
+/* One beam.  Geometry is given in float64 (float32 values convert
+ * exactly); geom_f32 = 1 when the source's position/v_y/transform are
+ * float32 arrays (a Source whose angles were never set), which changes the
+ * arithmetic the reference performs.  The block map may be cropped:
+ * `block` holds rows [block_r0, block_r0 + block_rows) and columns
+ * [block_c0, block_c0 + block_cols) of a full_rows x full_cols map that is
+ * zero outside the crop. */
+typedef struct {
+  double src[3];        /* source.position (cm) */
+  double vy[3];         /* source.v_y, blocking-plane normal */
+  double xform[9];      /* source.transform, row major */
+  double sad;           /* source.sad */
+  int geom_f32;
+  int sad_f32;          /* 1 when source.sad is a float32 scalar */
+  const float* block;   /* device pointer, row major [block_rows][block_cols] */
+  int block_rows, block_cols;
+  int block_r0, block_c0;
+  int full_rows, full_cols;
+} ch_beam;
+
+/* settings dict of Conehead.calculate (example.py:27-58) plus the spectrum
+ * (energies, weights) and mu_water(E), all float32 as the reference uses. */
+typedef struct {
+  double sPri, sAnn, zAnn, rInner, rOuter, zExp, sExp, kExp;
+  double softRatio, softLimit, hornRatio;
+  int samples;          /* fluenceResampling */
+  int n_energy;
+  float E[CH_MAX_ENERGY];
+  float w[CH_MAX_ENERGY];
+  float mu[CH_MAX_ENERGY];
+} ch_settings;
+
+/* Host tables of the polyenergetic kernel: cumulative K[n_phi][n_r]
+ * (float64, radii 0.05 + 0.01 k cm), azimuths theta[n_theta] and cone polar
+ * angles phi[n_phi] in degrees (float32). */
+typedef struct {
+  int n_phi, n_r, n_theta;
+  const double* cum;
+  const float* theta;
+  const float* phi;
+} ch_kernel;
+
+/* Optional per-voxel intermediates (device pointers, any may be NULL). */
+typedef struct {
+  double* blocked;      /* float64 like the reference's device array */
+  float* d_eff;
+  float* oad;
+  float* fluence;
+  float* f_soften;
+  float* f_horn;
+  float* terma;
+} ch_intermediates;
+
+/* Stage timings (ms, CUDA events) and counters of the last dose call. */
+typedef struct {
+  float ms_prologue;
+  float ms_range;
+  float ms_cone;
+  double updates;       /* voxel-direction updates issued by the cone stage */
+  int n_unique_dirs;
+  int n_units;
+} ch_stats;
+
+typedef struct ch_plan ch_plan;
+
+ch_status ch_plan_create(ch_plan** plan, int device);
+void ch_plan_destroy(ch_plan* plan);
+
+/* Upload the kernel tables; stencils are rebuilt lazily per voxel spacing. */
+ch_status ch_plan_set_kernel(ch_plan* plan, const ch_kernel* kernel);
+
+/* Single beam: dose_dev (float32 [x][y][z]) is overwritten.  rho_dev holds
+ * phantom.densities; swap_xy = 1 reproduces the reference's resampling step
+ * (densities read transposed in x/y, which it does for square x/y grids). */
+ch_status ch_dose(ch_plan* plan, const ch_grid* grid, const float* rho_dev, int swap_xy,
+                  const ch_beam* beam, const ch_settings* settings, float* dose_dev,
+                  void* stream);
+
+/* As ch_dose, also writing the intermediates that are non-NULL (every voxel
+ * is then evaluated, not just the ones the beam can reach). */
+ch_status ch_dose_ex(ch_plan* plan, const ch_grid* grid, const float* rho_dev, int swap_xy,
+                     const ch_beam* beam, const ch_settings* settings, float* dose_dev,
+                     const ch_intermediates* inter, void* stream);
+
+/* Many beams (each with its own grid/density/settings) in one pass: every
+ * beam's prologue, then one persistent cone launch over all beams' work. */
+ch_status ch_dose_batch(ch_plan* plan, int n_beams, const ch_grid* grids,
+                        const float* const* rho_dev, const int* swap_xy,
+                        const ch_beam* beams, const ch_settings* settings,
+                        float* const* dose_dev, void* stream);
+
+/* Plain path: prologue + per-voxel scatter with float32 atomics, one beam
+ * per launch (the reference's cuda_dose structure). */
+ch_status ch_dose_scatter(ch_plan* plan, const ch_grid* grid, const float* rho_dev,
+                          int swap_xy, const ch_beam* beam, const ch_settings* settings,
+                          float* dose_dev, void* stream);
+
+/* Test hook: n_rays DDA traces on the device.  starts int32 [n][3],
+ * dirs float32 [n][3] (used as given, no normalisation), grid dims/spacing
+ * from `grid`.  Writes voxels int32 [n][cap][3], t float32 [n][cap] and
+ * lengths int32 [n] (full length, even when > cap).  Device pointers. */
+ch_status ch_dda_trace(const ch_grid* grid, int n_rays, const int* starts_dev,
+                       const float* dirs_dev, int cap, int* voxels_dev, float* t_dev,
+                       int* len_dev, void* stream);
+
+/* Test hook: the cone directions the device computes for (theta_i, phi_j),
+ * float32 [n_theta][n_phi][3] into out_dev. */
+ch_status ch_cone_directions(ch_plan* plan, float* out_dev, void* stream);
+
+/* Wait for the plan's work on `stream` and report device-side failures
+ * (CH_ERR_TIMEOUT, CH_ERR_PARALLEL_RAY) of the last dose call. */
+ch_status ch_plan_sync(ch_plan* plan, void* stream);
+
+/* Stage timings and counters of the last dose call (waits for it). */
+ch_status ch_plan_stats(ch_plan* plan, ch_stats* out);
+
+const char* ch_status_string(ch_status status);
+const char* ch_last_error(void);
+int ch_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CONEHEAD_GB300_H */
