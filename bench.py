@@ -352,6 +352,8 @@ def run_ours(args):
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"},
             "onchip": onchip,
             "cone_ms_per_step": cone_ms,
+            "prologue_ms_per_step": statistics.mean(x["ms_prologue"] for x in stats),
+            "range_ms_per_step": statistics.mean(x["ms_range"] for x in stats),
             "updates_per_step": updates,
             "e2e": e2e,
             "clocks": clk,
