@@ -86,7 +86,7 @@ struct StencilSet {
   int n_dirs = 0;            // unique walks
   int n_raw = 0;             // theta x phi
   size_t total_taps = 0;
-  DevBuf tap_base, tap_len, taps, offs, tvals, chunk_base, n_chunks, chunk_start, dirs;
+  DevBuf tap_base, tap_len, taps, offs, tvals, chunk_base, n_chunks, chunk_start, chunk_rec, dirs;
   DevBuf raw_dirs;           // float [n_theta*n_phi][3] as the device computed them
 };
 
@@ -98,15 +98,16 @@ struct ch_plan {
   DevBuf K, theta, phi;
   StencilSet st;
   // scratch
-  DevBuf T, aabb, counters, ranges, cone_beams, range_beams;
+  DevBuf T, aabb, counters, ranges, cranges, cone_beams, range_beams, list_v, list_b;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaStream_t last_stream = nullptr;
   ch_stats stats{};
   bool stats_pending = false;
   bool timed = false;
   ~ch_plan() {
-    for (DevBuf* b : {&K, &theta, &phi, &T, &aabb, &counters, &ranges, &cone_beams, &range_beams, &st.tap_base,
-                      &st.tap_len, &st.taps, &st.offs, &st.tvals, &st.chunk_base, &st.n_chunks, &st.chunk_start,
+    for (DevBuf* b : {&K, &theta, &phi, &T, &aabb, &counters, &ranges, &cranges, &cone_beams, &range_beams, &list_v, &list_b,
+                      &st.tap_base,
+                      &st.tap_len, &st.taps, &st.offs, &st.tvals, &st.chunk_base, &st.n_chunks, &st.chunk_start, &st.chunk_rec,
                       &st.dirs, &st.raw_dirs})
       b->release();
     for (auto& e : ev)
@@ -175,9 +176,25 @@ ch_status build_stencils(ch_plan* P, const float* spacing, const int* cap, cudaS
   }
   const int U = (int)uniq_first.size();
   std::vector<int> tap_base(U), tap_len(U), chunk_base(U), n_chunks(U), chunk_start;
-  std::vector<int2> taps;
+  std::vector<int4> chunk_rec;
+  std::vector<int4> taps;
   std::vector<short4> offs;
   std::vector<float> tvals, dirs((size_t)U * 3);
+  // window variant that holds a chunk with these offset spreads (cheapest
+  // staged volume), or -1
+  auto pick_variant = [](int sx, int sy, int sz) {
+    int best = -1;
+    long best_vol = 0;
+    for (int v = 0; v < N_VARIANTS; ++v) {
+      if (sx > var_span_x(v) || sy > var_span_y(v) || sz > var_span_z(v)) continue;
+      const long vol = (long)var_p(v) * ((TY + sy + BOX_Y - 1) / BOX_Y * BOX_Y) * (TX + sx);
+      if (best < 0 || vol < best_vol) {
+        best = v;
+        best_vol = vol;
+      }
+    }
+    return best;
+  };
   for (int u = 0; u < U; ++u) {
     const int d = uniq_first[u], L = h_len[d];
     const short4* o = &h_off[(size_t)d * max_len];
@@ -185,23 +202,30 @@ ch_status build_stencils(ch_plan* P, const float* spacing, const int* cap, cudaS
     tap_len[u] = L;
     for (int k = 0; k < 3; ++k) dirs[(size_t)u * 3 + k] = h_dir[(size_t)d * 3 + k];
     for (int m = 0; m < L; ++m) {
-      const int toff = ((int)o[m].x * WY + (int)o[m].y) * WZ + (int)o[m].z;
+      int4 t;
+      int* tv4 = &t.x;
+      for (int v = 0; v < N_VARIANTS; ++v)
+        tv4[v] = ((int)o[m].x * var_rows(v) + (int)o[m].y) * var_p(v) + (int)o[m].z;
       const float w = h_dk[(size_t)d * max_len + m] * (float)mult[u];
-      int wb;
-      std::memcpy(&wb, &w, 4);
-      taps.push_back(make_int2(toff, wb));
+      std::memcpy(&t.w, &w, 4);
+      taps.push_back(t);
       offs.push_back(o[m]);
       tvals.push_back(h_t[(size_t)d * max_len + m]);
     }
-    // greedy chunks: the sources of a chunk must fit the window spans
+    // greedy chunks: grow while some window variant still holds the sources
     chunk_base[u] = (int)chunk_start.size();
     int a = 0;
     while (a < L) {
       int b = a;
-      while (b + 1 < L && std::abs(o[b + 1].x - o[a].x) <= SPAN_X && std::abs(o[b + 1].y - o[a].y) <= SPAN_Y &&
-             std::abs(o[b + 1].z - o[a].z) <= SPAN_Z)
+      while (b + 1 < L && b + 1 - a < MAX_CHUNK_TAPS &&
+             pick_variant(std::abs(o[b + 1].x - o[a].x), std::abs(o[b + 1].y - o[a].y),
+                          std::abs(o[b + 1].z - o[a].z)) >= 0)
         ++b;
       chunk_start.push_back(a);
+      const int sx = std::abs(o[b].x - o[a].x), sy = std::abs(o[b].y - o[a].y), sz = std::abs(o[b].z - o[a].z);
+      chunk_rec.push_back(make_int4(a, b, pick_variant(sx, sy, sz), sx | (sy << 16)));
+      chunk_rec.push_back(make_int4(std::max<int>(o[a].x, o[b].x), std::max<int>(o[a].y, o[b].y),
+                                    std::max<int>(o[a].z, o[b].z), 0));
       a = b + 1;
     }
     n_chunks[u] = (int)chunk_start.size() - chunk_base[u];
@@ -213,12 +237,13 @@ ch_status build_stencils(ch_plan* P, const float* spacing, const int* cap, cudaS
   };
   CH_CUDA(up(S.tap_base, tap_base.data(), tap_base.size() * sizeof(int)));
   CH_CUDA(up(S.tap_len, tap_len.data(), tap_len.size() * sizeof(int)));
-  CH_CUDA(up(S.taps, taps.data(), taps.size() * sizeof(int2)));
+  CH_CUDA(up(S.taps, taps.data(), taps.size() * sizeof(int4)));
   CH_CUDA(up(S.offs, offs.data(), offs.size() * sizeof(short4)));
   CH_CUDA(up(S.tvals, tvals.data(), tvals.size() * sizeof(float)));
   CH_CUDA(up(S.chunk_base, chunk_base.data(), chunk_base.size() * sizeof(int)));
   CH_CUDA(up(S.n_chunks, n_chunks.data(), n_chunks.size() * sizeof(int)));
   CH_CUDA(up(S.chunk_start, chunk_start.data(), chunk_start.size() * sizeof(int)));
+  CH_CUDA(up(S.chunk_rec, chunk_rec.data(), chunk_rec.size() * sizeof(int4)));
   CH_CUDA(up(S.dirs, dirs.data(), dirs.size() * sizeof(float)));
   CH_CUDA(cudaStreamSynchronize(s));
   S.valid = true;
@@ -249,12 +274,13 @@ ConeDirs cone_dirs(const ch_plan* P) {
   D.n_dirs = S.n_dirs;
   D.tap_base = S.tap_base.as<int>();
   D.tap_len = S.tap_len.as<int>();
-  D.taps = S.taps.as<int2>();
+  D.taps = S.taps.as<int4>();
   D.offs = S.offs.as<short4>();
   D.tvals = S.tvals.as<float>();
   D.chunk_base = S.chunk_base.as<int>();
   D.n_chunks = S.n_chunks.as<int>();
   D.chunk_start = S.chunk_start.as<int>();
+  D.chunk_rec = S.chunk_rec.as<int4>();
   D.dirs = S.dirs.as<float>();
   return D;
 }
@@ -264,6 +290,8 @@ ch_status check_grid(const ch_grid* g) {
   if (!g) return fail(CH_ERR_INVALID_ARG, "grid is NULL");
   for (int k = 0; k < 3; ++k) {
     if (g->n[k] <= 0 || g->n[k] > 4096) return fail(CH_ERR_INVALID_ARG, "grid dimension out of range (1..4096)");
+    if ((long long)g->n[0] * g->n[1] * g->n[2] >= (1ll << 31))
+      return fail(CH_ERR_INVALID_ARG, "grid holds 2^31 voxels or more");
     if (!(g->spacing[k] > 0.0f) || !std::isfinite(g->spacing[k]))
       return fail(CH_ERR_INVALID_ARG, "grid spacing must be positive");
     if (!std::isfinite(g->origin[k])) return fail(CH_ERR_INVALID_ARG, "grid origin must be finite");
@@ -493,8 +521,14 @@ ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, 
   CH_CUDA(P->aabb.ensure((size_t)n * 8 * sizeof(int)));
   CH_CUDA(P->counters.ensure(8 * sizeof(int)));
   CH_CUDA(P->ranges.ensure(std::max<size_t>(r_total, 1) * sizeof(uint32_t)));
+  CH_CUDA(P->cranges.ensure(std::max<size_t>(r_total, 1) * sizeof(uint32_t)));
   CH_CUDA(P->cone_beams.ensure((size_t)n * sizeof(ConeBeam)));
   CH_CUDA(P->range_beams.ensure((size_t)n * sizeof(RangeBeam)));
+  size_t max_vox = 1;
+  for (int i = 0; i < n; ++i)
+    max_vox = std::max(max_vox, (size_t)jobs[i].g.n[0] * jobs[i].g.n[1] * jobs[i].g.n[2]);
+  CH_CUDA(P->list_v.ensure(max_vox * sizeof(int)));
+  CH_CUDA(P->list_b.ensure(max_vox * sizeof(double)));
   int* counters = P->counters.as<int>();
   int* flags = counters + 1;
   unsigned long long* updates = reinterpret_cast<unsigned long long*>(counters + 2);
@@ -517,8 +551,9 @@ ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, 
       in.terma = inter->terma;
       all = (in.d_eff || in.oad || in.fluence || in.f_soften || in.f_horn) ? 1 : 0;
     }
-    launch_prologue(J.rho, J.g, J.b, J.s, P->T.as<float>() + J.t_off, in, all, P->aabb.as<int>() + 8 * i, flags,
-                    s);
+    // the voxel list is reused beam after beam (stream order)
+    launch_prologue(J.rho, J.g, J.b, J.s, P->T.as<float>() + J.t_off, in, all, P->aabb.as<int>() + 8 * i,
+                    P->list_v.as<int>(), P->list_b.as<double>(), P->n_sm, flags, s);
     CH_CUDA(cudaGetLastError());
   }
   CH_CUDA(cudaEventRecord(P->ev[1], s));
@@ -551,14 +586,21 @@ ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, 
     std::memset(&C, 0, sizeof(C));
     cuuint64_t gdim[3] = {(cuuint64_t)J.g.n[2], (cuuint64_t)J.g.n[1], (cuuint64_t)J.g.n[0]};
     cuuint64_t gstride[2] = {(cuuint64_t)J.g.zp * 4, (cuuint64_t)J.g.zp * J.g.n[1] * 4};
-    cuuint32_t box[3] = {(cuuint32_t)WZ, (cuuint32_t)BOX_Y, 1};
     cuuint32_t estr[3] = {1, 1, 1};
-    CUresult r = enc(&C.tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)(P->T.as<float>() + J.t_off), gdim, gstride,
-                     box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    for (int v = 0; v < N_VARIANTS; ++v) {
+      for (int ex = TX; ex <= var_max_ex(v); ++ex) {
+        cuuint32_t box[3] = {(cuuint32_t)var_p(v), (cuuint32_t)var_rows(v), (cuuint32_t)ex};
+        CUresult r = enc(&C.tmap[tmap_index(v, ex)], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                         (void*)(P->T.as<float>() + J.t_off), gdim, gstride, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS)
+          return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+      }
+    }
     C.dose = J.dose;
     C.ranges = P->ranges.as<uint32_t>() + J.r_off;
+    C.cranges = P->cranges.as<uint32_t>() + J.r_off;
     for (int k = 0; k < 3; ++k) {
       C.n[k] = J.g.n[k];
       C.ntile[k] = J.ntile[k];
@@ -579,6 +621,7 @@ ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, 
     make_planes(J.beam, J.grid, J.b, R);
     R.aabb = P->aabb.as<int>() + 8 * i;
     R.ranges = P->ranges.as<uint32_t>() + J.r_off;
+    R.cranges = P->cranges.as<uint32_t>() + J.r_off;
   }
   CH_CUDA(cudaMemcpyAsync(P->cone_beams.p, cb.data(), n * sizeof(ConeBeam), cudaMemcpyHostToDevice, s));
   CH_CUDA(cudaMemcpyAsync(P->range_beams.p, rb.data(), n * sizeof(RangeBeam), cudaMemcpyHostToDevice, s));

@@ -10,21 +10,39 @@
 namespace ch {
 
 // ------------------------------------------------------------------ sizes --
-// Cone gather tile: 32 (z, lanes) x 16 (y, per-thread run) x 8 (x, warps).
-constexpr int TZ = 32, TY = 16, TX = 8;
+// Cone gather tile: 16 (x) x 16 (y) x 16 (z) outputs.  Half a warp covers 16
+// consecutive z of one y row, the other half the same z two rows further
+// (y + 2); each thread holds the 16 x values of its (y, z) column in
+// registers; 8 consumer warps cover the 16 y rows.
+constexpr int TZ = 16, TY = 16, TX = 16;
 constexpr int TILE_VOX = TZ * TY * TX;
-// Shared-memory window per pipeline slot; a chunk of taps may span at most
-// SPAN_Z/SPAN_Y/SPAN_X voxels along z/y/x (z also absorbs the 4-float TMA
-// alignment of the window origin).
-constexpr int WZ = 48, WY = 24, WX = 16;
-constexpr int SPAN_Z = WZ - TZ - 3;   // 13
-constexpr int SPAN_Y = WY - TY;       // 8
-constexpr int SPAN_X = WX - TX;       // 8
-constexpr int WIN_FLOATS = WZ * WY * WX;
-constexpr int BOX_Y = 8;              // TMA box: 48 (z) x 8 (y) x 1 (x) floats
-constexpr int BOX_BYTES = WZ * BOX_Y * 4;
+constexpr int OUT_PER_THREAD = TX;
+// Shared-memory window of a chunk: [x][row][z] with z pitch P and `rows` y
+// rows per x slice.  Three shapes ("variants") trade z reach for x reach in
+// one fixed slot; the chunker picks the cheapest that holds the chunk.  Every
+// P is 8 mod 16, so the two half-warps (rows y and y + 2, 2P = 16 mod 32) hit
+// disjoint banks.  The TMA box of variant v is P x 8 x 1 floats.
+constexpr int N_VARIANTS = 3;
+__host__ __device__ constexpr int var_p(int v) { return v == 0 ? 24 : (v == 1 ? 40 : 56); }
+__host__ __device__ constexpr int var_rows(int v) { return v == 0 ? 32 : 24; }
+constexpr int WIN_FLOATS = 27648;     // one pipeline slot (108 KiB)
+__host__ __device__ constexpr int var_max_ex(int v) { return WIN_FLOATS / (var_p(v) * var_rows(v)); }
+// largest tap-offset spread a chunk may have along each axis in variant v
+// (z also absorbs the 4-float TMA alignment of the window origin)
+__host__ __device__ constexpr int var_span_z(int v) { return var_p(v) - TZ - 3; }
+__host__ __device__ constexpr int var_span_y(int v) { return var_rows(v) - TY; }
+__host__ __device__ constexpr int var_span_x(int v) { return var_max_ex(v) - TX; }
+constexpr int BOX_Y = 8;              // granularity of the y extent in the chunker
+// One TMA box loads a chunk's whole window: P x rows x ex floats, so every
+// (variant, x extent) pair has its own tensor map.
+__host__ __device__ constexpr int n_maps_before(int v) {
+  return v == 0 ? 0 : (v == 1 ? var_max_ex(0) - TX + 1 : (var_max_ex(0) - TX + 1) + (var_max_ex(1) - TX + 1));
+}
+constexpr int N_TMAPS = n_maps_before(2) + (var_max_ex(2) - TX + 1);
+__host__ __device__ constexpr int tmap_index(int v, int ex) { return n_maps_before(v) + (ex - TX); }
+constexpr int MAX_CHUNK_TAPS = 64;    // taps per chunk (their table is staged with the window)
 constexpr int N_SLOTS = 2;
-constexpr int CONE_CONSUMER_WARPS = TX;
+constexpr int CONE_CONSUMER_WARPS = TY / 2;
 constexpr int CONE_THREADS = (CONE_CONSUMER_WARPS + 1) * 32;
 constexpr int DIR_GROUP = 16;         // unique directions per work unit
 
@@ -117,15 +135,16 @@ __device__ __forceinline__ int dda_pick(const float* t) {
 constexpr uint32_t RANGE_EMPTY = 0xffffffffu;
 
 struct __align__(128) ConeBeam {
-  CUtensorMap tmap;       // TERMA volume (dims nz, ny, nx; pitch zp)
+  CUtensorMap tmap[N_TMAPS];  // TERMA volume (dims nz, ny, nx; pitch zp), box P x rows x ex per map
   float* dose;
   const uint32_t* ranges; // [n_tiles][n_dirs]
+  const uint32_t* cranges;
   int n[3];
   int ntile[3];
   int n_tiles;
   int unit_begin;
   int n_units;
-  int pad[3];
+  int pad[1];
 };
 static_assert(sizeof(ConeBeam) % 128 == 0, "ConeBeam must keep tensor maps aligned");
 
@@ -133,12 +152,14 @@ struct ConeDirs {
   int n_dirs;
   const int* tap_base;
   const int* tap_len;
-  const int2* taps;        // (window offset of O[m], float bits of w[m])
+  const int4* taps;        // window offset of O[m] in variants 0..2, float bits of w[m]
   const short4* offs;      // O[m] (x, y, z, step axis)
   const float* tvals;      // exit t of tap m
   const int* chunk_base;
   const int* n_chunks;
-  const int* chunk_start;
+  const int* chunk_start;  // first tap of each chunk (direction-local)
+  const int4* chunk_rec;   // 2 per chunk: {first, last, variant, span_x | span_y << 16},
+                           //              {max O_x, max O_y, max O_z, 0} over the chunk
   const float* dirs;       // unit direction (x, y, z)
 };
 
@@ -149,7 +170,8 @@ struct RangeBeam {
   float pa[4][3];
   float pk0[4];
   const int* aabb;
-  uint32_t* ranges;
+  uint32_t* ranges;        // [n_tiles][n_dirs]: first | last tap << 16, or RANGE_EMPTY
+  uint32_t* cranges;       // [n_tiles][n_dirs]: first | last chunk << 16 (direction-local)
 };
 
 struct Inter {
@@ -160,14 +182,15 @@ struct Inter {
 // ------------------------------------------------------------ launchers --
 void upload_unit_partials();
 void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const SettingsDev& s, float* T,
-                     const Inter& inter, int all_voxels, int* aabb, int* flags, cudaStream_t st);
+                     const Inter& inter, int all_voxels, int* aabb, int* list_v, double* list_b, int n_sm,
+                     int* flags, cudaStream_t st);
 void launch_stencil(const float* theta, int n_theta, const float* phi, int n_phi, const double* K, int n_r,
                     const float* spacing, const int* cap, int max_len, short4* off, float* t, float* dk,
                     int* len, float* dirs, cudaStream_t st);
 void launch_dda_trace(const int* n, const float* sp, int n_rays, const int* starts, const float* dirs, int cap,
                       int* vox, float* t, int* len, cudaStream_t st);
 void launch_scatter(const float* T, const int* n, int zp, int n_dirs, const int* tap_base, const int* tap_len,
-                    const short4* offs, const int2* taps, float* dose, cudaStream_t st);
+                    const short4* offs, const int4* taps, float* dose, cudaStream_t st);
 size_t cone_smem_bytes();
 cudaError_t setup_cone_kernel();
 void launch_range(const RangeBeam* rbs_dev, int n_beams, int max_tiles, const ConeDirs& D, cudaStream_t st);

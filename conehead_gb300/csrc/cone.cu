@@ -4,7 +4,7 @@
 //   dose(v) = sum_u sum_m T(v - O_u[m]) * w_u[m]
 //
 // u runs over the deduplicated cone directions, w_u = multiplicity * dK_u.
-// Work is split into units = (beam, 32x16x8 output tile, group of 16
+// Work is split into units = (beam, 16^3 output tile, group of 16
 // directions).  range_kernel first bounds, for every (tile, direction), the
 // taps m whose sources can hold TERMA: the source box of the tile must meet
 // the TERMA bounding box (exact, per axis, on the monotone offsets) and the
@@ -13,14 +13,16 @@
 // therefore reads only zero TERMA, so the result is exact.
 //
 // cone_gather_kernel is persistent and warp specialised:
-//   * warp 8 (producer) claims units from a global counter, splits each
-//     direction's tap range into chunks whose sources fit a 48x24x16-float
-//     shared-memory window, and fills the window with TMA tile loads
-//     (cp.async.bulk.tensor.3d, 48x8x1 boxes, out-of-grid reads zero-filled)
-//     into a two-slot mbarrier pipeline;
-//   * warps 0-7 (consumers) each own one x-slice of the tile; a thread holds
-//     16 outputs (its lane's z, 16 consecutive y) in registers and for every
-//     tap does 16 shared-memory loads + FMAs; on the unit's last chunk the
+//   * warp 8 (producer) claims units from a global counter, walks each
+//     direction's tap range chunk by chunk (chunks are cut on the host so
+//     their sources fit one of three window shapes in a 108 KiB slot), and
+//     fills the window with TMA tile loads (cp.async.bulk.tensor.3d, P x 8 x
+//     1 boxes sized to the chunk, out-of-grid reads zero-filled) into a
+//     two-slot mbarrier pipeline;
+//   * warps 0-7 (consumers): lanes cover 16 z x 2 y rows of the 16^3 tile and
+//     a thread holds the 16 x outputs of its (y, z) column in registers;
+//     every tap costs 16 shared-memory loads + FMAs per thread, with the next
+//     tap's offsets and weight prefetched; on the unit's last chunk the
 //     accumulators are added to the dose with red.global.add.f32.
 // Every mbarrier wait is bounded; on expiry the kernel records
 // FLAG_TIMEOUT and returns.
@@ -39,7 +41,7 @@ struct __align__(16) ChunkDesc {
   int x0w, y0w, z0w;
   int tx0, ty0, tz0;
   int beam, flags, ex;
-  int nyb, pad0, pad1, pad2;
+  int nyb, var, tb, pad;
 };
 
 // ------------------------------------------------------------- PTX glue --
@@ -75,6 +77,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
+// 1-D bulk copy global -> shared (both 16-byte aligned, size a multiple of 16)
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"((unsigned long long)src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1,
                                             int c2) {
   asm volatile(
@@ -162,7 +173,16 @@ __global__ void range_kernel(const RangeBeam* __restrict__ rbs, ConeDirs D) {
         mhi = -1;
       }
     }
-    if (mlo <= mhi) out = (uint32_t)mlo | ((uint32_t)mhi << 16);
+    if (mlo <= mhi) {
+      out = (uint32_t)mlo | ((uint32_t)mhi << 16);
+      // chunks holding the first and last tap
+      const int* cs = D.chunk_start + D.chunk_base[u];
+      const int nc = D.n_chunks[u];
+      auto ckey = [&](int c) { return (float)cs[c]; };
+      const int c_first = upper_bound(nc, (float)mlo, ckey) - 1;
+      const int c_last = upper_bound(nc, (float)mhi, ckey) - 1;
+      R.cranges[(long long)tile * D.n_dirs + u] = (uint32_t)c_first | ((uint32_t)c_last << 16);
+    }
   }
   R.ranges[(long long)tile * D.n_dirs + u] = out;
 }
@@ -170,8 +190,8 @@ __global__ void range_kernel(const RangeBeam* __restrict__ rbs, ConeDirs D) {
 // --------------------------------------------------------- gather pass --
 __device__ __forceinline__ void producer(const ConeBeam* __restrict__ beams, int n_beams, const ConeDirs& D,
                                          int total_units, int* unit_counter, unsigned long long* updates,
-                                         int* flags, float* win, ChunkDesc* desc, uint64_t* full,
-                                         uint64_t* empty) {
+                                         int* flags, float* win, int4* slot_taps, ChunkDesc* desc,
+                                         uint64_t* full, uint64_t* empty) {
   const int lane = threadIdx.x & 31;
   const int n_groups = (D.n_dirs + DIR_GROUP - 1) / DIR_GROUP;
   int k = 0;
@@ -183,20 +203,19 @@ __device__ __forceinline__ void producer(const ConeBeam* __restrict__ beams, int
     const uint32_t ph = (uint32_t)(k / N_SLOTS) & 1u;
     if (!mbar_wait(&empty[s], ph ^ 1u)) return false;
     const bool done = (d.flags & DESC_DONE) != 0;
-    const uint32_t bytes = done ? 0u : (uint32_t)(d.ex * d.nyb * BOX_BYTES);
+    const uint32_t tap_bytes = done ? 0u : (uint32_t)(d.b - d.a + 1) * (uint32_t)sizeof(int4);
+    const uint32_t win_bytes = done ? 0u : (uint32_t)(var_p(d.var) * var_rows(d.var) * d.ex * 4);
     if (lane == 0) {
       desc[s] = d;
-      mbar_arrive_expect_tx(&full[s], bytes);
-    }
-    __syncwarp();
-    if (!done) {
-      const CUtensorMap* map = &beams[d.beam].tmap;
-      float* slot = win + (size_t)s * WIN_FLOATS;
-      for (int q = lane; q < d.ex * d.nyb; q += 32) {
-        const int xs = q / d.nyb, yb = q % d.nyb;
-        tma_load_3d(slot + (xs * WY + yb * BOX_Y) * WZ, map, &full[s], d.z0w, d.y0w + yb * BOX_Y, d.x0w + xs);
+      mbar_arrive_expect_tx(&full[s], win_bytes + tap_bytes);
+      if (!done) {
+        // the whole window in one TMA box, the chunk's taps in one bulk copy
+        tma_load_3d(win + (size_t)s * WIN_FLOATS, &beams[d.beam].tmap[tmap_index(d.var, d.ex)], &full[s], d.z0w,
+                    d.y0w, d.x0w);
+        bulk_load(slot_taps + (size_t)s * MAX_CHUNK_TAPS, D.taps + d.tb + d.a, tap_bytes, &full[s]);
       }
     }
+    __syncwarp();
     ++k;
     return true;
   };
@@ -214,39 +233,64 @@ __device__ __forceinline__ void producer(const ConeBeam* __restrict__ beams, int
     const int tx0 = (tile / (B.ntile[1] * B.ntile[2])) * TX;
     const int ty0 = ((tile / B.ntile[2]) % B.ntile[1]) * TY;
     const int tz0 = (tile % B.ntile[2]) * TZ;
-    const int u_end = min(D.n_dirs, (g + 1) * DIR_GROUP);
+    // lanes 0..15 fetch the ranges of the group's directions in parallel
+    const int u0 = g * DIR_GROUP;
+    uint32_t r = RANGE_EMPTY, cr = 0;
+    int cb = 0, tb = 0;
+    if (lane < DIR_GROUP && u0 + lane < D.n_dirs) {
+      const long long ri = (long long)tile * D.n_dirs + u0 + lane;
+      r = __ldg(B.ranges + ri);
+      if (r != RANGE_EMPTY) {
+        cr = __ldg(B.cranges + ri);
+        cb = __ldg(D.chunk_base + u0 + lane);
+        tb = __ldg(D.tap_base + u0 + lane);
+      }
+    }
+    unsigned act = __ballot_sync(0xffffffffu, r != RANGE_EMPTY);
     unsigned long long work = 0;
-    for (int u = g * DIR_GROUP; u < u_end && ok; ++u) {
-      const uint32_t r = __ldg(B.ranges + (long long)tile * D.n_dirs + u);
-      if (r == RANGE_EMPTY) continue;
-      const int mlo = (int)(r & 0xffffu), mhi = (int)(r >> 16);
-      const int cb = D.chunk_base[u], nc = D.n_chunks[u], tb = D.tap_base[u], L = D.tap_len[u];
-      for (int c = 0; c < nc && ok; ++c) {
-        const int ca = D.chunk_start[cb + c];
-        const int ce = (c + 1 < nc) ? D.chunk_start[cb + c + 1] - 1 : L - 1;
-        if (ce < mlo) continue;
-        if (ca > mhi) break;
-        const int a = max(ca, mlo), b = min(ce, mhi);
-        const short4 oa = D.offs[tb + a], ob = D.offs[tb + b];
-        ChunkDesc d;
-        d.u = u;
-        d.a = a;
-        d.b = b;
-        d.x0w = tx0 - max((int)oa.x, (int)ob.x);
-        d.y0w = ty0 - max((int)oa.y, (int)ob.y);
-        d.z0w = (tz0 - max((int)oa.z, (int)ob.z)) & ~3;
-        d.tx0 = tx0;
-        d.ty0 = ty0;
-        d.tz0 = tz0;
-        d.beam = bi;
-        d.flags = 0;
-        d.ex = TX + abs((int)ob.x - (int)oa.x);
-        d.nyb = (TY + abs((int)ob.y - (int)oa.y) + BOX_Y - 1) / BOX_Y;
-        d.pad0 = d.pad1 = d.pad2 = 0;
-        work += (unsigned long long)(b - a + 1);
-        if (have) ok = emit(pend);
-        pend = d;
-        have = true;
+    while (act && ok) {
+      const int j = __ffs(act) - 1;
+      act &= act - 1;
+      const uint32_t rj = __shfl_sync(0xffffffffu, r, j), crj = __shfl_sync(0xffffffffu, cr, j);
+      const int cbj = __shfl_sync(0xffffffffu, cb, j), tbj = __shfl_sync(0xffffffffu, tb, j);
+      const int mlo = (int)(rj & 0xffffu), mhi = (int)(rj >> 16);
+      const int c_first = (int)(crj & 0xffffu), c_last = (int)(crj >> 16);
+      for (int c0 = c_first; c0 <= c_last && ok; c0 += 32) {
+        // lanes fetch up to 32 chunk records at once
+        int4 r0 = make_int4(0, 0, 0, 0), r1 = make_int4(0, 0, 0, 0);
+        if (c0 + lane <= c_last) {
+          r0 = __ldg(D.chunk_rec + 2 * (cbj + c0 + lane));
+          r1 = __ldg(D.chunk_rec + 2 * (cbj + c0 + lane) + 1);
+        }
+        const int nrec = min(32, c_last - c0 + 1);
+        for (int q = 0; q < nrec && ok; ++q) {
+          const int a0 = __shfl_sync(0xffffffffu, r0.x, q), b0 = __shfl_sync(0xffffffffu, r0.y, q);
+          const int var = __shfl_sync(0xffffffffu, r0.z, q), sxy = __shfl_sync(0xffffffffu, r0.w, q);
+          const int mox = __shfl_sync(0xffffffffu, r1.x, q), moy = __shfl_sync(0xffffffffu, r1.y, q);
+          const int moz = __shfl_sync(0xffffffffu, r1.z, q);
+          ChunkDesc d;
+          d.u = u0 + j;
+          d.a = max(a0, mlo);
+          d.b = min(b0, mhi);
+          // window of the whole chunk (covers the clipped taps too)
+          d.x0w = tx0 - mox;
+          d.y0w = ty0 - moy;
+          d.z0w = (tz0 - moz) & ~3;
+          d.tx0 = tx0;
+          d.ty0 = ty0;
+          d.tz0 = tz0;
+          d.beam = bi;
+          d.flags = 0;
+          d.ex = TX + (sxy & 0xffff);
+          d.nyb = 0;
+          d.var = var;
+          d.tb = tbj;
+          d.pad = 0;
+          work += (unsigned long long)(d.b - d.a + 1);
+          if (have) ok = emit(pend);
+          pend = d;
+          have = true;
+        }
       }
     }
     if (have && ok) {
@@ -268,13 +312,34 @@ __device__ __forceinline__ void producer(const ConeBeam* __restrict__ beams, int
   }
 }
 
-__device__ __forceinline__ void consumer(const ConeBeam* __restrict__ beams, const ConeDirs& D, int* flags,
-                                         const float* win, const ChunkDesc* desc, uint64_t* full,
-                                         uint64_t* empty) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float acc[TY];
+// One chunk of taps for one thread: 16 outputs (x = 0..15) of its (y, z)
+// column; window variant V fixes the pitches at compile time.
+template <int V>
+__device__ __forceinline__ void consume_chunk(const float* w, const int4* tp, int n_taps, int base0, float* acc) {
+  constexpr int XS = var_rows(V) * var_p(V);
+  // the chunk's taps sit in shared memory next to its window; the next one
+  // is read an iteration ahead
+  int4 next = tp[0];
+  for (int m = 0; m < n_taps; ++m) {
+    const int4 tap = next;
+    if (m + 1 < n_taps) next = tp[m + 1];
+    const int toff = V == 0 ? tap.x : (V == 1 ? tap.y : tap.z);
+    const float wt = __int_as_float(tap.w);
+    const float* src = w + (base0 - toff);
 #pragma unroll
-  for (int i = 0; i < TY; ++i) acc[i] = 0.0f;
+    for (int i = 0; i < OUT_PER_THREAD; ++i) acc[i] = fmaf(wt, src[i * XS], acc[i]);
+  }
+}
+
+__device__ __forceinline__ void consumer(const ConeBeam* __restrict__ beams, const ConeDirs& D, int* flags,
+                                         const float* win, const int4* slot_taps, const ChunkDesc* desc,
+                                         uint64_t* full, uint64_t* empty) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int zl = lane & 15;                                      // z within the tile
+  const int yl = (warp & 1) + 4 * (warp >> 1) + 2 * (lane >> 4); // y within the tile
+  float acc[OUT_PER_THREAD];                                     // x = 0 .. TX-1
+#pragma unroll
+  for (int i = 0; i < OUT_PER_THREAD; ++i) acc[i] = 0.0f;
   for (int k = 0;; ++k) {
     const int s = k % N_SLOTS;
     if (!mbar_wait(&full[s], (uint32_t)(k / N_SLOTS) & 1u)) {
@@ -284,28 +349,27 @@ __device__ __forceinline__ void consumer(const ConeBeam* __restrict__ beams, con
     const ChunkDesc d = desc[s];
     if (d.flags & DESC_DONE) break;
     const float* w = win + (size_t)s * WIN_FLOATS;
-    const int base0 = ((d.tx0 + warp - d.x0w) * WY + (d.ty0 - d.y0w)) * WZ + (d.tz0 + lane - d.z0w);
-    const int2* tp = D.taps + D.tap_base[d.u];
-    for (int m = d.a; m <= d.b; ++m) {
-      const int2 tap = __ldg(tp + m);
-      const float wt = __int_as_float(tap.y);
-      const float* src = w + (base0 - tap.x);
-#pragma unroll
-      for (int i = 0; i < TY; ++i) acc[i] = fmaf(wt, src[i * WZ], acc[i]);
-    }
+    const int4* tp = slot_taps + (size_t)s * MAX_CHUNK_TAPS;
+    const int nt = d.b - d.a + 1;
+    const int rows = var_rows(d.var), P = var_p(d.var);
+    const int base0 = ((d.tx0 - d.x0w) * rows + (d.ty0 + yl - d.y0w)) * P + (d.tz0 + zl - d.z0w);
+    if (d.var == 0) consume_chunk<0>(w, tp, nt, base0, acc);
+    else if (d.var == 1) consume_chunk<1>(w, tp, nt, base0, acc);
+    else consume_chunk<2>(w, tp, nt, base0, acc);
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
     if (d.flags & DESC_LAST) {
       const ConeBeam& B = beams[d.beam];
-      const int x = d.tx0 + warp, z = d.tz0 + lane;
-      if (x < B.n[0] && z < B.n[2]) {
-        float* out = B.dose + ((long long)x * B.n[1] + d.ty0) * B.n[2] + z;
+      const int y = d.ty0 + yl, z = d.tz0 + zl;
+      if (y < B.n[1] && z < B.n[2]) {
+        float* out = B.dose + ((long long)d.tx0 * B.n[1] + y) * B.n[2] + z;
+        const long long xs = (long long)B.n[1] * B.n[2];
 #pragma unroll
-        for (int i = 0; i < TY; ++i)
-          if (d.ty0 + i < B.n[1]) atomicAdd(out + (long long)i * B.n[2], acc[i]);
+        for (int i = 0; i < OUT_PER_THREAD; ++i)
+          if (d.tx0 + i < B.n[0]) atomicAdd(out + i * xs, acc[i]);
       }
 #pragma unroll
-      for (int i = 0; i < TY; ++i) acc[i] = 0.0f;
+      for (int i = 0; i < OUT_PER_THREAD; ++i) acc[i] = 0.0f;
     }
   }
 }
@@ -318,7 +382,8 @@ __global__ void __launch_bounds__(CONE_THREADS, 1)
   const uint32_t base = smem_u32(smem_raw);
   unsigned char* sm = smem_raw + ((1024u - (base & 1023u)) & 1023u);
   float* win = reinterpret_cast<float*>(sm);
-  ChunkDesc* desc = reinterpret_cast<ChunkDesc*>(sm + (size_t)N_SLOTS * WIN_FLOATS * 4);
+  int4* slot_taps = reinterpret_cast<int4*>(sm + (size_t)N_SLOTS * WIN_FLOATS * 4);
+  ChunkDesc* desc = reinterpret_cast<ChunkDesc*>(slot_taps + N_SLOTS * MAX_CHUNK_TAPS);
   uint64_t* full = reinterpret_cast<uint64_t*>(desc + N_SLOTS);
   uint64_t* empty = full + N_SLOTS;
   if (threadIdx.x == 0) {
@@ -330,13 +395,14 @@ __global__ void __launch_bounds__(CONE_THREADS, 1)
   }
   __syncthreads();
   if ((threadIdx.x >> 5) == CONE_CONSUMER_WARPS)
-    producer(beams, n_beams, D, total_units, unit_counter, updates, flags, win, desc, full, empty);
+    producer(beams, n_beams, D, total_units, unit_counter, updates, flags, win, slot_taps, desc, full, empty);
   else
-    consumer(beams, D, flags, win, desc, full, empty);
+    consumer(beams, D, flags, win, slot_taps, desc, full, empty);
 }
 
 size_t cone_smem_bytes() {
-  return 1024 + (size_t)N_SLOTS * WIN_FLOATS * 4 + N_SLOTS * sizeof(ChunkDesc) + 2 * N_SLOTS * sizeof(uint64_t);
+  return 1024 + (size_t)N_SLOTS * WIN_FLOATS * 4 + (size_t)N_SLOTS * MAX_CHUNK_TAPS * sizeof(int4) +
+         N_SLOTS * sizeof(ChunkDesc) + 2 * N_SLOTS * sizeof(uint64_t);
 }
 
 cudaError_t setup_cone_kernel() {

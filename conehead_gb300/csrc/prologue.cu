@@ -197,14 +197,11 @@ __device__ double blocked_fraction(const BeamDev& b, const GridDev& g, int S, co
 }
 
 // ------------------------------------------------------------------ DDA --
-__device__ __forceinline__ float rho_at(const float* __restrict__ rho, const GridDev& g, int x, int y,
-                                        int z) {
-  const long long idx = g.swap_xy ? ((long long)y * g.n[0] + x) * g.n[2] + z
-                                  : ((long long)x * g.n[1] + y) * g.n[2] + z;
-  return __ldg(rho + idx);
-}
+// radiological depth from voxel (x, y, z) toward the source (cuda_d_eff).
+// The walk is generated UNROLL steps at a time so their density loads are
+// in flight together; the float32 accumulation keeps the reference order.
+constexpr int DDA_UNROLL = 8;
 
-// radiological depth from voxel (x, y, z) toward the source (cuda_d_eff)
 __device__ float radiological_depth(const float* __restrict__ rho, const GridDev& g, int x, int y, int z,
                                     const float* rd) {
   const float mag = __fsqrt_rn(fadd(fadd(fmul(rd[0], rd[0]), fmul(rd[1], rd[1])), fmul(rd[2], rd[2])));
@@ -213,49 +210,74 @@ __device__ float radiological_depth(const float* __restrict__ rho, const GridDev
   dda_axis(fdiv(rd[0], mag), g.spacing[0], s0, t0, d0);
   dda_axis(fdiv(rd[1], mag), g.spacing[1], s1, t1, d1);
   dda_axis(fdiv(rd[2], mag), g.spacing[2], s2, t2, d2);
+  const int n0 = g.n[0], n1 = g.n[1], n2 = g.n[2];
+  // linear index of the density the reference reads at (x, y, z) and its
+  // step along each grid axis (x and y swapped when swap_xy)
+  // (volumes are limited to < 2^31 voxels by the host, so 32-bit indices)
+  const int st0 = g.swap_xy ? n2 : n1 * n2;
+  const int st1 = g.swap_xy ? n0 * n2 : n2;
+  int idx = g.swap_xy ? (y * n0 + x) * n2 + z : (x * n1 + y) * n2 + z;
+  const int dx = s0 * st0, dy = s1 * st1, dz = s2;
   int cx = x, cy = y, cz = z;
   float deff = 0.0f, tprev = 0.0f;
-  bool first = true;
-  const int n0 = g.n[0], n1 = g.n[1], n2 = g.n[2];
-  while (cx >= 0 && cx < n0 && cy >= 0 && cy < n1 && cz >= 0 && cz < n2) {
-    const float r = rho_at(rho, g, cx, cy, cz);
-    float tv;
-    if (t0 < t1) {
-      if (t0 < t2) { tv = t0; t0 = fadd(t0, d0); cx += s0; }
-      else { tv = t2; t2 = fadd(t2, d2); cz += s2; }
-    } else {
-      if (t1 < t2) { tv = t1; t1 = fadd(t1, d1); cy += s1; }
-      else { tv = t2; t2 = fadd(t2, d2); cz += s2; }
+  bool first = true, inside = true;
+  while (inside) {
+    int vi[DDA_UNROLL];
+    float tv[DDA_UNROLL];
+    int cnt = 0;
+#pragma unroll
+    for (int q = 0; q < DDA_UNROLL; ++q) {
+      if (inside) {
+        vi[q] = idx;
+        if (t0 < t1) {
+          if (t0 < t2) { tv[q] = t0; t0 = fadd(t0, d0); cx += s0; idx += dx; }
+          else { tv[q] = t2; t2 = fadd(t2, d2); cz += s2; idx += dz; }
+        } else {
+          if (t1 < t2) { tv[q] = t1; t1 = fadd(t1, d1); cy += s1; idx += dy; }
+          else { tv[q] = t2; t2 = fadd(t2, d2); cz += s2; idx += dz; }
+        }
+        cnt = q + 1;
+        inside = cx >= 0 && cx < n0 && cy >= 0 && cy < n1 && cz >= 0 && cz < n2;
+      }
     }
-    // the reference accumulates in the returned order: voxel v, exit t_v
-    deff = first ? fadd(deff, fmul(r, tv)) : fadd(deff, fmul(r, fsub(tv, tprev)));
-    first = false;
-    tprev = tv;
+    float r[DDA_UNROLL];
+#pragma unroll
+    for (int q = 0; q < DDA_UNROLL; ++q) r[q] = q < cnt ? __ldg(rho + vi[q]) : 0.0f;
+#pragma unroll
+    for (int q = 0; q < DDA_UNROLL; ++q) {
+      if (q < cnt) {
+        deff = first ? fadd(deff, fmul(r[q], tv[q])) : fadd(deff, fmul(r[q], fsub(tv[q], tprev)));
+        first = false;
+        tprev = tv[q];
+      }
+    }
   }
   return deff;
 }
 
-// -------------------------------------------------------------- kernel --
-__global__ void __launch_bounds__(256) prologue_kernel(
-    const float* __restrict__ rho, GridDev g, BeamDev b, SettingsDev s, float* __restrict__ T,
-    Inter inter, int all_voxels, int* __restrict__ aabb, int* __restrict__ flags) {
+// ------------------------------------------------------------ kernels --
+// Pass 1, every voxel: cull, blocked fraction; voxels the beam reaches (or
+// every voxel when intermediates are requested) go to a compact list so the
+// depth/TERMA pass runs on full warps.
+__global__ void __launch_bounds__(256) blocked_kernel(GridDev g, BeamDev b, SettingsDev s,
+                                                      float* __restrict__ T, Inter inter, int all_voxels,
+                                                      int* __restrict__ list_count, int* __restrict__ list_v,
+                                                      double* __restrict__ list_b, int* __restrict__ flags) {
   const long long N = (long long)g.n[0] * g.n[1] * g.n[2];
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = v < N;
-  int x = 0, y = 0, z = 0;
-  float Tv = 0.0f;
   int bad = 0;
+  double blocked = 0.0;
+  bool keep = false;
   if (live) {
-    z = (int)(v % g.n[2]);
+    const int z = (int)(v % g.n[2]);
     const long long r = v / g.n[2];
-    y = (int)(r % g.n[1]);
-    x = (int)(r / g.n[1]);
+    const int y = (int)(r % g.n[1]);
+    const int x = (int)(r / g.n[1]);
     float pos[3];
     pos[0] = voxel_centre(g.origin[0], g.spacing[0], x);
     pos[1] = voxel_centre(g.origin[1], g.spacing[1], y);
     pos[2] = voxel_centre(g.origin[2], g.spacing[2], z);
-
-    // ---- cull: voxels whose every sub-sample misses the open block region
     bool candidate = true;
     if (b.cull_enable) {
       const float np_ = b.vyf[0] * pos[0] + b.vyf[1] * pos[1] + b.vyf[2] * pos[2];
@@ -274,10 +296,60 @@ __global__ void __launch_bounds__(256) prologue_kernel(
           candidate = false;
       }
     }
-    double blocked = 0.0;
     if (candidate) blocked = blocked_fraction(b, g, s.samples, pos, bad);
+    keep = blocked != 0.0 || all_voxels;
+    T[((long long)x * g.n[1] + y) * g.zp + z] = 0.0f;
+    if (inter.blocked) inter.blocked[v] = blocked;
+    if (!keep) {
+      if (inter.d_eff) inter.d_eff[v] = 0.0f;
+      if (inter.oad) inter.oad[v] = 0.0f;
+      if (inter.fluence) inter.fluence[v] = 0.0f;
+      if (inter.f_soften) inter.f_soften[v] = 1.0f;
+      if (inter.f_horn) inter.f_horn[v] = 1.0f;
+      if (inter.terma) inter.terma[v] = 0.0f;
+    }
+  }
+  const unsigned m = __ballot_sync(0xffffffffu, keep);
+  if (m) {
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(list_count, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (keep) {
+      const int slot = base + __popc(m & ((1u << lane) - 1u));
+      list_v[slot] = (int)v;
+      list_b[slot] = blocked;
+    }
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flags, FLAG_PARALLEL_RAY);
+}
 
-    if (blocked != 0.0 || all_voxels) {
+// Pass 2, listed voxels: radiological depth, oad, fluence, softening/horn,
+// TERMA; TERMA support box for the cone stage.
+__global__ void __launch_bounds__(256) terma_kernel(const float* __restrict__ rho, GridDev g, BeamDev b,
+                                                    SettingsDev s, float* __restrict__ T, Inter inter,
+                                                    const int* __restrict__ list_count,
+                                                    const int* __restrict__ list_v,
+                                                    const double* __restrict__ list_b, int* __restrict__ aabb,
+                                                    int* __restrict__ flags) {
+  const int count = *list_count;
+  const int rounds = (count + blockDim.x * gridDim.x - 1) / (blockDim.x * gridDim.x);
+  for (int it = 0; it < rounds; ++it) {
+    const int e = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
+    const bool live = e < count;
+    int x = 0, y = 0, z = 0, bad = 0;
+    float Tv = 0.0f;
+    if (live) {
+      const long long v = list_v[e];
+      const double blocked = list_b[e];
+      z = (int)(v % g.n[2]);
+      const long long r = v / g.n[2];
+      y = (int)(r % g.n[1]);
+      x = (int)(r / g.n[1]);
+      float pos[3];
+      pos[0] = voxel_centre(g.origin[0], g.spacing[0], x);
+      pos[1] = voxel_centre(g.origin[1], g.spacing[1], y);
+      pos[2] = voxel_centre(g.origin[2], g.spacing[2], z);
       float rd[3];
       ray_to_source(b, pos, rd);
       // ---- radiological depth (float32, exact mirror)
@@ -309,49 +381,42 @@ __global__ void __launch_bounds__(256) prologue_kernel(
       // ---- TERMA (float32, reference order)
       float terma = 0.0f;
       for (int i = 0; i < s.n_energy; ++i) {
-        const float e = expf(fmul(fmul(-s.mu[i], fs), deff));
-        terma = fadd(terma, fmul(fmul(fmul(fmul(fmul(s.w[i], fluence), e), s.E[i]), s.mu[i]), fh));
+        const float ex = expf(fmul(fmul(-s.mu[i], fs), deff));
+        terma = fadd(terma, fmul(fmul(fmul(fmul(fmul(s.w[i], fluence), ex), s.E[i]), s.mu[i]), fh));
       }
       Tv = d2f(dmul((double)terma, blocked));
+      T[((long long)x * g.n[1] + y) * g.zp + z] = Tv;
       if (inter.d_eff) inter.d_eff[v] = deff;
       if (inter.oad) inter.oad[v] = oad;
       if (inter.fluence) inter.fluence[v] = fluence;
       if (inter.f_soften) inter.f_soften[v] = fs;
       if (inter.f_horn) inter.f_horn[v] = fh;
-    } else {
-      if (inter.d_eff) inter.d_eff[v] = 0.0f;
-      if (inter.oad) inter.oad[v] = 0.0f;
-      if (inter.fluence) inter.fluence[v] = 0.0f;
-      if (inter.f_soften) inter.f_soften[v] = 1.0f;
-      if (inter.f_horn) inter.f_horn[v] = 1.0f;
+      if (inter.terma) inter.terma[v] = Tv;
     }
-    if (inter.blocked) inter.blocked[v] = blocked;
-    if (inter.terma) inter.terma[v] = Tv;
-    T[((long long)x * g.n[1] + y) * g.zp + z] = Tv;
-  }
-  // ---- support box of T != 0 (reference skips T == 0 sources)
-  const bool nz_ = live && Tv != 0.0f;
-  const unsigned m = __ballot_sync(0xffffffffu, nz_);
-  if (m) {
-    int lo0 = nz_ ? x : INT_MAX, hi0 = nz_ ? x : INT_MIN;
-    int lo1 = nz_ ? y : INT_MAX, hi1 = nz_ ? y : INT_MIN;
-    int lo2 = nz_ ? z : INT_MAX, hi2 = nz_ ? z : INT_MIN;
+    // ---- support box of T != 0 (the reference skips T == 0 sources)
+    const bool nz_ = live && Tv != 0.0f;
+    const unsigned m = __ballot_sync(0xffffffffu, nz_);
+    if (m) {
+      int lo0 = nz_ ? x : INT_MAX, hi0 = nz_ ? x : INT_MIN;
+      int lo1 = nz_ ? y : INT_MAX, hi1 = nz_ ? y : INT_MIN;
+      int lo2 = nz_ ? z : INT_MAX, hi2 = nz_ ? z : INT_MIN;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      lo0 = min(lo0, __shfl_xor_sync(0xffffffffu, lo0, o));
-      hi0 = max(hi0, __shfl_xor_sync(0xffffffffu, hi0, o));
-      lo1 = min(lo1, __shfl_xor_sync(0xffffffffu, lo1, o));
-      hi1 = max(hi1, __shfl_xor_sync(0xffffffffu, hi1, o));
-      lo2 = min(lo2, __shfl_xor_sync(0xffffffffu, lo2, o));
-      hi2 = max(hi2, __shfl_xor_sync(0xffffffffu, hi2, o));
+      for (int o = 16; o > 0; o >>= 1) {
+        lo0 = min(lo0, __shfl_xor_sync(0xffffffffu, lo0, o));
+        hi0 = max(hi0, __shfl_xor_sync(0xffffffffu, hi0, o));
+        lo1 = min(lo1, __shfl_xor_sync(0xffffffffu, lo1, o));
+        hi1 = max(hi1, __shfl_xor_sync(0xffffffffu, hi1, o));
+        lo2 = min(lo2, __shfl_xor_sync(0xffffffffu, lo2, o));
+        hi2 = max(hi2, __shfl_xor_sync(0xffffffffu, hi2, o));
+      }
+      if ((threadIdx.x & 31) == 0) {
+        atomicMin(aabb + 0, lo0); atomicMax(aabb + 1, hi0);
+        atomicMin(aabb + 2, lo1); atomicMax(aabb + 3, hi1);
+        atomicMin(aabb + 4, lo2); atomicMax(aabb + 5, hi2);
+      }
     }
-    if ((threadIdx.x & 31) == 0) {
-      atomicMin(aabb + 0, lo0); atomicMax(aabb + 1, hi0);
-      atomicMin(aabb + 2, lo1); atomicMax(aabb + 3, hi1);
-      atomicMin(aabb + 4, lo2); atomicMax(aabb + 5, hi2);
-    }
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flags, FLAG_PARALLEL_RAY);
   }
-  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flags, FLAG_PARALLEL_RAY);
 }
 
 void upload_unit_partials() {
@@ -362,18 +427,25 @@ void upload_unit_partials() {
   cudaMemcpyToSymbol(c_unit_partial, p, sizeof(p));
 }
 
-void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const SettingsDev& s,
-                     float* T, const Inter& inter, int all_voxels, int* aabb, int* flags,
-                     cudaStream_t st) {
+void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const SettingsDev& s, float* T,
+                     const Inter& inter, int all_voxels, int* aabb, int* list_v, double* list_b, int n_sm,
+                     int* flags, cudaStream_t st) {
   const long long N = (long long)g.n[0] * g.n[1] * g.n[2];
   const int threads = 256;
   const long long blocks = (N + threads - 1) / threads;
-  prologue_kernel<<<(unsigned)blocks, threads, 0, st>>>(rho, g, b, s, T, inter, all_voxels, aabb, flags);
+  int* list_count = aabb + 6;
+  blocked_kernel<<<(unsigned)blocks, threads, 0, st>>>(g, b, s, T, inter, all_voxels, list_count, list_v, list_b,
+                                                       flags);
+  const long long want = (N + threads - 1) / threads;
+  const int grid = (int)(want < (long long)n_sm * 8 ? want : (long long)n_sm * 8);
+  terma_kernel<<<grid > 0 ? grid : 1, threads, 0, st>>>(rho, g, b, s, T, inter, list_count, list_v, list_b, aabb,
+                                                        flags);
 }
 
 __global__ void init_scratch_kernel(int* aabb, int n_beams, int* counters) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n_beams * 8) aabb[i] = (i % 2 == 0) ? INT_MAX : INT_MIN;
+  // per beam: lo/hi pairs of the TERMA box, then the prologue list count
+  if (i < n_beams * 8) aabb[i] = (i % 8 >= 6) ? 0 : ((i % 2 == 0) ? INT_MAX : INT_MIN);
   if (i < 8) counters[i] = 0;
 }
 

@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(128) scatter_kernel(const float* __restrict__ 
                                                       int zp, int n_dirs, const int* __restrict__ tap_base,
                                                       const int* __restrict__ tap_len,
                                                       const short4* __restrict__ offs,
-                                                      const int2* __restrict__ taps, float* __restrict__ dose) {
+                                                      const int4* __restrict__ taps, float* __restrict__ dose) {
   const long long N = (long long)n0 * n1 * n2;
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= N) return;
@@ -160,13 +160,13 @@ __global__ void __launch_bounds__(128) scatter_kernel(const float* __restrict__ 
       const short4 o = offs[b + m];
       const int tx = x + o.x, ty = y + o.y, tz = z + o.z;
       if (tx < 0 || tx >= n0 || ty < 0 || ty >= n1 || tz < 0 || tz >= n2) break;
-      atomicAdd(dose + ((long long)tx * n1 + ty) * n2 + tz, Tv * __int_as_float(taps[b + m].y));
+      atomicAdd(dose + ((long long)tx * n1 + ty) * n2 + tz, Tv * __int_as_float(taps[b + m].w));
     }
   }
 }
 
 void launch_scatter(const float* T, const int* n, int zp, int n_dirs, const int* tap_base, const int* tap_len,
-                    const short4* offs, const int2* taps, float* dose, cudaStream_t st) {
+                    const short4* offs, const int4* taps, float* dose, cudaStream_t st) {
   const long long N = (long long)n[0] * n[1] * n[2];
   scatter_kernel<<<(unsigned)((N + 127) / 128), 128, 0, st>>>(T, n[0], n[1], n[2], zp, n_dirs, tap_base, tap_len,
                                                               offs, taps, dose);
