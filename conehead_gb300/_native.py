@@ -74,6 +74,7 @@ SIGNATURES = {
     "ch_dose_batch": (ctypes.c_int, [VP, ctypes.c_int, P(Grid), P(VP), P(ctypes.c_int), P(Beam),
                                      P(Settings), P(VP), VP]),
     "ch_dose_scatter": (ctypes.c_int, [VP, P(Grid), VP, ctypes.c_int, P(Beam), P(Settings), VP, VP]),
+    "ch_dose_static": (ctypes.c_int, [VP, P(Grid), VP, ctypes.c_int, P(Beam), P(Settings), VP, VP]),
     "ch_dda_trace": (ctypes.c_int, [P(Grid), ctypes.c_int, VP, VP, ctypes.c_int, VP, VP, VP, VP]),
     "ch_cone_directions": (ctypes.c_int, [VP, VP, VP]),
     "ch_plan_sync": (ctypes.c_int, [VP, VP]),

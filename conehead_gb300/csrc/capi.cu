@@ -641,6 +641,42 @@ ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, 
 
 }  // namespace
 
+// ------------------------------------------------------ static scratch --
+// Scratch of ch_dose_static: a fixed device array, so that call allocates
+// nothing.  It holds one beam's TERMA volume, the prologue voxel list, the
+// tile range tables and the launch records; 36 MiB covers a 128^3 grid.
+// The array belongs to this library's module and stays allocated on every
+// GPU that uses it until the process exits.
+#define CH_STATIC_SCRATCH_BYTES (36ull << 20)
+static __device__ __align__(256) unsigned char g_static_scratch[CH_STATIC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mutex;
+unsigned char* g_static_ptr[kMaxDevices] = {};
+
+// Device address of the static scratch on the current device (host code
+// cannot use the array's name as a device pointer).  Looked up once per
+// device, on that device's first ch_dose_static call.
+ch_status static_scratch(int device, unsigned char** out) {
+  if (device < 0 || device >= kMaxDevices) return fail(CH_ERR_INVALID_ARG, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  if (!g_static_ptr[device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(CH_ERR_DEVICE, std::string("cudaGetSymbolAddress(static scratch): ") + cudaGetErrorString(e));
+    g_static_ptr[device] = static_cast<unsigned char*>(p);
+  }
+  *out = g_static_ptr[device];
+  return CH_OK;
+}
+
+inline size_t align_up(size_t a, size_t b) { return (a + b - 1) / b * b; }
+
+}  // namespace
+
 extern "C" {
 
 ch_status ch_plan_create(ch_plan** plan, int device) {
@@ -708,6 +744,129 @@ ch_status ch_dose_batch(ch_plan* P, int n, const ch_grid* grids, const float* co
 ch_status ch_dose_scatter(ch_plan* P, const ch_grid* grid, const float* rho, int swap_xy, const ch_beam* beam,
                           const ch_settings* settings, float* dose, void* stream) {
   return run(P, 1, grid, &rho, &swap_xy, beam, settings, &dose, nullptr, true, (cudaStream_t)stream);
+}
+
+ch_status ch_dose_static(ch_plan* P, const ch_grid* grid, const float* rho, int swap_xy, const ch_beam* beam,
+                         const ch_settings* settings, float* dose, void* stream) {
+  if (!P) return fail(CH_ERR_INVALID_ARG, "plan is NULL");
+  if (!P->have_kernel) return fail(CH_ERR_NO_KERNEL, "ch_plan_set_kernel has not been called");
+  ch_status st;
+  if ((st = check_grid(grid)) != CH_OK) return st;
+  if ((st = check_beam(beam)) != CH_OK) return st;
+  if ((st = check_settings(settings)) != CH_OK) return st;
+  if (!rho || !dose) return fail(CH_ERR_INVALID_ARG, "density or dose pointer is NULL");
+  if (swap_xy && grid->n[0] != grid->n[1]) return fail(CH_ERR_INVALID_ARG, "swap_xy needs a square x/y grid");
+  // everything that allocates must already exist on the plan
+  const StencilSet& S = P->st;
+  bool ready = S.valid && P->counters.p;
+  for (int k = 0; k < 3 && ready; ++k) ready = S.spacing[k] == grid->spacing[k] && S.cap[k] >= grid->n[k];
+  if (!ready)
+    return fail(CH_ERR_INVALID_ARG,
+                "plan not prepared for this grid: run one ch_dose with the same voxel spacing and a grid at "
+                "least this large on the plan first");
+  cudaStream_t s = (cudaStream_t)stream;
+  CH_CUDA(cudaSetDevice(P->device));
+
+  // layout of the static scratch for this grid
+  GridDev g{};
+  for (int k = 0; k < 3; ++k) {
+    g.n[k] = grid->n[k];
+    g.origin[k] = grid->origin[k];
+    g.spacing[k] = grid->spacing[k];
+  }
+  g.zp = round_up(grid->n[2], 4);
+  g.swap_xy = swap_xy;
+  const size_t N = (size_t)g.n[0] * g.n[1] * g.n[2];
+  const int ntile[3] = {(g.n[0] + TX - 1) / TX, (g.n[1] + TY - 1) / TY, (g.n[2] + TZ - 1) / TZ};
+  const int n_tiles = ntile[0] * ntile[1] * ntile[2];
+  const int U = S.n_dirs;
+  const int n_units = n_tiles * ((U + DIR_GROUP - 1) / DIR_GROUP);
+  size_t off = 0;
+  const size_t o_T = off;
+  off = align_up(off + (size_t)g.n[0] * g.n[1] * g.zp * sizeof(float), 256);
+  const size_t o_lv = off;
+  off = align_up(off + N * sizeof(int), 256);
+  const size_t o_lb = off;
+  off = align_up(off + N * sizeof(double), 256);
+  const size_t o_aabb = off;
+  off = align_up(off + 8 * sizeof(int), 256);
+  const size_t o_r = off;
+  off = align_up(off + (size_t)n_tiles * U * sizeof(uint32_t), 256);
+  const size_t o_cr = off;
+  off = align_up(off + (size_t)n_tiles * U * sizeof(uint32_t), 256);
+  const size_t o_cb = off;
+  off = align_up(off + sizeof(ConeBeam), 256);
+  const size_t o_rb = off;
+  off = align_up(off + sizeof(RangeBeam), 256);
+  if (off > CH_STATIC_SCRATCH_BYTES)
+    return fail(CH_ERR_INVALID_ARG, "grid needs " + std::to_string(off) + " bytes of scratch; the static scratch of "
+                                    "ch_dose_static holds " + std::to_string(CH_STATIC_SCRATCH_BYTES) +
+                                    " (about a 128^3 grid)");
+  unsigned char* base = nullptr;
+  if ((st = static_scratch(P->device, &base)) != CH_OK) return st;
+  float* T = reinterpret_cast<float*>(base + o_T);
+  int* aabb = reinterpret_cast<int*>(base + o_aabb);
+  int* counters = P->counters.as<int>();
+  int* flags = counters + 1;
+  unsigned long long* updates = reinterpret_cast<unsigned long long*>(counters + 2);
+
+  const BeamDev b = make_beam(*beam, *grid);
+  const SettingsDev sd = make_settings(*settings);
+  // aabb and the list count must start from their reset values; TERMA is
+  // rewritten in full by the prologue and the range tables by range_kernel
+  launch_init_scratch(aabb, 1, counters, s);
+  launch_prologue(rho, g, b, sd, T, Inter{}, 0, aabb, reinterpret_cast<int*>(base + o_lv),
+                  reinterpret_cast<double*>(base + o_lb), P->n_sm, flags, s);
+  CH_CUDA(cudaGetLastError());
+  CH_CUDA(cudaMemsetAsync(dose, 0, N * sizeof(float), s));
+
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled is not available from the driver");
+  ConeBeam C;
+  std::memset(&C, 0, sizeof(C));
+  cuuint64_t gdim[3] = {(cuuint64_t)g.n[2], (cuuint64_t)g.n[1], (cuuint64_t)g.n[0]};
+  cuuint64_t gstride[2] = {(cuuint64_t)g.zp * 4, (cuuint64_t)g.zp * g.n[1] * 4};
+  cuuint32_t estr[3] = {1, 1, 1};
+  for (int v = 0; v < N_VARIANTS; ++v) {
+    for (int ex = TX; ex <= var_max_ex(v); ++ex) {
+      cuuint32_t box[3] = {(cuuint32_t)var_p(v), (cuuint32_t)var_rows(v), (cuuint32_t)ex};
+      CUresult r = enc(&C.tmap[tmap_index(v, ex)], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)T, gdim, gstride, box,
+                       estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS) return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    }
+  }
+  C.dose = dose;
+  C.ranges = reinterpret_cast<uint32_t*>(base + o_r);
+  C.cranges = reinterpret_cast<uint32_t*>(base + o_cr);
+  for (int k = 0; k < 3; ++k) {
+    C.n[k] = g.n[k];
+    C.ntile[k] = ntile[k];
+  }
+  C.n_tiles = n_tiles;
+  C.unit_begin = 0;
+  C.n_units = n_units;
+  RangeBeam R;
+  std::memset(&R, 0, sizeof(R));
+  for (int k = 0; k < 3; ++k) {
+    R.n[k] = g.n[k];
+    R.ntile[k] = ntile[k];
+    R.origin[k] = g.origin[k];
+    R.spacing[k] = g.spacing[k];
+  }
+  R.n_tiles = n_tiles;
+  make_planes(*beam, *grid, b, R);
+  R.aabb = aabb;
+  R.ranges = reinterpret_cast<uint32_t*>(base + o_r);
+  R.cranges = reinterpret_cast<uint32_t*>(base + o_cr);
+  CH_CUDA(cudaMemcpyAsync(base + o_cb, &C, sizeof(C), cudaMemcpyHostToDevice, s));
+  CH_CUDA(cudaMemcpyAsync(base + o_rb, &R, sizeof(R), cudaMemcpyHostToDevice, s));
+  const ConeDirs D = cone_dirs(P);
+  launch_range(reinterpret_cast<const RangeBeam*>(base + o_rb), 1, n_tiles, D, s);
+  CH_CUDA(cudaGetLastError());
+  launch_gather(reinterpret_cast<const ConeBeam*>(base + o_cb), 1, D, n_units, P->n_sm, counters, updates, flags, s);
+  CH_CUDA(cudaGetLastError());
+  return CH_OK;
 }
 
 ch_status ch_dda_trace(const ch_grid* grid, int n_rays, const int* starts, const float* dirs, int cap, int* vox,

@@ -151,6 +151,21 @@ ch_status ch_dose_scatter(ch_plan* plan, const ch_grid* grid, const float* rho_d
                           int swap_xy, const ch_beam* beam, const ch_settings* settings,
                           float* dose_dev, void* stream);
 
+/* ch_dose without allocating: for callers that cannot call cudaMalloc
+ * (e.g. inside a host framework that owns the device allocator, or in code
+ * that must not allocate once set up).  No counterpart in the reference.
+ * Same arguments and result as ch_dose, but the per-beam scratch lives in a
+ * fixed 36 MiB device array inside this library (about a 128^3 grid; larger
+ * grids return CH_ERR_INVALID_ARG with the size needed).  The plan must
+ * already hold kernel tables and stencils for this voxel spacing and a grid
+ * at least this large: run one ch_dose on it first.  The first call on a
+ * device looks up the array's device address, so make that call before any
+ * stream capture.  Every call shares the one array: calls whose work
+ * overlaps on the GPU race, so serialise them (one stream, or events). */
+ch_status ch_dose_static(ch_plan* plan, const ch_grid* grid, const float* rho_dev, int swap_xy,
+                         const ch_beam* beam, const ch_settings* settings, float* dose_dev,
+                         void* stream);
+
 /* Test hook: n_rays DDA traces on the device.  starts int32 [n][3],
  * dirs float32 [n][3] (used as given, no normalisation), grid dims/spacing
  * from `grid`.  Writes voxels int32 [n][cap][3], t float32 [n][cap] and
