@@ -294,7 +294,8 @@ def run_ours(args):
             for i in range(B):
                 d_blocks[i].copy_(h_blocks[i], non_blocking=True)
                 db = dblocks[i]
-                jobs.append(eng.job(ph, d_rho, beams[i][0], DeviceBlock(d_blocks[i], db.r0, db.c0, db.full_shape),
+                jobs.append(eng.job(ph, d_rho, beams[i][0],
+                                    DeviceBlock(d_blocks[i], db.r0, db.c0, db.full_shape, db.uniform),
                                     SETTINGS, dose=doses[i]))
             eng.run_batch(jobs)
             for i in range(B):

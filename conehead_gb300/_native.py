@@ -31,7 +31,7 @@ class Beam(ctypes.Structure):
                 ("block", ctypes.c_void_p), ("block_rows", ctypes.c_int),
                 ("block_cols", ctypes.c_int), ("block_r0", ctypes.c_int),
                 ("block_c0", ctypes.c_int), ("full_rows", ctypes.c_int),
-                ("full_cols", ctypes.c_int)]
+                ("full_cols", ctypes.c_int), ("block_uniform", ctypes.c_int)]
 
 
 SETTING_KEYS = ("sPri", "sAnn", "zAnn", "rInner", "rOuter", "zExp", "sExp", "kExp",
@@ -163,7 +163,7 @@ def block_crop(block_values):
     return np.ascontiguousarray(bv[r0:r1, c0:c1]), int(r0), int(c0)
 
 
-def beam_struct(source, block_dev_ptr, crop_shape, r0, c0, full_shape):
+def beam_struct(source, block_dev_ptr, crop_shape, r0, c0, full_shape, uniform=False):
     b = Beam()
     pos = np.asarray(source.position)
     vy = np.asarray(source.v_y)
@@ -181,4 +181,5 @@ def beam_struct(source, block_dev_ptr, crop_shape, r0, c0, full_shape):
     b.block_rows, b.block_cols = int(crop_shape[0]), int(crop_shape[1])
     b.block_r0, b.block_c0 = int(r0), int(c0)
     b.full_rows, b.full_cols = int(full_shape[0]), int(full_shape[1])
+    b.block_uniform = int(bool(uniform))
     return b

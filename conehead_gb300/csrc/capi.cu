@@ -98,14 +98,14 @@ struct ch_plan {
   DevBuf K, theta, phi;
   StencilSet st;
   // scratch
-  DevBuf T, aabb, counters, ranges, cranges, cone_beams, range_beams, list_v, list_b;
+  DevBuf T, aabb, counters, ranges, cranges, cone_beams, range_beams, list_v;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaStream_t last_stream = nullptr;
   ch_stats stats{};
   bool stats_pending = false;
   bool timed = false;
   ~ch_plan() {
-    for (DevBuf* b : {&K, &theta, &phi, &T, &aabb, &counters, &ranges, &cranges, &cone_beams, &range_beams, &list_v, &list_b,
+    for (DevBuf* b : {&K, &theta, &phi, &T, &aabb, &counters, &ranges, &cranges, &cone_beams, &range_beams, &list_v,
                       &st.tap_base,
                       &st.tap_len, &st.taps, &st.offs, &st.tvals, &st.chunk_base, &st.n_chunks, &st.chunk_start, &st.chunk_rec,
                       &st.dirs, &st.raw_dirs})
@@ -367,6 +367,7 @@ BeamDev make_beam(const ch_beam& in, const ch_grid& g) {
   b.bc0 = in.block_c0;
   b.full_rows = in.full_rows;
   b.full_cols = in.full_cols;
+  b.uniform = in.block_uniform;
   b.sad = in.sad;
   b.sad_f32 = in.sad_f32;
   return b;
@@ -528,7 +529,6 @@ ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, 
   for (int i = 0; i < n; ++i)
     max_vox = std::max(max_vox, (size_t)jobs[i].g.n[0] * jobs[i].g.n[1] * jobs[i].g.n[2]);
   CH_CUDA(P->list_v.ensure(max_vox * sizeof(int)));
-  CH_CUDA(P->list_b.ensure(max_vox * sizeof(double)));
   int* counters = P->counters.as<int>();
   int* flags = counters + 1;
   unsigned long long* updates = reinterpret_cast<unsigned long long*>(counters + 2);
@@ -553,7 +553,7 @@ ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, 
     }
     // the voxel list is reused beam after beam (stream order)
     launch_prologue(J.rho, J.g, J.b, J.s, P->T.as<float>() + J.t_off, in, all, P->aabb.as<int>() + 8 * i,
-                    P->list_v.as<int>(), P->list_b.as<double>(), P->n_sm, flags, s);
+                    P->list_v.as<int>(), P->n_sm, flags, s);
     CH_CUDA(cudaGetLastError());
   }
   CH_CUDA(cudaEventRecord(P->ev[1], s));
@@ -644,7 +644,8 @@ ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, 
 // ------------------------------------------------------ static scratch --
 // Scratch of ch_dose_static: a fixed device array, so that call allocates
 // nothing.  It holds one beam's TERMA volume, the prologue voxel list, the
-// tile range tables and the launch records; 36 MiB covers a 128^3 grid.
+// tile range tables and the launch records; 36 MiB covers grids up to
+// about 160^3.
 // The array belongs to this library's module and stays allocated on every
 // GPU that uses it until the process exits.
 #define CH_STATIC_SCRATCH_BYTES (36ull << 20)
@@ -786,8 +787,6 @@ ch_status ch_dose_static(ch_plan* P, const ch_grid* grid, const float* rho, int 
   off = align_up(off + (size_t)g.n[0] * g.n[1] * g.zp * sizeof(float), 256);
   const size_t o_lv = off;
   off = align_up(off + N * sizeof(int), 256);
-  const size_t o_lb = off;
-  off = align_up(off + N * sizeof(double), 256);
   const size_t o_aabb = off;
   off = align_up(off + 8 * sizeof(int), 256);
   const size_t o_r = off;
@@ -801,7 +800,7 @@ ch_status ch_dose_static(ch_plan* P, const ch_grid* grid, const float* rho, int 
   if (off > CH_STATIC_SCRATCH_BYTES)
     return fail(CH_ERR_INVALID_ARG, "grid needs " + std::to_string(off) + " bytes of scratch; the static scratch of "
                                     "ch_dose_static holds " + std::to_string(CH_STATIC_SCRATCH_BYTES) +
-                                    " (about a 128^3 grid)");
+                                    " (grids up to about 160^3)");
   unsigned char* base = nullptr;
   if ((st = static_scratch(P->device, &base)) != CH_OK) return st;
   float* T = reinterpret_cast<float*>(base + o_T);
@@ -815,8 +814,7 @@ ch_status ch_dose_static(ch_plan* P, const ch_grid* grid, const float* rho, int 
   // aabb and the list count must start from their reset values; TERMA is
   // rewritten in full by the prologue and the range tables by range_kernel
   launch_init_scratch(aabb, 1, counters, s);
-  launch_prologue(rho, g, b, sd, T, Inter{}, 0, aabb, reinterpret_cast<int*>(base + o_lv),
-                  reinterpret_cast<double*>(base + o_lb), P->n_sm, flags, s);
+  launch_prologue(rho, g, b, sd, T, Inter{}, 0, aabb, reinterpret_cast<int*>(base + o_lv), P->n_sm, flags, s);
   CH_CUDA(cudaGetLastError());
   CH_CUDA(cudaMemsetAsync(dose, 0, N * sizeof(float), s));
 

@@ -73,6 +73,7 @@ struct BeamDev {
   // block crop
   const float* block;
   int brows, bcols, br0, bc0, full_rows, full_cols;
+  int uniform;          // every crop value is 1.0
   // fluence / TERMA
   double sad;
   int sad_f32;
@@ -182,8 +183,8 @@ struct Inter {
 // ------------------------------------------------------------ launchers --
 void upload_unit_partials();
 void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const SettingsDev& s, float* T,
-                     const Inter& inter, int all_voxels, int* aabb, int* list_v, double* list_b, int n_sm,
-                     int* flags, cudaStream_t st);
+                     const Inter& inter, int all_voxels, int* aabb, int* list_v, int n_sm, int* flags,
+                     cudaStream_t st);
 void launch_stencil(const float* theta, int n_theta, const float* phi, int n_phi, const double* K, int n_r,
                     const float* spacing, const int* cap, int max_len, short4* off, float* t, float* dk,
                     int* len, float* dirs, cudaStream_t st);

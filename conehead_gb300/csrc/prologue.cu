@@ -33,25 +33,24 @@ __constant__ double c_unit_partial[28];
 // cell index i = floor(100 x) (x in cm, beam coordinates); the reference
 // reads block_values[i + 1999] after checking i + 2000 in [0, 3999]; index
 // -1 wraps to the last row/column.
-__device__ __forceinline__ float cell_value(const BeamDev& b, long long fi, long long fk) {
-  long long c0 = fi + 2000, c1 = fk + 2000;
+__device__ __forceinline__ float cell_value(const BeamDev& b, int fi, int fk) {
+  const int c0 = fi + 2000, c1 = fk + 2000;
   if (c0 < 0 || c0 > 3999 || c1 < 0 || c1 > 3999) return 0.0f;
-  long long r = c0 - 1, c = c1 - 1;
+  int r = c0 - 1, c = c1 - 1;
   if (r < 0) r += b.full_rows;
   if (c < 0) c += b.full_cols;
   r -= b.br0;
   c -= b.bc0;
   if (r < 0 || r >= b.brows || c < 0 || c >= b.bcols) return 0.0f;
-  return __ldg(b.block + r * b.bcols + c);
+  if (b.uniform) return 1.0f;
+  return __ldg(b.block + (size_t)r * b.bcols + c);
 }
 
-__device__ __forceinline__ long long floor_cell(float v) {
-  // floor(f32 product) as the reference stores it; NaN -> out of range
-  if (!(v == v)) return 1ll << 40;
-  float f = floorf(v);
-  if (f > 1e12f) return 1ll << 40;
-  if (f < -1e12f) return -(1ll << 40);
-  return (long long)f;
+// floor of a float32 cell coordinate as the reference stores it; values far
+// outside the map (and NaN) land outside [-2000, 1999], where every cell reads 0
+__device__ __forceinline__ int floor_cell(float v) {
+  if (!(v == v)) return 1 << 24;
+  return (int)floorf(fminf(fmaxf(v, -1.0e7f), 1.0e7f));
 }
 
 // Exact projection, float64 source arrays (conehead.py:25-47 + :109-116).
@@ -98,8 +97,10 @@ __device__ __forceinline__ bool project_exact(const BeamDev& b, const float* rd,
   return b.geom_f32 ? project_exact_f32(b, rd, px, pz) : project_exact_mixed(b, rd, px, pz);
 }
 
-// Exact transmission of one sub-sample (reference path end to end).
-__device__ float sample_exact(const BeamDev& b, const GridDev& g, const float* pos, const float* off,
+// Exact transmission of one sub-sample (reference path end to end).  Kept
+// out of line: it is rare, and inlining it at every sample site would bloat
+// the kernel past the instruction cache.
+__device__ __noinline__ float sample_exact(const BeamDev& b, const GridDev& g, const float* pos, const float* off,
                               int ix, int iy, int iz, int& bad) {
   const int ii[3] = {ix, iy, iz};
   float ps[3];
@@ -121,12 +122,13 @@ __device__ float sample_exact(const BeamDev& b, const GridDev& g, const float* p
 }
 
 // ------------------------------------------------------------ blocking --
-// Transmission of sub-sample (ix, iy, iz): float32 projection, exact
-// float64 mirror only when the block cell is ambiguous within SAMPLE_DELTA.
+// Transmission of sub-sample (ix, iy, iz) at pos + (rx, ry, rz): float32
+// projection, exact float64 mirror only when the block cell is ambiguous
+// within SAMPLE_DELTA.
 __device__ __forceinline__ float sample_value(const BeamDev& b, const GridDev& g, const float* pos,
-                                              const float* off, const float (*rel)[8], int ix, int iy,
+                                              const float* off, float rx, float ry, float rz, int ix, int iy,
                                               int iz, int& bad) {
-  const float p0 = pos[0] + rel[0][ix], p1 = pos[1] + rel[1][iy], p2 = pos[2] + rel[2][iz];
+  const float p0 = pos[0] + rx, p1 = pos[1] + ry, p2 = pos[2] + rz;
   const float np_ = b.vyf[0] * p0 + b.vyf[1] * p1 + b.vyf[2] * p2;
   const float m0p = b.m0f[0] * p0 + b.m0f[1] * p1 + b.m0f[2] * p2;
   const float m2p = b.m2f[0] * p0 + b.m2f[1] * p1 + b.m2f[2] * p2;
@@ -135,11 +137,11 @@ __device__ __forceinline__ float sample_value(const BeamDev& b, const GridDev& g
   // to the source plane (or behind it) take the exact path, which also
   // reports rays parallel to the blocking plane as the reference does
   if (!(fabsf(ndr) > 0.2f * fabsf(b.a_K))) return sample_exact(b, g, pos, off, ix, iy, iz, bad);
-  const float si = b.a_K / ndr;
+  const float si = __fdividef(b.a_K, ndr);
   const float ux = (b.a_c0 + si * (b.a_m0S - m0p)) * 100.0f;
   const float uz = (b.a_c2 + si * (b.a_m2S - m2p)) * 100.0f;
-  const long long i0 = floor_cell(ux - SAMPLE_DELTA), i1 = floor_cell(ux + SAMPLE_DELTA);
-  const long long k0 = floor_cell(uz - SAMPLE_DELTA), k1 = floor_cell(uz + SAMPLE_DELTA);
+  const int i0 = floor_cell(ux - SAMPLE_DELTA), i1 = floor_cell(ux + SAMPLE_DELTA);
+  const int k0 = floor_cell(uz - SAMPLE_DELTA), k1 = floor_cell(uz + SAMPLE_DELTA);
   float v = cell_value(b, i0, k0);
   if (i0 != i1 || k0 != k1) {
     const float v1 = cell_value(b, i1, k0), v2 = cell_value(b, i0, k1), v3 = cell_value(b, i1, k1);
@@ -148,36 +150,15 @@ __device__ __forceinline__ float sample_value(const BeamDev& b, const GridDev& g
   return v;
 }
 
-// blocked fraction of one voxel (float64, reference accumulation order:
-// acc = acc + v / S^3 over ix, iy, iz)
-__device__ double blocked_fraction(const BeamDev& b, const GridDev& g, int S, const float* pos,
-                                   int& bad) {
-  float off[3], rel[3][8];
-#pragma unroll
+// General blocked fraction: any sample count, float32 source arrays, or
+// transmission values other than 0 and 1 (float64, reference order
+// acc = acc + v / S^3 over ix, iy, iz).
+__device__ __noinline__ double blocked_general(const BeamDev& b, const GridDev& g, int S, const float* pos,
+                                               int& bad) {
+  float off[3];
   // f32(f64(s) / S) == fdiv(s, S): double rounding is innocuous for float32 operands
   for (int k = 0; k < 3; ++k) off[k] = fdiv(g.spacing[k], (float)S);
-  const bool exact_all = b.geom_f32 != 0 || S > 8;
-  if (!exact_all) {
-    for (int k = 0; k < 3; ++k)
-      for (int i = 0; i < S; ++i) rel[k][i] = off[k] * ((float)i + 0.5f) - g.spacing[k] * 0.5f;
-  }
-  if (!exact_all && S == 3) {
-    // jaw maps hold only 0 and 1: then the float64 sum is a table lookup
-    int n_one = 0;
-    bool other = false;
-    for (int ix = 0; ix < 3 && !other; ++ix)
-      for (int iy = 0; iy < 3 && !other; ++iy)
-        for (int iz = 0; iz < 3; ++iz) {
-          const float v = sample_value(b, g, pos, off, rel, ix, iy, iz, bad);
-          if (v == 1.0f) {
-            ++n_one;
-          } else if (v != 0.0f) {
-            other = true;
-            break;
-          }
-        }
-    if (!other) return c_unit_partial[n_one];
-  }
+  const bool exact_all = b.geom_f32 != 0;
   double acc = 0.0;
   const double denom = (double)S * (double)S * (double)S;
   float last_v = -1.0f;
@@ -185,8 +166,15 @@ __device__ double blocked_fraction(const BeamDev& b, const GridDev& g, int S, co
   for (int ix = 0; ix < S; ++ix)
     for (int iy = 0; iy < S; ++iy)
       for (int iz = 0; iz < S; ++iz) {
-        const float v = exact_all ? sample_exact(b, g, pos, off, ix, iy, iz, bad)
-                                  : sample_value(b, g, pos, off, rel, ix, iy, iz, bad);
+        float v;
+        if (exact_all) {
+          v = sample_exact(b, g, pos, off, ix, iy, iz, bad);
+        } else {
+          const float rx = off[0] * ((float)ix + 0.5f) - g.spacing[0] * 0.5f;
+          const float ry = off[1] * ((float)iy + 0.5f) - g.spacing[1] * 0.5f;
+          const float rz = off[2] * ((float)iz + 0.5f) - g.spacing[2] * 0.5f;
+          v = sample_value(b, g, pos, off, rx, ry, rz, ix, iy, iz, bad);
+        }
         if (v != last_v) {
           last_v = v;
           last_q = ddiv((double)v, denom);
@@ -194,6 +182,33 @@ __device__ double blocked_fraction(const BeamDev& b, const GridDev& g, int S, co
         acc = dadd(acc, last_q);
       }
   return acc;
+}
+
+// blocked fraction of one voxel; the 3x3x3 jaw case (values 0 and 1 only)
+// is unrolled and sums through the precomputed float64 partial sums
+__device__ double blocked_fraction(const BeamDev& b, const GridDev& g, int S, const float* pos, int& bad) {
+  if (S != 3 || b.geom_f32) return blocked_general(b, g, S, pos, bad);
+  float off[3], rel[3][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    off[k] = fdiv(g.spacing[k], 3.0f);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) rel[k][i] = off[k] * ((float)i + 0.5f) - g.spacing[k] * 0.5f;
+  }
+  int n_one = 0;
+  bool other = false;
+#pragma unroll
+  for (int ix = 0; ix < 3; ++ix)
+#pragma unroll
+    for (int iy = 0; iy < 3; ++iy)
+#pragma unroll
+      for (int iz = 0; iz < 3; ++iz) {
+        const float v = sample_value(b, g, pos, off, rel[0][ix], rel[1][iy], rel[2][iz], ix, iy, iz, bad);
+        n_one += v == 1.0f ? 1 : 0;
+        other |= v != 0.0f && v != 1.0f;
+      }
+  if (!other) return c_unit_partial[n_one];
+  return blocked_general(b, g, 3, pos, bad);
 }
 
 // ------------------------------------------------------------------ DDA --
@@ -256,24 +271,22 @@ __device__ float radiological_depth(const float* __restrict__ rho, const GridDev
 }
 
 // ------------------------------------------------------------ kernels --
-// Pass 1, every voxel: cull, blocked fraction; voxels the beam reaches (or
-// every voxel when intermediates are requested) go to a compact list so the
-// depth/TERMA pass runs on full warps.
-__global__ void __launch_bounds__(256) blocked_kernel(GridDev g, BeamDev b, SettingsDev s,
-                                                      float* __restrict__ T, Inter inter, int all_voxels,
-                                                      int* __restrict__ list_count, int* __restrict__ list_v,
-                                                      double* __restrict__ list_b, int* __restrict__ flags) {
-  const long long N = (long long)g.n[0] * g.n[1] * g.n[2];
-  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+// Pass 1, every voxel: zero TERMA and keep the voxels the beam may reach
+// (all voxels when intermediates are requested) on a compact list, so the
+// blocking/depth/TERMA pass runs on full warps.
+__global__ void __launch_bounds__(256) cull_kernel(GridDev g, BeamDev b, float* __restrict__ T, Inter inter,
+                                                   int all_voxels, int* __restrict__ list_count,
+                                                   int* __restrict__ list_v) {
+  // volumes hold fewer than 2^31 voxels (checked on the host)
+  const int N = g.n[0] * g.n[1] * g.n[2];
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = v < N;
-  int bad = 0;
-  double blocked = 0.0;
   bool keep = false;
   if (live) {
-    const int z = (int)(v % g.n[2]);
-    const long long r = v / g.n[2];
-    const int y = (int)(r % g.n[1]);
-    const int x = (int)(r / g.n[1]);
+    const int z = v % g.n[2];
+    const int r = v / g.n[2];
+    const int y = r % g.n[1];
+    const int x = r / g.n[1];
     float pos[3];
     pos[0] = voxel_centre(g.origin[0], g.spacing[0], x);
     pos[1] = voxel_centre(g.origin[1], g.spacing[1], y);
@@ -296,11 +309,10 @@ __global__ void __launch_bounds__(256) blocked_kernel(GridDev g, BeamDev b, Sett
           candidate = false;
       }
     }
-    if (candidate) blocked = blocked_fraction(b, g, s.samples, pos, bad);
-    keep = blocked != 0.0 || all_voxels;
-    T[((long long)x * g.n[1] + y) * g.zp + z] = 0.0f;
-    if (inter.blocked) inter.blocked[v] = blocked;
+    keep = candidate || all_voxels;
+    T[((size_t)x * g.n[1] + y) * g.zp + z] = 0.0f;
     if (!keep) {
+      if (inter.blocked) inter.blocked[v] = 0.0;
       if (inter.d_eff) inter.d_eff[v] = 0.0f;
       if (inter.oad) inter.oad[v] = 0.0f;
       if (inter.fluence) inter.fluence[v] = 0.0f;
@@ -315,22 +327,18 @@ __global__ void __launch_bounds__(256) blocked_kernel(GridDev g, BeamDev b, Sett
     int base = 0;
     if (lane == 0) base = atomicAdd(list_count, __popc(m));
     base = __shfl_sync(0xffffffffu, base, 0);
-    if (keep) {
-      const int slot = base + __popc(m & ((1u << lane) - 1u));
-      list_v[slot] = (int)v;
-      list_b[slot] = blocked;
-    }
+    if (keep) list_v[base + __popc(m & ((1u << lane) - 1u))] = v;
   }
-  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flags, FLAG_PARALLEL_RAY);
 }
 
-// Pass 2, listed voxels: radiological depth, oad, fluence, softening/horn,
-// TERMA; TERMA support box for the cone stage.
+// Pass 2, listed voxels: blocked fraction, then (where the beam is not
+// fully blocked, or for every voxel when intermediates are requested)
+// radiological depth, oad, fluence, softening/horn and TERMA; TERMA support
+// box for the cone stage.
 __global__ void __launch_bounds__(256) terma_kernel(const float* __restrict__ rho, GridDev g, BeamDev b,
                                                     SettingsDev s, float* __restrict__ T, Inter inter,
-                                                    const int* __restrict__ list_count,
-                                                    const int* __restrict__ list_v,
-                                                    const double* __restrict__ list_b, int* __restrict__ aabb,
+                                                    int all_voxels, const int* __restrict__ list_count,
+                                                    const int* __restrict__ list_v, int* __restrict__ aabb,
                                                     int* __restrict__ flags) {
   const int count = *list_count;
   const int rounds = (count + blockDim.x * gridDim.x - 1) / (blockDim.x * gridDim.x);
@@ -340,16 +348,22 @@ __global__ void __launch_bounds__(256) terma_kernel(const float* __restrict__ rh
     int x = 0, y = 0, z = 0, bad = 0;
     float Tv = 0.0f;
     if (live) {
-      const long long v = list_v[e];
-      const double blocked = list_b[e];
-      z = (int)(v % g.n[2]);
-      const long long r = v / g.n[2];
-      y = (int)(r % g.n[1]);
-      x = (int)(r / g.n[1]);
+      const int v = list_v[e];
+      z = v % g.n[2];
+      const int r = v / g.n[2];
+      y = r % g.n[1];
+      x = r / g.n[1];
       float pos[3];
       pos[0] = voxel_centre(g.origin[0], g.spacing[0], x);
       pos[1] = voxel_centre(g.origin[1], g.spacing[1], y);
       pos[2] = voxel_centre(g.origin[2], g.spacing[2], z);
+      const double blocked = blocked_fraction(b, g, s.samples, pos, bad);
+      if (inter.blocked) inter.blocked[v] = blocked;
+      if (blocked == 0.0 && !all_voxels) {
+        if (inter.terma) inter.terma[v] = 0.0f;
+        goto next;
+      }
+      {
       float rd[3];
       ray_to_source(b, pos, rd);
       // ---- radiological depth (float32, exact mirror)
@@ -385,14 +399,16 @@ __global__ void __launch_bounds__(256) terma_kernel(const float* __restrict__ rh
         terma = fadd(terma, fmul(fmul(fmul(fmul(fmul(s.w[i], fluence), ex), s.E[i]), s.mu[i]), fh));
       }
       Tv = d2f(dmul((double)terma, blocked));
-      T[((long long)x * g.n[1] + y) * g.zp + z] = Tv;
+      T[((size_t)x * g.n[1] + y) * g.zp + z] = Tv;
       if (inter.d_eff) inter.d_eff[v] = deff;
       if (inter.oad) inter.oad[v] = oad;
       if (inter.fluence) inter.fluence[v] = fluence;
       if (inter.f_soften) inter.f_soften[v] = fs;
       if (inter.f_horn) inter.f_horn[v] = fh;
       if (inter.terma) inter.terma[v] = Tv;
+      }
     }
+  next:
     // ---- support box of T != 0 (the reference skips T == 0 sources)
     const bool nz_ = live && Tv != 0.0f;
     const unsigned m = __ballot_sync(0xffffffffu, nz_);
@@ -428,18 +444,17 @@ void upload_unit_partials() {
 }
 
 void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const SettingsDev& s, float* T,
-                     const Inter& inter, int all_voxels, int* aabb, int* list_v, double* list_b, int n_sm,
-                     int* flags, cudaStream_t st) {
+                     const Inter& inter, int all_voxels, int* aabb, int* list_v, int n_sm, int* flags,
+                     cudaStream_t st) {
   const long long N = (long long)g.n[0] * g.n[1] * g.n[2];
   const int threads = 256;
   const long long blocks = (N + threads - 1) / threads;
   int* list_count = aabb + 6;
-  blocked_kernel<<<(unsigned)blocks, threads, 0, st>>>(g, b, s, T, inter, all_voxels, list_count, list_v, list_b,
-                                                       flags);
+  cull_kernel<<<(unsigned)blocks, threads, 0, st>>>(g, b, T, inter, all_voxels, list_count, list_v);
   const long long want = (N + threads - 1) / threads;
   const int grid = (int)(want < (long long)n_sm * 8 ? want : (long long)n_sm * 8);
-  terma_kernel<<<grid > 0 ? grid : 1, threads, 0, st>>>(rho, g, b, s, T, inter, list_count, list_v, list_b, aabb,
-                                                        flags);
+  terma_kernel<<<grid > 0 ? grid : 1, threads, 0, st>>>(rho, g, b, s, T, inter, all_voxels, list_count, list_v,
+                                                        aabb, flags);
 }
 
 __global__ void init_scratch_kernel(int* aabb, int n_beams, int* counters) {

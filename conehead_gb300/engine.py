@@ -23,6 +23,7 @@ class DeviceBlock:
     r0: int
     c0: int
     full_shape: tuple
+    uniform: bool = False  # every crop value is 1.0 (a jaw rectangle)
 
 
 @dataclass
@@ -82,7 +83,7 @@ class DoseEngine:
     def upload_block(self, block_values):
         crop, r0, c0 = N.block_crop(block_values)
         t = self.torch.from_numpy(crop).to(self.device)
-        return DeviceBlock(t, r0, c0, tuple(np.shape(block_values)))
+        return DeviceBlock(t, r0, c0, tuple(np.shape(block_values)), bool(np.all(crop == 1.0)))
 
     def upload_densities(self, densities):
         return self.torch.from_numpy(np.ascontiguousarray(densities, dtype=np.float32)).to(self.device)
@@ -93,7 +94,7 @@ class DoseEngine:
             swap_xy = int(size[0] == size[1])
         grid = N.grid_struct(size, phantom.origin, phantom.spacing)
         beam = N.beam_struct(source, dblock.crop.data_ptr(), dblock.crop.shape, dblock.r0, dblock.c0,
-                             dblock.full_shape)
+                             dblock.full_shape, dblock.uniform)
         s = settings if isinstance(settings, N.Settings) else N.settings_struct(settings)
         if dose is None:
             dose = self.torch.empty(size, dtype=self.torch.float32, device=self.device)

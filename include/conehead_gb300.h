@@ -72,6 +72,8 @@ typedef struct {
   int block_rows, block_cols;
   int block_r0, block_c0;
   int full_rows, full_cols;
+  int block_uniform;    /* 1 when every value of the crop is 1.0 (a jaw
+                           rectangle): lookups then read no memory */
 } ch_beam;
 
 /* settings dict of Conehead.calculate (example.py:27-58) plus the spectrum
@@ -155,8 +157,8 @@ ch_status ch_dose_scatter(ch_plan* plan, const ch_grid* grid, const float* rho_d
  * (e.g. inside a host framework that owns the device allocator, or in code
  * that must not allocate once set up).  No counterpart in the reference.
  * Same arguments and result as ch_dose, but the per-beam scratch lives in a
- * fixed 36 MiB device array inside this library (about a 128^3 grid; larger
- * grids return CH_ERR_INVALID_ARG with the size needed).  The plan must
+ * fixed 36 MiB device array inside this library (grids up to about 160^3;
+ * larger grids return CH_ERR_INVALID_ARG with the size needed).  The plan must
  * already hold kernel tables and stencils for this voxel spacing and a grid
  * at least this large: run one ch_dose on it first.  The first call on a
  * device looks up the array's device address, so make that call before any

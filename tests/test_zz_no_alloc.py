@@ -83,11 +83,11 @@ def test_static_refuses_grids_beyond_its_scratch(setup):
     from conehead_gb300.phantoms import random_beam, slab_phantom
     eng, settings = setup
     rng = np.random.default_rng(3)
-    ph = slab_phantom(160, 0.25, seed=3, n_inserts=4)
+    ph = slab_phantom(192, 0.25, seed=3, n_inserts=4)
     rho = eng.upload_densities(ph.densities)
     src, blk = random_beam(rng, field=5.0)
     db = eng.upload_block(blk.block_values)
-    eng.run(eng.job(ph, rho, src, db, settings))      # prepares the plan for 160^3
+    eng.run(eng.job(ph, rho, src, db, settings))      # prepares the plan for 192^3
     eng.sync()
     job = eng.job(ph, rho, src, db, settings)
     with pytest.raises(N.CHError) as err:
