@@ -13,6 +13,8 @@ import numpy as np
 from .build import LIB
 
 CH_MAX_ENERGY = 32
+CH_MAX_LEAF_PAIRS = 256
+CH_MLC_TIP_CELLS = 15
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "CUDA error",
           4: "device wait timed out", 5: "ray parallel to the blocking plane",
@@ -55,6 +57,15 @@ class Intermediates(ctypes.Structure):
                 ("blocked", "d_eff", "oad", "fluence", "f_soften", "f_horn", "terma")]
 
 
+class MLC(ctypes.Structure):
+    _fields_ = [("n_pairs", ctypes.c_int), ("map_rows", ctypes.c_int), ("map_cols", ctypes.c_int),
+                ("open_r0", ctypes.c_int), ("open_r1", ctypes.c_int), ("open_c0", ctypes.c_int),
+                ("open_c1", ctypes.c_int), ("reserved", ctypes.c_int),
+                ("row0", ctypes.c_int * CH_MAX_LEAF_PAIRS), ("rows", ctypes.c_int * CH_MAX_LEAF_PAIRS),
+                ("a_end", ctypes.c_int * CH_MAX_LEAF_PAIRS), ("b_start", ctypes.c_int * CH_MAX_LEAF_PAIRS),
+                ("tip", ctypes.c_double * CH_MLC_TIP_CELLS)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("ms_prologue", ctypes.c_float), ("ms_range", ctypes.c_float),
                 ("ms_cone", ctypes.c_float), ("updates", ctypes.c_double),
@@ -75,6 +86,8 @@ SIGNATURES = {
                                      P(Settings), P(VP), VP]),
     "ch_dose_scatter": (ctypes.c_int, [VP, P(Grid), VP, ctypes.c_int, P(Beam), P(Settings), VP, VP]),
     "ch_dose_static": (ctypes.c_int, [VP, P(Grid), VP, ctypes.c_int, P(Beam), P(Settings), VP, VP]),
+    "ch_block_from_mlc": (ctypes.c_int, [P(MLC), VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         VP]),
     "ch_dda_trace": (ctypes.c_int, [P(Grid), ctypes.c_int, VP, VP, ctypes.c_int, VP, VP, VP, VP]),
     "ch_cone_directions": (ctypes.c_int, [VP, VP, VP]),
     "ch_plan_sync": (ctypes.c_int, [VP, VP]),

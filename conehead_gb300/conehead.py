@@ -46,7 +46,7 @@ class Conehead:
         eng.set_kernel(settings["energy_weights"], self.kernel_dir)
         self.dose_grid = DoseGrid(phantom.size, phantom.origin, phantom.spacing)
         rho = eng.upload_densities(phantom.densities)
-        dblock = eng.upload_block(block.block_values)
+        dblock = eng.block_for(block)
         job = eng.job(phantom, rho, source, dblock, settings)
         if return_intermediates:
             dose, inter = eng.run(job, intermediates=True)
@@ -69,7 +69,7 @@ class Conehead:
         eng = engine(self.device)
         eng.set_kernel(settings["energy_weights"], self.kernel_dir)
         rho = eng.upload_densities(phantom.densities)
-        jobs = [eng.job(phantom, rho, src, eng.upload_block(blk.block_values), settings)
+        jobs = [eng.job(phantom, rho, src, eng.block_for(blk), settings)
                 for src, blk in beams]
         doses = eng.run_batch(jobs)
         eng.sync()

@@ -867,6 +867,34 @@ ch_status ch_dose_static(ch_plan* P, const ch_grid* grid, const float* rho, int 
   return CH_OK;
 }
 
+ch_status ch_block_from_mlc(const ch_mlc* m, float* out, int rows, int cols, int r0, int c0, void* stream) {
+  if (!m || !out) return fail(CH_ERR_INVALID_ARG, "MLC table or output is NULL");
+  if (rows < 1 || cols < 1 || rows > 65535) return fail(CH_ERR_INVALID_ARG, "window must be 1..65535 rows and >= 1 column");
+  if (m->n_pairs < 1 || m->n_pairs > CH_MAX_LEAF_PAIRS)
+    return fail(CH_ERR_INVALID_ARG, "n_pairs out of range (1.." + std::to_string(CH_MAX_LEAF_PAIRS) + ")");
+  if (m->map_rows < 1 || m->map_cols < CH_MLC_TIP_CELLS + 1)
+    return fail(CH_ERR_INVALID_ARG, "map size out of range");
+  int prev_end = 0;
+  for (int n = 0; n < m->n_pairs; ++n) {
+    const std::string leaf = "leaf pair " + std::to_string(n) + ": ";
+    if (m->rows[n] < 3) return fail(CH_ERR_INVALID_ARG, leaf + "fewer than 3 rows");
+    if (m->row0[n] < prev_end) return fail(CH_ERR_INVALID_ARG, leaf + "rows overlap the previous pair or start below 0");
+    if ((long long)m->row0[n] + m->rows[n] > m->map_rows) return fail(CH_ERR_INVALID_ARG, leaf + "rows run past the map");
+    if (m->a_end[n] < CH_MLC_TIP_CELLS || m->a_end[n] > m->map_cols)
+      return fail(CH_ERR_INVALID_ARG, leaf + "bank A leaf shorter than its 15-cell tip or past the map");
+    if (m->b_start[n] < 0 || m->b_start[n] > m->map_cols - 1 - CH_MLC_TIP_CELLS)
+      return fail(CH_ERR_INVALID_ARG, leaf + "bank B leaf shorter than its 15-cell tip or past the map");
+    prev_end = m->row0[n] + m->rows[n];
+  }
+  if (m->open_r0 < 0 || m->open_r1 > m->map_rows || m->open_c0 < 0 || m->open_c1 > m->map_cols)
+    return fail(CH_ERR_INVALID_ARG, "jaw opening lies outside the map");
+  for (int k = 0; k < CH_MLC_TIP_CELLS; ++k)
+    if (!std::isfinite(m->tip[k])) return fail(CH_ERR_INVALID_ARG, "leaf tip ramp is not finite");
+  launch_mlc_raster(*m, out, rows, cols, r0, c0, (cudaStream_t)stream);
+  CH_CUDA(cudaGetLastError());
+  return CH_OK;
+}
+
 ch_status ch_dda_trace(const ch_grid* grid, int n_rays, const int* starts, const float* dirs, int cap, int* vox,
                        float* t, int* len, void* stream) {
   ch_status st = check_grid(grid);

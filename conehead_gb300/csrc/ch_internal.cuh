@@ -198,5 +198,6 @@ void launch_range(const RangeBeam* rbs_dev, int n_beams, int max_tiles, const Co
 void launch_gather(const ConeBeam* beams_dev, int n_beams, const ConeDirs& D, int total_units, int n_ctas,
                    int* unit_counter, unsigned long long* updates, int* flags, cudaStream_t st);
 void launch_init_scratch(int* aabb, int n_beams, int* counters, cudaStream_t st);
+void launch_mlc_raster(const ch_mlc& m, float* out, int rows, int cols, int r0, int c0, cudaStream_t st);
 
 }  // namespace ch

@@ -15,10 +15,12 @@
 // cone_gather_kernel is persistent and warp specialised:
 //   * warp 8 (producer) claims units from a global counter, walks each
 //     direction's tap range chunk by chunk (chunks are cut on the host so
-//     their sources fit one of three window shapes in a 108 KiB slot), and
-//     fills the window with TMA tile loads (cp.async.bulk.tensor.3d, P x 8 x
-//     1 boxes sized to the chunk, out-of-grid reads zero-filled) into a
-//     two-slot mbarrier pipeline;
+//     their sources fit one of three window shapes in a 108 KiB slot: P z x
+//     rows y x ex x floats with (P, rows) = (24, 32), (40, 24), (56, 24)),
+//     and fills the window with ONE TMA box per chunk
+//     (cp.async.bulk.tensor.3d through the tensor map of that shape and x
+//     extent, out-of-grid reads zero-filled) plus a bulk copy of the chunk's
+//     taps into a two-slot mbarrier pipeline;
 //   * warps 0-7 (consumers): lanes cover 16 z x 2 y rows of the 16^3 tile and
 //     a thread holds the 16 x outputs of its (y, z) column in registers;
 //     every tap costs 16 shared-memory loads + FMAs per thread, with the next

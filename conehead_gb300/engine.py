@@ -85,6 +85,28 @@ class DoseEngine:
         t = self.torch.from_numpy(crop).to(self.device)
         return DeviceBlock(t, r0, c0, tuple(np.shape(block_values)), bool(np.all(crop == 1.0)))
 
+    def upload_mlc(self, mlc):
+        """Rasterise the jaw opening of an MLC map on the device (no host map)."""
+        r0, r1, c0, c1 = mlc.window
+        full = (mlc.rows, 4000)
+        if r1 <= r0 or c1 <= c0:
+            return DeviceBlock(self.torch.zeros((1, 1), dtype=self.torch.float32, device=self.device), 0, 0, full)
+        crop = self.torch.empty((r1 - r0, c1 - c0), dtype=self.torch.float32, device=self.device)
+        m = mlc.struct()
+        N.check(self.L.ch_block_from_mlc(ctypes.byref(m), crop.data_ptr(), r1 - r0, c1 - c0, r0, c0,
+                                         self.stream()), "ch_block_from_mlc")
+        return DeviceBlock(crop, r0, c0, full)
+
+    def block_for(self, block):
+        """Device block of a Block-like object: plan blocks whose map was never
+        read on the host are rasterised from their leaf table, anything else
+        is cropped from ``block_values``."""
+        table = getattr(block, "device_mlc", None)
+        mlc = table() if callable(table) else None
+        if mlc is not None:
+            return self.upload_mlc(mlc)
+        return self.upload_block(block.block_values)
+
     def upload_densities(self, densities):
         return self.torch.from_numpy(np.ascontiguousarray(densities, dtype=np.float32)).to(self.device)
 

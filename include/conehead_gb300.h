@@ -168,6 +168,47 @@ ch_status ch_dose_static(ch_plan* plan, const ch_grid* grid, const float* rho_de
                          const ch_beam* beam, const ch_settings* settings, float* dose_dev,
                          void* stream);
 
+/* Jaw + MLCX block map of one static beam, in 0.1 mm map cells, as
+ * Block._set_from_plan builds it (conehead/block.py:87-215).  The full map
+ * is map_rows x map_cols (rows: leaf-boundary direction, map_rows =
+ * |last - first leaf boundary|; columns: leaf travel, 4000).  Leaf pair n
+ * covers rows [row0[n], row0[n] + rows[n]); its bank-A leaf covers columns
+ * [0, a_end[n]) and its bank-B leaf [b_start[n], map_cols - 1).  A leaf's
+ * transmission is 1 - profile(row) * ramp(column): the profile is 0.2, 0.5,
+ * 0.75 on the three rows at each side (tongue and groove, later rows of that
+ * list winning on narrow leaves) and 1 elsewhere; the ramp is tip[] over
+ * the 15 columns at the leaf end and 1 elsewhere.  Bank B is bank A turned
+ * by 180 degrees and is drawn over it.  Rows outside every pair read 1.
+ * Everything outside the jaw opening [open_r0, open_r1) x [open_c0,
+ * open_c1) reads 0.  The host fills this from the plan (conehead_gb300's
+ * block.MLCField does, with the reference's rounding). */
+#define CH_MAX_LEAF_PAIRS 256
+#define CH_MLC_TIP_CELLS 15
+typedef struct {
+  int n_pairs;
+  int map_rows, map_cols;
+  int open_r0, open_r1, open_c0, open_c1;
+  int reserved;
+  int row0[CH_MAX_LEAF_PAIRS];
+  int rows[CH_MAX_LEAF_PAIRS];
+  int a_end[CH_MAX_LEAF_PAIRS];
+  int b_start[CH_MAX_LEAF_PAIRS];
+  double tip[CH_MLC_TIP_CELLS];   /* numpy.linspace(1, 0, 15) */
+} ch_mlc;
+
+/* Rasterise the window [r0, r0 + rows) x [c0, c0 + cols) of an MLC block
+ * map into out_dev (float32, row major [rows][cols], device pointer) on the
+ * device: no host map, no 64 MB upload.  Cells outside the map read 0.  Pass
+ * the jaw opening as the window and the result is the cropped map that
+ * ch_beam.block takes (block_r0 = open_r0, block_c0 = open_c0, full_rows =
+ * map_rows, full_cols = map_cols).  Replaces building block_values on the
+ * host and copying it to the device (conehead/block.py:87-215 and
+ * conehead/conehead.py:555).  Leaf pairs must be ordered, disjoint and inside
+ * the map, at least 3 rows high, with leaf lengths of at least 15 columns;
+ * other tables give CH_ERR_INVALID_ARG. */
+ch_status ch_block_from_mlc(const ch_mlc* mlc, float* out_dev, int rows, int cols, int r0, int c0,
+                            void* stream);
+
 /* Test hook: n_rays DDA traces on the device.  starts int32 [n][3],
  * dirs float32 [n][3] (used as given, no normalisation), grid dims/spacing
  * from `grid`.  Writes voxels int32 [n][cap][3], t float32 [n][cap] and

@@ -205,6 +205,9 @@ float block_lookup(const or_beam& b, F px, F pz) {
   int64_t r = (int64_t)c0 - 1, c = (int64_t)c1 - 1;
   if (r < 0) r += b.block_rows;
   if (c < 0) c += b.block_cols;
+  // a map smaller than 4000 x 4000 is read past its end by the reference
+  // (undefined); both implementations read 0 there
+  if (r >= b.block_rows || c >= b.block_cols) return 0.0f;
   return b.block[r * b.block_cols + c];
 }
 

@@ -28,6 +28,13 @@ Three fixture families:
    ``dda_3d_c`` (oracle/build_ref.py) for a battery of directions/grids,
    including the notebook cases (dir (1,2,3)/sqrt(14) from (50,50,50) of
    101^3; dir (0.997859, 0, -0.065403) on 41^3).
+4. ``plans.npz`` -- ``Block(plan=...)`` (conehead/block.py:87-215) run on
+   the reference's RT Plan fixture (RP.3DCRT.dcm, read with this package's
+   pydicom-free reader) and on seeded synthetic plans (Millennium-,
+   Agility- and HD120-like leaf banks, colliding leaves, jaws beyond the map,
+   a two-beam plan): every input number, the SHA-256 of each full map and
+   the map inside its nonzero bounding box, or the error the reference
+   raises (maps other than 4000 rows).
 3. ``tables.npz`` -- the reference's host tables: ``KernelPoly.kernel_cum``
    for the example.py spectrum (every 7th column plus the last, and the
    full row sums), the 48 cone angles, ``mu_water`` at the
@@ -324,14 +331,114 @@ def make_tables(ref):
                         geometry=np.array(geo), squares=np.array(sq, dtype=np.float64))
 
 
+def _plan_ns(beams):
+    """An RT Plan as nested namespaces with the keywords Block reads."""
+    ns = types.SimpleNamespace
+    out = []
+    for bm in beams:
+        devs = [ns(RTBeamLimitingDeviceType=t, LeafPositionBoundaries=list(map(float, b)))
+                for t, b in bm["devices"]]
+        pos = [ns(RTBeamLimitingDeviceType=t, LeafJawPositions=list(map(float, v)))
+               for t, v in bm["positions"]]
+        out.append(ns(BeamType=bm.get("type", "STATIC"), BeamLimitingDeviceSequence=devs,
+                      ControlPointSequence=[ns(BeamLimitingDevicePositionSequence=pos)]))
+    return ns(BeamSequence=out)
+
+
+def synthetic_plans(seed=5):
+    """Seeded plan descriptions (dicts of plain numbers)."""
+    rng = np.random.default_rng(seed)
+    plans = {}
+    # Millennium-120-like bank: 10 mm outer, 5 mm inner leaves over +-200 mm
+    mil = np.r_[np.arange(-200, -100, 10), np.arange(-100, 100, 5), np.arange(100, 201, 10)].astype(float)
+    n = len(mil) - 1
+    a = rng.uniform(-90, 30, n).round(1)
+    b = (a + rng.uniform(0.5, 80, n)).round(1)
+    plans["millennium_random"] = [dict(devices=[("MLCX", mil)], positions=[
+        ("ASYMX", [-61.3, 47.8]), ("ASYMY", [-73.0, 55.5]), ("MLCX", np.r_[a, b])])]
+    # Agility-like: 80 pairs of 5 mm; some leaves colliding (A beyond B)
+    agi = np.arange(-200, 201, 5).astype(float)
+    n = len(agi) - 1
+    a = rng.uniform(-60, 40, n).round(2)
+    b = a + rng.uniform(-6, 50, n).round(2)
+    plans["agility_collide"] = [dict(devices=[("MLCX", agi)], positions=[
+        ("X", [-45.0, 45.0]), ("Y", [-52.25, 38.75]), ("MLCX", np.r_[a, b])])]
+    # HD120-like: map of 2200 rows (narrower than the 4000-cell lookup range)
+    hd = np.r_[np.arange(-110, -40, 5), np.arange(-40, 40, 2.5), np.arange(40, 111, 5)].astype(float)
+    n = len(hd) - 1
+    a = rng.uniform(-30, 10, n).round(1)
+    b = (a + rng.uniform(2, 40, n)).round(1)
+    plans["hd120_narrow"] = [dict(devices=[("MLCX", hd)], positions=[
+        ("ASYMX", [-25.0, 31.0]), ("ASYMY", [-48.0, 52.0]), ("MLCX", np.r_[a, b])])]
+    # irregular boundaries (0.01 mm values) over the 400 mm span, jaws past
+    # the map on the left and a crossed Y jaw: numpy's slice rules on
+    # negative indices decide which rows and columns stay open
+    w = rng.uniform(0.5, 1.0, 60)
+    irr = np.r_[-200.0, (-200.0 + np.cumsum(w / w.sum() * 400.0))[:-1].round(2), 200.0]
+    n = len(irr) - 1
+    a = rng.uniform(-50, 20, n).round(1)
+    b = (a + rng.uniform(1, 60, n)).round(1)
+    plans["irregular_wide_jaws"] = [dict(devices=[("MLCX", irr)], positions=[
+        ("ASYMX", [-250.0, 210.0]), ("ASYMY", [-150.0, -230.0]), ("MLCX", np.r_[a, b])])]
+    # two beams: the second control point has no X jaw, so the first beam's
+    # X jaw stays in force (the reference keeps the last value it read)
+    a1 = np.full(60, -20.0)
+    b1 = np.full(60, 20.0)
+    a2 = rng.uniform(-40, 0, 60).round(1)
+    b2 = (a2 + rng.uniform(5, 50, 60)).round(1)
+    plans["two_beams"] = [
+        dict(devices=[("ASYMX", [0.0]), ("MLCX", mil)], positions=[
+            ("ASYMX", [-30.0, 30.0]), ("ASYMY", [-30.0, 30.0]), ("MLCX", np.r_[a1, b1])]),
+        dict(devices=[("MLCX", mil)], positions=[
+            ("ASYMY", [-44.0, 36.0]), ("MLCX", np.r_[a2, b2])])]
+    return plans
+
+
+def make_plans(ref):
+    sys.path.insert(0, ref)
+    sys.path.insert(0, REPO)
+    _install_stubs()
+    import hashlib
+    from conehead.block import Block as RefBlock
+    from conehead_gb300 import dicom
+    out = {}
+    cases = {"fixture": dicom.read(os.path.join(ref, "RP.3DCRT.dcm"), force=True)}
+    descs = synthetic_plans()
+    for name, d in descs.items():
+        cases[name] = _plan_ns(d)
+        for i, bm in enumerate(d):
+            for j, (t, v) in enumerate(bm["devices"]):
+                out[f"{name}/beam{i}/dev{j}/{t}"] = np.asarray(v, dtype=np.float64)
+            for j, (t, v) in enumerate(bm["positions"]):
+                out[f"{name}/beam{i}/pos{j}/{t}"] = np.asarray(v, dtype=np.float64)
+    for name, plan in cases.items():
+        try:
+            bv = RefBlock(plan=plan).block_values
+        except ValueError as e:          # maps that are not 4000 rows (scipy interpolator check)
+            out[f"{name}/raises"] = np.array(str(e))
+            continue
+        assert bv.dtype == np.float32
+        nz = np.argwhere(bv != 0)
+        r0, c0 = nz.min(axis=0)
+        r1, c1 = nz.max(axis=0) + 1
+        out[f"{name}/shape"] = np.array(bv.shape)
+        out[f"{name}/sha256"] = np.frombuffer(hashlib.sha256(bv.tobytes()).digest(), dtype=np.uint8)
+        out[f"{name}/bbox"] = np.array([r0, r1, c0, c1])
+        out[f"{name}/crop"] = bv[r0:r1, c0:c1]
+    np.savez_compressed(os.path.join(HERE, "plans.npz"), **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", default=None, help="pipeline|dda|tables")
+    ap.add_argument("--only", default=None, help="pipeline|dda|tables|plans")
     a = ap.parse_args()
     if a.only in (None, "tables"):
         make_tables(a.ref)
         print("tables done")
+    if a.only in (None, "plans"):
+        make_plans(a.ref)
+        print("plans done")
     if a.only in (None, "dda"):
         make_dda(a.ref)
         print("dda done")

@@ -66,3 +66,48 @@ def test_block_crop_keeps_every_nonzero():
     full[r0:r0 + crop.shape[0], c0:c0 + crop.shape[1]] = crop
     assert np.array_equal(full, b.block_values)
     assert crop.shape == (800, 350)
+
+
+def test_mlc_table_validation_runs_on_the_host():
+    """ch_block_from_mlc refuses bad leaf tables before touching the GPU."""
+    import ctypes
+    from conehead_gb300 import _native as N
+    from conehead_gb300.block import MLCField
+    import numpy as np
+    L = N.lib()
+    good = MLCField(np.arange(-200, 201, 10.0), np.r_[np.full(40, -10.0), np.full(40, 10.0)], [-50, 50], [-50, 50])
+
+    def status(mutate):
+        m = good.struct()
+        mutate(m)
+        return L.ch_block_from_mlc(ctypes.byref(m), ctypes.c_void_p(0x1000), 4, 4, 0, 0, None)
+
+    def narrow(m):
+        m.rows[3] = 2
+
+    def overlap(m):
+        m.row0[5] -= 1
+
+    def short_a(m):
+        m.a_end[0] = 14
+
+    def short_b(m):
+        m.b_start[0] = 3985
+
+    def too_many(m):
+        m.n_pairs = N.CH_MAX_LEAF_PAIRS + 1
+
+    def jaw_outside(m):
+        m.open_r1 = m.map_rows + 1
+
+    def tip_nan(m):
+        m.tip[3] = float("nan")
+
+    for mutate, word in ((narrow, "3 rows"), (overlap, "overlap"), (short_a, "bank A"), (short_b, "bank B"),
+                         (too_many, "n_pairs"), (jaw_outside, "jaw"), (tip_nan, "tip")):
+        assert status(mutate) == 1
+        assert word in L.ch_last_error().decode(), mutate.__name__
+    m = good.struct()
+    assert L.ch_block_from_mlc(ctypes.byref(m), None, 4, 4, 0, 0, None) == 1
+    assert L.ch_block_from_mlc(ctypes.byref(m), ctypes.c_void_p(0x1000), 0, 4, 0, 0, None) == 1
+    assert ctypes.sizeof(N.MLC) == 8 * 4 + 4 * 4 * N.CH_MAX_LEAF_PAIRS + 8 * N.CH_MLC_TIP_CELLS
