@@ -18,6 +18,11 @@ fluence -> TERMA -> collapsed-cone dose (float32 dose and accumulation).
   cpu_baseline / --impl reference
               the CPU oracle (C++ FP64 restatement of the reference path,
               OpenMP over every host core) on whole beams of the workload
+  serving     the continuous-batching server (conehead_gb300.serving) under
+              open-loop Poisson arrivals: requests of 1-8 beams (5 x 5 cm,
+              gantry U[0, 360)) on resident slab phantoms of 64^3, 96^3,
+              128^3 and 192^3, HBM budget 80% of the device, doses copied to
+              pinned host memory; p50/p99 request latency and beams/s per rate
 
 Multi-GPU (torchrun): beams are independent, so each rank runs its own
 batches (weak scaling, no data-path collective); the step time is the
@@ -183,6 +188,42 @@ def run_reference(args):
     return 0
 
 
+def serving_extras(args, dev):
+    """Poisson-arrival serving runs, one per rate; results dropped as they land."""
+    import torch
+    from conehead_gb300.serving import DoseServer, GpuExecutor, drive, poisson_workload
+    sizes = (64, 96, 128, 192)
+    ex = GpuExecutor(dev.index, n_slots=2)
+    for n in sizes:
+        ex.add_phantom(f"p{n}", workload(n, args.spacing, seed=n))
+    ex.prepare(SETTINGS, (args.spacing,) * 3, (max(sizes),) * 3)
+    budget = int(0.8 * torch.cuda.mem_get_info(dev)[1])
+    names = [f"p{n}" for n in sizes]
+
+    def drop(req):
+        assert req.error is None, req.error
+        req.doses = None
+
+    # warm-up (pinned host buffers, lazy CUDA state), not reported
+    arr, specs = poisson_workload(np.random.default_rng(99), names, 400.0, 24)
+    drive(DoseServer(ex, budget, max_wave_beams=args.serve_batch), arr, specs, SETTINGS, on_done=drop)
+    rows = []
+    for rate in args.serve_rates:
+        rng = np.random.default_rng(int(rate))
+        arr, specs = poisson_workload(rng, names, float(rate), args.serve_requests)
+        server = DoseServer(ex, budget, max_wave_beams=args.serve_batch)
+        drive(server, arr, specs, SETTINGS, on_done=drop)
+        st = server.stats()
+        rows.append({"rate_req_s": rate, "requests": st["requests"], "beams": st["beams"],
+                     "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "beams_per_s": st["beams_per_s"],
+                     "mean_batch_beams": st["mean_batch_beams"], "peak_gb": st["peak_bytes"] / 1e9})
+    ex.close()
+    return {"workload": "Poisson arrivals, 1-8 beams per request (5x5 cm, gantry U[0,360)), phantoms "
+                        "64^3/96^3/128^3/192^3 @ 0.25 cm resident, 2 slots, latency = arrival to dose "
+                        "in pinned host memory",
+            "budget_gb": budget / 1e9, "max_batch_beams": args.serve_batch, "rates": rows}
+
+
 def config(args, beams_per_step=None):
     return {"workload": f"heterogeneous slab phantom {args.grid}^3 @ {args.spacing:g} cm, "
                         f"{args.field:g}x{args.field:g} cm2 field, gantry U[0,360), 6 MV, 12x48 cones",
@@ -334,6 +375,8 @@ def run_ours(args):
             pl.append(time.perf_counter() - t0)
         extras["plain_gpu_beams_per_s"] = len(pl) / sum(pl)
         extras["plain_gpu_path"] = "prologue + per-voxel scatter with float32 atomics, one beam per launch"
+        if args.serve_requests > 0:
+            extras["serving"] = serving_extras(args, dev)
         if not args.no_cpu:
             cv, cores, dt = cpu_oracle_beams(ph, beams[:args.cpu_beams])
             extras["cpu_baseline"] = {
@@ -358,7 +401,7 @@ def run_ours(args):
             "updates_per_step": updates,
             "e2e": e2e,
             "clocks": clk,
-            "gpu_launches": args.steps * (B + 3),
+            "gpu_launches": args.steps * (2 * B + 3),
         }
         line.update(extras)
         print(json.dumps(line))
@@ -379,6 +422,9 @@ def main(argv=None):
     ap.add_argument("--latency-beams", type=int, default=20)
     ap.add_argument("--plain-beams", type=int, default=2)
     ap.add_argument("--cpu-beams", type=int, default=2)
+    ap.add_argument("--serve-requests", type=int, default=100, help="requests per serving rate (0: skip)")
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 200.0, 2000.0])
+    ap.add_argument("--serve-batch", type=int, default=32, help="beams per serving batch at most")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args(argv)

@@ -90,6 +90,11 @@ SIGNATURES = {
                                          VP]),
     "ch_dda_trace": (ctypes.c_int, [P(Grid), ctypes.c_int, VP, VP, ctypes.c_int, VP, VP, VP, VP]),
     "ch_cone_directions": (ctypes.c_int, [VP, VP, VP]),
+    "ch_plan_prepare": (ctypes.c_int, [VP, P(Grid), VP]),
+    "ch_plan_memory": (ctypes.c_int, [VP, P(ctypes.c_size_t), P(ctypes.c_size_t)]),
+    "ch_batch_scratch_bytes": (ctypes.c_int, [VP, ctypes.c_int, P(Grid), P(ctypes.c_size_t),
+                                              P(ctypes.c_size_t)]),
+    "ch_plan_trim": (ctypes.c_int, [VP]),
     "ch_plan_sync": (ctypes.c_int, [VP, VP]),
     "ch_plan_stats": (ctypes.c_int, [VP, P(Stats)]),
     "ch_status_string": (ctypes.c_char_p, [ctypes.c_int]),

@@ -212,6 +212,7 @@ class Block:
         self.rotation = rotation
         self.mlc = None
         self._values = None
+        self._rects = []
         if plan is not None:
             self._set_mlc(MLCField.from_plan(plan))
             return
@@ -223,7 +224,7 @@ class Block:
         self.ymax = np.float32(20)
         self.ynum = np.int32(4000)
         self.yres = self.ynum / (self.ymax - self.ymin)
-        self.block_values = np.zeros((self.xnum, self.ynum), dtype=np.float32)
+        self._rects = []        # jaw openings (row and column slices) not yet painted into a map
 
     @classmethod
     def from_plan(cls, plan, beam=None, rotation=np.array([0, 0, 0], dtype=np.float32)):
@@ -246,21 +247,53 @@ class Block:
 
     @property
     def block_values(self):
-        """The transmission map.  For a plan block it is built on first read;
-        from then on the engine uses this array (which the caller may edit)
-        instead of rasterising the leaf table."""
-        if self._values is None and self.mlc is not None:
-            self._values = self.mlc.values()
+        """The transmission map, built on first read.
+
+        Until then a jaw block is only its list of opened rectangles and a
+        plan block its leaf table, and the engine hands those to the GPU
+        directly.  Once read, the engine uses this array (which the caller may
+        edit) instead.
+        """
+        if self._values is None:
+            if self.mlc is not None:
+                self._values = self.mlc.values()
+            else:
+                v = np.zeros((self.xnum, self.ynum), dtype=np.float32)
+                for r0, r1, c0, c1 in self._rects:
+                    v[r0:r1, c0:c1] = np.float32(1)
+                self._values = v
+            self._rects = []
         return self._values
 
     @block_values.setter
     def block_values(self, value):
         self._values = value
         self.mlc = None
+        self._rects = []
 
     def device_mlc(self):
         """The leaf table when the map has never been materialised, else None."""
         return self.mlc if self._values is None else None
+
+    def device_rect(self):
+        """(r0, r1, c0, c1): the open cells when the map was never materialised
+        and is one rectangle of ones (one opening, or openings nested in the
+        largest); (0, 0, 0, 0) when nothing is open; None otherwise."""
+        if self._values is not None or self.mlc is not None:
+            return None
+        n_r, n_c = int(self.xnum), int(self.ynum)
+        boxes = []
+        for r0, r1, c0, c1 in self._rects:
+            a, b, _ = slice(r0, r1).indices(n_r)
+            c, d, _ = slice(c0, c1).indices(n_c)
+            if a < b and c < d:
+                boxes.append((a, b, c, d))
+        if not boxes:
+            return (0, 0, 0, 0)
+        big = max(boxes, key=lambda q: (q[1] - q[0]) * (q[3] - q[2]))
+        if all(big[0] <= q[0] and q[1] <= big[1] and big[2] <= q[2] and q[3] <= big[3] for q in boxes):
+            return big
+        return None
 
     def transmission(self, position):
         """Transmission at an isocentre-plane point (cm), reference rules.
@@ -277,7 +310,10 @@ class Block:
         return self.block_values[int(cell[0]) - 1, int(cell[1]) - 1]
 
     def _open(self, x1, x2, y1, y2):
-        self.block_values[x1:x2, y1:y2] = np.float32(1)
+        if self._values is None:
+            self._rects.append((x1, x2, y1, y2))
+        else:
+            self._values[x1:x2, y1:y2] = np.float32(1)
 
     def set_square(self, length):
         """Open a centred square of side ``length`` cm."""

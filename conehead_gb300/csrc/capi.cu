@@ -104,7 +104,17 @@ struct ch_plan {
   ch_stats stats{};
   bool stats_pending = false;
   bool timed = false;
+  // pinned staging of the per-beam launch records, double buffered, so
+  // their upload is a true async copy; ev_rec[i] marks when the upload from
+  // buffer i has read it
+  void* h_rec[2] = {nullptr, nullptr};
+  size_t h_rec_bytes[2] = {0, 0};
+  cudaEvent_t ev_rec[2] = {nullptr, nullptr};
+  bool rec_pending[2] = {false, false};
+  int rec_next = 0;
   ~ch_plan() {
+    for (int i = 0; i < 2; ++i)
+      if (rec_pending[i] && ev_rec[i]) cudaEventSynchronize(ev_rec[i]);
     for (DevBuf* b : {&K, &theta, &phi, &T, &aabb, &counters, &ranges, &cranges, &cone_beams, &range_beams, &list_v,
                       &st.tap_base,
                       &st.tap_len, &st.taps, &st.offs, &st.tvals, &st.chunk_base, &st.n_chunks, &st.chunk_start, &st.chunk_rec,
@@ -112,6 +122,10 @@ struct ch_plan {
       b->release();
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
+    for (int i = 0; i < 2; ++i) {
+      if (ev_rec[i]) cudaEventDestroy(ev_rec[i]);
+      if (h_rec[i]) cudaFreeHost(h_rec[i]);
+    }
   }
 };
 
@@ -301,7 +315,7 @@ ch_status check_grid(const ch_grid* g) {
 
 ch_status check_beam(const ch_beam* b) {
   if (!b) return fail(CH_ERR_INVALID_ARG, "beam is NULL");
-  if (!b->block || b->block_rows <= 0 || b->block_cols <= 0)
+  if ((!b->block && !b->block_uniform) || b->block_rows <= 0 || b->block_cols <= 0)
     return fail(CH_ERR_INVALID_ARG, "beam block map missing");
   if (b->full_rows < b->block_r0 + b->block_rows || b->full_cols < b->block_c0 + b->block_cols ||
       b->block_r0 < 0 || b->block_c0 < 0)
@@ -460,6 +474,41 @@ struct BeamJob {
   ch_beam beam;
 };
 
+// Scratch arena sizes of one batch, in the order T, aabb, counters, ranges,
+// cranges, cone_beams, range_beams, list_v (the buffers run() grows).
+struct ScratchNeed {
+  size_t bytes[8];
+};
+
+ScratchNeed scratch_need(int n, const ch_grid* grids, int U) {
+  size_t t_total = 0, r_total = 0, max_vox = 1;
+  for (int i = 0; i < n; ++i) {
+    const size_t zp = (size_t)round_up(grids[i].n[2], 4);
+    t_total += (size_t)grids[i].n[0] * grids[i].n[1] * zp;
+    t_total = (t_total + 63) / 64 * 64;
+    const size_t tiles = (size_t)((grids[i].n[0] + TX - 1) / TX) * ((grids[i].n[1] + TY - 1) / TY) *
+                         ((grids[i].n[2] + TZ - 1) / TZ);
+    r_total += tiles * U;
+    max_vox = std::max(max_vox, (size_t)grids[i].n[0] * grids[i].n[1] * grids[i].n[2]);
+  }
+  ScratchNeed r;
+  r.bytes[0] = t_total * sizeof(float);
+  r.bytes[1] = (size_t)n * 8 * sizeof(int);
+  r.bytes[2] = 8 * sizeof(int);
+  r.bytes[3] = std::max<size_t>(r_total, 1) * sizeof(uint32_t);
+  r.bytes[4] = r.bytes[3];
+  r.bytes[5] = (size_t)n * sizeof(ConeBeam);
+  r.bytes[6] = (size_t)n * sizeof(RangeBeam);
+  r.bytes[7] = max_vox * sizeof(int);
+  return r;
+}
+
+const DevBuf* scratch_bufs(const ch_plan* P, int k) {
+  const DevBuf* b[8] = {&P->T, &P->aabb, &P->counters, &P->ranges, &P->cranges, &P->cone_beams, &P->range_beams,
+                        &P->list_v};
+  return b[k];
+}
+
 ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, const int* swap_xy,
               const ch_beam* beams, const ch_settings* settings, float* const* dose, const ch_intermediates* inter,
               bool scatter, cudaStream_t s) {
@@ -518,23 +567,94 @@ ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, 
     total_units += J.n_units;
     max_tiles = std::max(max_tiles, J.n_tiles);
   }
-  CH_CUDA(P->T.ensure(t_total * sizeof(float)));
-  CH_CUDA(P->aabb.ensure((size_t)n * 8 * sizeof(int)));
-  CH_CUDA(P->counters.ensure(8 * sizeof(int)));
-  CH_CUDA(P->ranges.ensure(std::max<size_t>(r_total, 1) * sizeof(uint32_t)));
-  CH_CUDA(P->cranges.ensure(std::max<size_t>(r_total, 1) * sizeof(uint32_t)));
-  CH_CUDA(P->cone_beams.ensure((size_t)n * sizeof(ConeBeam)));
-  CH_CUDA(P->range_beams.ensure((size_t)n * sizeof(RangeBeam)));
-  size_t max_vox = 1;
-  for (int i = 0; i < n; ++i)
-    max_vox = std::max(max_vox, (size_t)jobs[i].g.n[0] * jobs[i].g.n[1] * jobs[i].g.n[2]);
-  CH_CUDA(P->list_v.ensure(max_vox * sizeof(int)));
+  const ScratchNeed need = scratch_need(n, grids, U);
+  CH_CUDA(P->T.ensure(need.bytes[0]));
+  CH_CUDA(P->aabb.ensure(need.bytes[1]));
+  CH_CUDA(P->counters.ensure(need.bytes[2]));
+  CH_CUDA(P->ranges.ensure(need.bytes[3]));
+  CH_CUDA(P->cranges.ensure(need.bytes[4]));
+  CH_CUDA(P->cone_beams.ensure(need.bytes[5]));
+  CH_CUDA(P->range_beams.ensure(need.bytes[6]));
+  CH_CUDA(P->list_v.ensure(need.bytes[7]));
   int* counters = P->counters.as<int>();
   int* flags = counters + 1;
   unsigned long long* updates = reinterpret_cast<unsigned long long*>(counters + 2);
 
   for (auto& e : P->ev)
     if (!e) CH_CUDA(cudaEventCreate(&e));
+  if (!scatter) {
+    // per-beam launch records
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled is not available from the driver");
+    std::vector<ConeBeam> cb(n);
+    std::vector<RangeBeam> rb(n);
+    int unit_begin = 0;
+    for (int i = 0; i < n; ++i) {
+      const BeamJob& J = jobs[i];
+      ConeBeam& C = cb[i];
+      std::memset(&C, 0, sizeof(C));
+      cuuint64_t gdim[3] = {(cuuint64_t)J.g.n[2], (cuuint64_t)J.g.n[1], (cuuint64_t)J.g.n[0]};
+      cuuint64_t gstride[2] = {(cuuint64_t)J.g.zp * 4, (cuuint64_t)J.g.zp * J.g.n[1] * 4};
+      cuuint32_t estr[3] = {1, 1, 1};
+      for (int v = 0; v < N_VARIANTS; ++v) {
+        for (int ex = TX; ex <= var_max_ex(v); ++ex) {
+          cuuint32_t box[3] = {(cuuint32_t)var_p(v), (cuuint32_t)var_rows(v), (cuuint32_t)ex};
+          CUresult r = enc(&C.tmap[tmap_index(v, ex)], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                           (void*)(P->T.as<float>() + J.t_off), gdim, gstride, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+          if (r != CUDA_SUCCESS)
+            return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+        }
+      }
+      C.dose = J.dose;
+      C.ranges = P->ranges.as<uint32_t>() + J.r_off;
+      C.cranges = P->cranges.as<uint32_t>() + J.r_off;
+      for (int k = 0; k < 3; ++k) {
+        C.n[k] = J.g.n[k];
+        C.ntile[k] = J.ntile[k];
+      }
+      C.n_tiles = J.n_tiles;
+      C.unit_begin = unit_begin;
+      C.n_units = J.n_units;
+      unit_begin += J.n_units;
+      RangeBeam& R = rb[i];
+      std::memset(&R, 0, sizeof(R));
+      for (int k = 0; k < 3; ++k) {
+        R.n[k] = J.g.n[k];
+        R.ntile[k] = J.ntile[k];
+        R.origin[k] = J.g.origin[k];
+        R.spacing[k] = J.g.spacing[k];
+      }
+      R.n_tiles = J.n_tiles;
+      make_planes(J.beam, J.grid, J.b, R);
+      R.aabb = P->aabb.as<int>() + 8 * i;
+      R.ranges = P->ranges.as<uint32_t>() + J.r_off;
+      R.cranges = P->cranges.as<uint32_t>() + J.r_off;
+    }
+    // stage through pinned memory: the buffer used two calls ago, once its
+    // upload has read it
+    const int hb = P->rec_next;
+    P->rec_next ^= 1;
+    if (P->rec_pending[hb]) CH_CUDA(cudaEventSynchronize(P->ev_rec[hb]));
+    P->rec_pending[hb] = false;
+    const size_t cb_bytes = n * sizeof(ConeBeam), rb_bytes = n * sizeof(RangeBeam);
+    if (cb_bytes + rb_bytes > P->h_rec_bytes[hb]) {
+      if (P->h_rec[hb]) CH_CUDA(cudaFreeHost(P->h_rec[hb]));
+      P->h_rec[hb] = nullptr;
+      P->h_rec_bytes[hb] = 0;
+      CH_CUDA(cudaMallocHost(&P->h_rec[hb], cb_bytes + rb_bytes));
+      P->h_rec_bytes[hb] = cb_bytes + rb_bytes;
+    }
+    if (!P->ev_rec[hb]) CH_CUDA(cudaEventCreateWithFlags(&P->ev_rec[hb], cudaEventDisableTiming));
+    char* h = static_cast<char*>(P->h_rec[hb]);
+    std::memcpy(h, cb.data(), cb_bytes);
+    std::memcpy(h + cb_bytes, rb.data(), rb_bytes);
+    CH_CUDA(cudaMemcpyAsync(P->cone_beams.p, h, cb_bytes, cudaMemcpyHostToDevice, s));
+    CH_CUDA(cudaMemcpyAsync(P->range_beams.p, h + cb_bytes, rb_bytes, cudaMemcpyHostToDevice, s));
+    CH_CUDA(cudaEventRecord(P->ev_rec[hb], s));
+    P->rec_pending[hb] = true;
+  }
   CH_CUDA(cudaEventRecord(P->ev[0], s));
   launch_init_scratch(P->aabb.as<int>(), n, counters, s);
   for (int i = 0; i < n; ++i) {
@@ -574,57 +694,6 @@ ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, 
     P->last_stream = s;
     return CH_OK;
   }
-  // per-beam launch records
-  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
-  if (!enc) return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled is not available from the driver");
-  std::vector<ConeBeam> cb(n);
-  std::vector<RangeBeam> rb(n);
-  int unit_begin = 0;
-  for (int i = 0; i < n; ++i) {
-    const BeamJob& J = jobs[i];
-    ConeBeam& C = cb[i];
-    std::memset(&C, 0, sizeof(C));
-    cuuint64_t gdim[3] = {(cuuint64_t)J.g.n[2], (cuuint64_t)J.g.n[1], (cuuint64_t)J.g.n[0]};
-    cuuint64_t gstride[2] = {(cuuint64_t)J.g.zp * 4, (cuuint64_t)J.g.zp * J.g.n[1] * 4};
-    cuuint32_t estr[3] = {1, 1, 1};
-    for (int v = 0; v < N_VARIANTS; ++v) {
-      for (int ex = TX; ex <= var_max_ex(v); ++ex) {
-        cuuint32_t box[3] = {(cuuint32_t)var_p(v), (cuuint32_t)var_rows(v), (cuuint32_t)ex};
-        CUresult r = enc(&C.tmap[tmap_index(v, ex)], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
-                         (void*)(P->T.as<float>() + J.t_off), gdim, gstride, box, estr,
-                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (r != CUDA_SUCCESS)
-          return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
-      }
-    }
-    C.dose = J.dose;
-    C.ranges = P->ranges.as<uint32_t>() + J.r_off;
-    C.cranges = P->cranges.as<uint32_t>() + J.r_off;
-    for (int k = 0; k < 3; ++k) {
-      C.n[k] = J.g.n[k];
-      C.ntile[k] = J.ntile[k];
-    }
-    C.n_tiles = J.n_tiles;
-    C.unit_begin = unit_begin;
-    C.n_units = J.n_units;
-    unit_begin += J.n_units;
-    RangeBeam& R = rb[i];
-    std::memset(&R, 0, sizeof(R));
-    for (int k = 0; k < 3; ++k) {
-      R.n[k] = J.g.n[k];
-      R.ntile[k] = J.ntile[k];
-      R.origin[k] = J.g.origin[k];
-      R.spacing[k] = J.g.spacing[k];
-    }
-    R.n_tiles = J.n_tiles;
-    make_planes(J.beam, J.grid, J.b, R);
-    R.aabb = P->aabb.as<int>() + 8 * i;
-    R.ranges = P->ranges.as<uint32_t>() + J.r_off;
-    R.cranges = P->cranges.as<uint32_t>() + J.r_off;
-  }
-  CH_CUDA(cudaMemcpyAsync(P->cone_beams.p, cb.data(), n * sizeof(ConeBeam), cudaMemcpyHostToDevice, s));
-  CH_CUDA(cudaMemcpyAsync(P->range_beams.p, rb.data(), n * sizeof(RangeBeam), cudaMemcpyHostToDevice, s));
   launch_range(P->range_beams.as<RangeBeam>(), n, max_tiles, D, s);
   CH_CUDA(cudaGetLastError());
   CH_CUDA(cudaEventRecord(P->ev[2], s));
@@ -917,6 +986,59 @@ ch_status ch_cone_directions(ch_plan* P, float* out, void* stream) {
   }
   CH_CUDA(cudaMemcpyAsync(out, P->st.raw_dirs.p, (size_t)P->st.n_raw * 3 * sizeof(float),
                           cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+  return CH_OK;
+}
+
+ch_status ch_plan_prepare(ch_plan* P, const ch_grid* grid, void* stream) {
+  if (!P) return fail(CH_ERR_INVALID_ARG, "plan is NULL");
+  if (!P->have_kernel) return fail(CH_ERR_NO_KERNEL, "ch_plan_set_kernel has not been called");
+  ch_status st = check_grid(grid);
+  if (st != CH_OK) return st;
+  CH_CUDA(cudaSetDevice(P->device));
+  return ensure_stencils(P, grid->spacing, grid->n, (cudaStream_t)stream);
+}
+
+ch_status ch_plan_memory(ch_plan* P, size_t* tables, size_t* scratch) {
+  if (!P) return fail(CH_ERR_INVALID_ARG, "plan is NULL");
+  size_t b = P->K.bytes + P->theta.bytes + P->phi.bytes;
+  const StencilSet& S = P->st;
+  for (const DevBuf* d : {&S.tap_base, &S.tap_len, &S.taps, &S.offs, &S.tvals, &S.chunk_base, &S.n_chunks,
+                          &S.chunk_start, &S.chunk_rec, &S.dirs, &S.raw_dirs})
+    b += d->bytes;
+  size_t a = 0;
+  for (int k = 0; k < 8; ++k) a += scratch_bufs(P, k)->bytes;
+  if (tables) *tables = b;
+  if (scratch) *scratch = a;
+  return CH_OK;
+}
+
+ch_status ch_batch_scratch_bytes(ch_plan* P, int n, const ch_grid* grids, size_t* growth, size_t* total) {
+  if (!P || !grids || n <= 0) return fail(CH_ERR_INVALID_ARG, "plan, grids or count missing");
+  for (int i = 0; i < n; ++i) {
+    ch_status st = check_grid(&grids[i]);
+    if (st != CH_OK) return st;
+  }
+  const int U = P->st.valid ? P->st.n_dirs : P->n_theta * P->n_phi > 0 ? P->n_theta * P->n_phi : 576;
+  const ScratchNeed need = scratch_need(n, grids, U);
+  size_t g = 0, t = 0;
+  for (int k = 0; k < 8; ++k) {
+    const size_t cur = scratch_bufs(P, k)->bytes;
+    t += need.bytes[k];
+    if (need.bytes[k] > cur) g += need.bytes[k] - cur;
+  }
+  if (growth) *growth = g;
+  if (total) *total = t;
+  return CH_OK;
+}
+
+ch_status ch_plan_trim(ch_plan* P) {
+  if (!P) return fail(CH_ERR_INVALID_ARG, "plan is NULL");
+  CH_CUDA(cudaSetDevice(P->device));
+  // cudaFree waits for the device, so no call of this plan is still reading the arena
+  for (DevBuf* b : {&P->T, &P->aabb, &P->counters, &P->ranges, &P->cranges, &P->cone_beams, &P->range_beams,
+                    &P->list_v})
+    b->release();
+  P->stats_pending = false;
   return CH_OK;
 }
 

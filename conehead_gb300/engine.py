@@ -19,11 +19,19 @@ from .kernel import poly_kernel_tables
 @dataclass
 class DeviceBlock:
     """Block map on the device, cropped to its nonzero bounding box."""
-    crop: object          # torch float32 tensor [rows, cols]
+    crop: object          # torch float32 tensor [rows, cols]; None for a uniform crop
     r0: int
     c0: int
     full_shape: tuple
     uniform: bool = False  # every crop value is 1.0 (a jaw rectangle)
+    shape: tuple = None    # crop shape when there is no tensor
+    zero: bool = False     # nothing open: a 1 x 1 crop of zeros
+
+    def __post_init__(self):
+        if self.crop is not None:
+            self.shape = tuple(self.crop.shape)
+        elif self.zero:
+            self.uniform = False
 
 
 @dataclass
@@ -97,10 +105,22 @@ class DoseEngine:
                                          self.stream()), "ch_block_from_mlc")
         return DeviceBlock(crop, r0, c0, full)
 
+    def jaw_block(self, rect, full_shape=(4000, 4000)):
+        """A rectangle of ones: no memory at all, the kernels read the flag."""
+        r0, r1, c0, c1 = rect
+        if r1 <= r0 or c1 <= c0:
+            return DeviceBlock(None, 0, 0, full_shape, True, (1, 1), zero=True)
+        return DeviceBlock(None, r0, c0, full_shape, True, (r1 - r0, c1 - c0))
+
     def block_for(self, block):
-        """Device block of a Block-like object: plan blocks whose map was never
-        read on the host are rasterised from their leaf table, anything else
-        is cropped from ``block_values``."""
+        """Device block of a Block-like object.  Blocks whose map was never read
+        on the host go to the GPU as what they are -- a jaw rectangle (a
+        uniform crop, no memory) or a leaf table (rasterised on the device);
+        anything else is cropped from ``block_values``."""
+        rect = getattr(block, "device_rect", None)
+        rect = rect() if callable(rect) else None
+        if rect is not None:
+            return self.jaw_block(rect, (int(block.xnum), int(block.ynum)))
         table = getattr(block, "device_mlc", None)
         mlc = table() if callable(table) else None
         if mlc is not None:
@@ -115,12 +135,32 @@ class DoseEngine:
         if swap_xy is None:
             swap_xy = int(size[0] == size[1])
         grid = N.grid_struct(size, phantom.origin, phantom.spacing)
-        beam = N.beam_struct(source, dblock.crop.data_ptr(), dblock.crop.shape, dblock.r0, dblock.c0,
+        if dblock.zero:
+            if getattr(self, "_zero_crop", None) is None:
+                self._zero_crop = self.torch.zeros((1, 1), dtype=self.torch.float32, device=self.device)
+            dblock = DeviceBlock(self._zero_crop, 0, 0, dblock.full_shape)
+        ptr = dblock.crop.data_ptr() if dblock.crop is not None else None
+        beam = N.beam_struct(source, ptr, dblock.shape, dblock.r0, dblock.c0,
                              dblock.full_shape, dblock.uniform)
-        s = settings if isinstance(settings, N.Settings) else N.settings_struct(settings)
+        s = settings if isinstance(settings, N.Settings) else self._settings(settings)
         if dose is None:
             dose = self.torch.empty(size, dtype=self.torch.float32, device=self.device)
         return BeamJob(grid, rho, int(swap_xy), beam, s, dose, (dblock.crop,))
+
+    def _settings(self, settings):
+        """ch_settings of a settings dict, cached on its contents."""
+        try:
+            key = tuple((k, tuple(v.items()) if isinstance(v, dict) else v) for k, v in sorted(settings.items()))
+            hash(key)
+        except TypeError:
+            return N.settings_struct(settings)
+        cache = self.__dict__.setdefault("_settings_cache", {})
+        s = cache.get(key)
+        if s is None:
+            if len(cache) > 64:
+                cache.clear()
+            s = cache[key] = N.settings_struct(settings)
+        return s
 
     # ----------------------------------------------------------- compute --
     def run(self, job, intermediates=False, scatter=False):

@@ -73,7 +73,8 @@ typedef struct {
   int block_r0, block_c0;
   int full_rows, full_cols;
   int block_uniform;    /* 1 when every value of the crop is 1.0 (a jaw
-                           rectangle): lookups then read no memory */
+                           rectangle): lookups then read no memory, and
+                           `block` may be NULL */
 } ch_beam;
 
 /* settings dict of Conehead.calculate (example.py:27-58) plus the spectrum
@@ -220,6 +221,28 @@ ch_status ch_dda_trace(const ch_grid* grid, int n_rays, const int* starts_dev,
 /* Test hook: the cone directions the device computes for (theta_i, phi_j),
  * float32 [n_theta][n_phi][3] into out_dev. */
 ch_status ch_cone_directions(ch_plan* plan, float* out_dev, void* stream);
+
+/* Build the plan's direction stencils for this grid's voxel spacing and
+ * size ahead of the first dose call (otherwise the first call that brings
+ * a new spacing or a larger grid builds them).  Serving code prepares each
+ * plan for its largest grid once, so no request pays the build.  No
+ * counterpart in the reference (it rebuilds everything per call,
+ * conehead/conehead.py:541-738). */
+ch_status ch_plan_prepare(ch_plan* plan, const ch_grid* grid, void* stream);
+
+/* Device bytes the plan holds: kernel tables and stencils (`tables`), and
+ * its scratch arena (`scratch`).  Either pointer may be NULL. */
+ch_status ch_plan_memory(ch_plan* plan, size_t* tables, size_t* scratch);
+
+/* Scratch a ch_dose_batch call over these n grids needs: `total` is the
+ * arena size it uses, `growth` how many bytes the plan's arena would grow
+ * by (the arena only grows).  For admission control; no counterpart in the
+ * reference.  Stencil tables (a few MB per spacing) are not included. */
+ch_status ch_batch_scratch_bytes(ch_plan* plan, int n, const ch_grid* grids, size_t* growth, size_t* total);
+
+/* Free the plan's scratch arena (kernel tables and stencils stay).  Waits
+ * for all work on the device first. */
+ch_status ch_plan_trim(ch_plan* plan);
 
 /* Wait for the plan's work on `stream` and report device-side failures
  * (CH_ERR_TIMEOUT, CH_ERR_PARALLEL_RAY) of the last dose call. */
