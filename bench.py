@@ -18,6 +18,12 @@ fluence -> TERMA -> collapsed-cone dose (float32 dose and accumulation).
   cpu_baseline / --impl reference
               the CPU oracle (C++ FP64 restatement of the reference path,
               OpenMP over every host core) on whole beams of the workload
+  batched_captured
+              64 beams on mixed 64^3-160^3 slab phantoms (jaws U[2,20] cm,
+              gantry U[0,360), collimator U[0,90)) in one captured CUDA graph
+              with the autotuned schedule
+  adjoint     forward dose and beamlet-weight gradient (ch_dose_adjoint) on
+              the 128^3 phantom with 40 x 40 beamlets of 0.5 cm
   serving     the continuous-batching server (conehead_gb300.serving) under
               open-loop Poisson arrivals: requests of 1-8 beams (5 x 5 cm,
               gantry U[0, 360)) on resident slab phantoms of 64^3, 96^3,
@@ -224,6 +230,97 @@ def serving_extras(args, dev):
             "budget_gb": budget / 1e9, "max_batch_beams": args.serve_batch, "rates": rows}
 
 
+def adjoint_extras(args, dev):
+    """Beamlet-weight gradient at 128^3: 40 x 40 beamlets of 0.5 cm, weights
+    U[0, 1], L = sum (dose - target)^2 with target 2 in a 2 cm-radius sphere.
+    Times (CUDA events on the engine's stream) the forward dose, the objective
+    gradient in torch, and ch_dose_adjoint."""
+    import torch
+    from conehead_gb300.adjoint import BeamletDose, BeamletGrid, sphere_target
+    from conehead_gb300.conehead import engine
+    from conehead_gb300 import Source
+    rng = np.random.default_rng(7)
+    ph = workload(args.grid, args.spacing)
+    target = torch.from_numpy(sphere_target(ph, tuple(rng.uniform(-3, 3, 3)), 2.0)).to(dev)
+    src = Source()
+    src.gantry = float(rng.uniform(0, 360))
+    src.collimator = 0.0
+    bl = BeamletGrid.square(40, 0.5)
+    op = BeamletDose(engine(dev.index), ph, src, bl, SETTINGS)
+    w = torch.tensor(rng.uniform(0, 1, bl.shape).astype(np.float32), device=dev)
+    st = torch.cuda.current_stream(dev)
+    fwd, bwd = [], []
+    for it in range(args.adjoint_iters + 3):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(st)
+        dose = op.forward(w)
+        e1.record(st)
+        grad_dose = 2.0 * (dose - target)
+        g = op.backward(grad_dose)
+        e2.record(st)
+        e2.synchronize()
+        if it >= 3:
+            fwd.append(e0.elapsed_time(e1))
+            bwd.append(e1.elapsed_time(e2))
+    op.eng.sync()
+    assert float(g.abs().max()) > 0
+    return {"workload": f"{args.grid}^3 slab phantom @ {args.spacing:g} cm, 40x40 beamlets of 0.5 cm, "
+                        "weights U[0,1], L = sum (dose - target)^2",
+            "forward_ms": statistics.median(fwd), "gradient_ms": statistics.median(bwd),
+            "gradient_evals_per_s": 1000.0 / (statistics.median(fwd) + statistics.median(bwd)),
+            "iters": len(fwd)}
+
+
+def batched_extras(args, dev):
+    """64 beams in one captured launch: heterogeneous slab phantoms of 64^3,
+    96^3, 128^3 and 160^3 at 0.25 cm, jaws X and Y each U[2, 20] cm, gantry
+    U[0, 360), collimator U[0, 90); schedule from the autotuner.  Times graph
+    replays (CUDA events, L2 flushed between replays) and, for reference, the
+    same batch uncaptured with the default schedule."""
+    import torch
+    from conehead_gb300.autotune import autotune, time_batch
+    from conehead_gb300.engine import DoseEngine
+    from conehead_gb300.phantoms import random_beam
+    eng = DoseEngine(dev.index)
+    eng.set_kernel(SETTINGS["energy_weights"])
+    sizes = (64, 96, 128, 160)
+    phantoms = {n: workload(n, args.spacing, seed=n) for n in sizes}
+    rhos = {n: eng.upload_densities(ph.densities) for n, ph in phantoms.items()}
+    rng = np.random.default_rng(64)
+    jobs = []
+    for i in range(args.batch_beams):
+        n = sizes[int(rng.integers(0, len(sizes)))]
+        src, blk = random_beam(rng, rect=(2.0, 20.0), collimator=True)
+        jobs.append(eng.job(phantoms[n], rhos[n], src, eng.block_for(blk), SETTINGS))
+    eng.prepare((max(sizes),) * 3, (args.spacing,) * 3)
+    eng.set_tuning()
+    default_ms = time_batch(eng, jobs, iters=2)
+    tuned = autotune(eng, jobs)
+    batch = eng.capture(jobs)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream(dev)
+    ms = []
+    for it in range(args.batch_iters + 2):
+        flush.fill_(float(it))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        batch.launch()
+        e1.record(st)
+        e1.synchronize()
+        if it >= 2:
+            ms.append(e0.elapsed_time(e1))
+    batch.sync()
+    batch.close()
+    eng.close()
+    med = statistics.median(ms)
+    return {"workload": f"{args.batch_beams} beams, slab phantoms 64^3/96^3/128^3/160^3 @ {args.spacing:g} cm, "
+                        "jaws U[2,20] cm, gantry U[0,360), collimator U[0,90), one captured CUDA graph",
+            "beams_per_s": args.batch_beams * 1000.0 / med, "ms_per_batch": med,
+            "uncaptured_default_schedule_ms": default_ms, "tuning": tuned["tuning"],
+            "tuned_uncaptured_ms": tuned["ms"], "autotune_cached": tuned["cached"],
+            "kernels_per_batch": 2 * args.batch_beams + 3, "graph_launches_per_batch": 1}
+
+
 def config(args, beams_per_step=None):
     return {"workload": f"heterogeneous slab phantom {args.grid}^3 @ {args.spacing:g} cm, "
                         f"{args.field:g}x{args.field:g} cm2 field, gantry U[0,360), 6 MV, 12x48 cones",
@@ -377,6 +474,10 @@ def run_ours(args):
         extras["plain_gpu_path"] = "prologue + per-voxel scatter with float32 atomics, one beam per launch"
         if args.serve_requests > 0:
             extras["serving"] = serving_extras(args, dev)
+        if args.adjoint_iters > 0:
+            extras["adjoint"] = adjoint_extras(args, dev)
+        if args.batch_beams > 0:
+            extras["batched_captured"] = batched_extras(args, dev)
         if not args.no_cpu:
             cv, cores, dt = cpu_oracle_beams(ph, beams[:args.cpu_beams])
             extras["cpu_baseline"] = {
@@ -425,6 +526,9 @@ def main(argv=None):
     ap.add_argument("--serve-requests", type=int, default=100, help="requests per serving rate (0: skip)")
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 200.0, 2000.0])
     ap.add_argument("--serve-batch", type=int, default=32, help="beams per serving batch at most")
+    ap.add_argument("--adjoint-iters", type=int, default=5, help="timed gradient evaluations (0: skip)")
+    ap.add_argument("--batch-beams", type=int, default=64, help="beams of the captured mixed batch (0: skip)")
+    ap.add_argument("--batch-iters", type=int, default=5)
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args(argv)

@@ -66,6 +66,15 @@ class MLC(ctypes.Structure):
                 ("tip", ctypes.c_double * CH_MLC_TIP_CELLS)]
 
 
+class Beamlets(ctypes.Structure):
+    _fields_ = [("rows", ctypes.c_int), ("cols", ctypes.c_int), ("cell_rows", ctypes.c_int),
+                ("cell_cols", ctypes.c_int), ("r0", ctypes.c_int), ("c0", ctypes.c_int)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("dir_group", ctypes.c_int), ("unit_order", ctypes.c_int), ("terma_ctas_per_sm", ctypes.c_int)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("ms_prologue", ctypes.c_float), ("ms_range", ctypes.c_float),
                 ("ms_cone", ctypes.c_float), ("updates", ctypes.c_double),
@@ -88,8 +97,19 @@ SIGNATURES = {
     "ch_dose_static": (ctypes.c_int, [VP, P(Grid), VP, ctypes.c_int, P(Beam), P(Settings), VP, VP]),
     "ch_block_from_mlc": (ctypes.c_int, [P(MLC), VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          VP]),
+    "ch_block_from_beamlets": (ctypes.c_int, [P(Beamlets), VP, VP, VP]),
+    "ch_cone": (ctypes.c_int, [VP, P(Grid), VP, VP, ctypes.c_int, VP]),
+    "ch_dose_adjoint": (ctypes.c_int, [VP, P(Grid), VP, ctypes.c_int, P(Beam), P(Beamlets), P(Settings), VP, VP, VP,
+                                       VP]),
     "ch_dda_trace": (ctypes.c_int, [P(Grid), ctypes.c_int, VP, VP, ctypes.c_int, VP, VP, VP, VP]),
     "ch_cone_directions": (ctypes.c_int, [VP, VP, VP]),
+    "ch_plan_set_tuning": (ctypes.c_int, [VP, P(Tuning)]),
+    "ch_plan_get_tuning": (ctypes.c_int, [VP, P(Tuning)]),
+    "ch_batch_create": (ctypes.c_int, [VP, ctypes.c_int, P(Grid), P(VP), P(ctypes.c_int), P(Beam), P(Settings),
+                                       P(VP), VP, P(VP)]),
+    "ch_batch_launch": (ctypes.c_int, [VP, VP]),
+    "ch_batch_sync": (ctypes.c_int, [VP, VP]),
+    "ch_batch_destroy": (None, [VP]),
     "ch_plan_prepare": (ctypes.c_int, [VP, P(Grid), VP]),
     "ch_plan_memory": (ctypes.c_int, [VP, P(ctypes.c_size_t), P(ctypes.c_size_t)]),
     "ch_batch_scratch_bytes": (ctypes.c_int, [VP, ctypes.c_int, P(Grid), P(ctypes.c_size_t),

@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -93,12 +94,16 @@ struct StencilSet {
 struct ch_plan {
   int device = 0;
   int n_sm = 0;
+  ch_tuning tuning{DIR_GROUP, 0, 8};
+  int live_batches = 0;      // captured batches reading this plan's stencils
   bool have_kernel = false;
   int n_phi = 0, n_r = 0, n_theta = 0;
   DevBuf K, theta, phi;
   StencilSet st;
+  StencilSet st_adj;         // the same walks mirrored (offsets and directions negated): the transposed cone
   // scratch
   DevBuf T, aabb, counters, ranges, cranges, cone_beams, range_beams, list_v;
+  DevBuf adj_in, adj_out, adj_w;   // cone-operator input (padded), output, beamlet gradient (float64)
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaStream_t last_stream = nullptr;
   ch_stats stats{};
@@ -116,10 +121,12 @@ struct ch_plan {
     for (int i = 0; i < 2; ++i)
       if (rec_pending[i] && ev_rec[i]) cudaEventSynchronize(ev_rec[i]);
     for (DevBuf* b : {&K, &theta, &phi, &T, &aabb, &counters, &ranges, &cranges, &cone_beams, &range_beams, &list_v,
-                      &st.tap_base,
-                      &st.tap_len, &st.taps, &st.offs, &st.tvals, &st.chunk_base, &st.n_chunks, &st.chunk_start, &st.chunk_rec,
-                      &st.dirs, &st.raw_dirs})
+                      &adj_in, &adj_out, &adj_w})
       b->release();
+    for (StencilSet* S : {&st, &st_adj})
+      for (DevBuf* b : {&S->tap_base, &S->tap_len, &S->taps, &S->offs, &S->tvals, &S->chunk_base, &S->n_chunks,
+                        &S->chunk_start, &S->chunk_rec, &S->dirs, &S->raw_dirs})
+        b->release();
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     for (int i = 0; i < 2; ++i) {
@@ -132,6 +139,12 @@ struct ch_plan {
 namespace {
 
 // ------------------------------------------------------------ stencils --
+ch_status assemble_stencils(ch_plan* P, StencilSet& S, int sign, int n_raw, int max_len,
+                            const std::vector<short4>& h_off_in, const std::vector<float>& h_t,
+                            const std::vector<float>& h_dk, const std::vector<int>& h_len,
+                            const std::vector<float>& h_dir_in, const float* spacing, const int* cap,
+                            cudaStream_t s);
+
 ch_status build_stencils(ch_plan* P, const float* spacing, const int* cap, cudaStream_t s) {
   StencilSet& S = P->st;
   const int n_raw = P->n_theta * P->n_phi;
@@ -160,6 +173,30 @@ ch_status build_stencils(ch_plan* P, const float* spacing, const int* cap, cudaS
   dk.release();
   len.release();
 
+  ch_status st = assemble_stencils(P, P->st, +1, n_raw, max_len, h_off, h_t, h_dk, h_len, h_dir, spacing, cap, s);
+  if (st != CH_OK) return st;
+  return assemble_stencils(P, P->st_adj, -1, n_raw, max_len, h_off, h_t, h_dk, h_len, h_dir, spacing, cap, s);
+}
+
+// Tap tables, chunks and launch data of one stencil set from the raw walks.
+// sign = -1 mirrors every walk (offsets -O[m], direction -d): the DDA from a
+// voxel centre along -d visits exactly -O[m] at the same t (the tie rule
+// compares the same t values), so the mirrored set gathers the transpose.
+ch_status assemble_stencils(ch_plan* P, StencilSet& S, int sign, int n_raw, int max_len,
+                            const std::vector<short4>& h_off_in, const std::vector<float>& h_t,
+                            const std::vector<float>& h_dk, const std::vector<int>& h_len,
+                            const std::vector<float>& h_dir_in, const float* spacing, const int* cap,
+                            cudaStream_t s) {
+  std::vector<short4> h_off(h_off_in);
+  std::vector<float> h_dir(h_dir_in);
+  if (sign < 0) {
+    for (short4& o : h_off) {
+      o.x = (short)-o.x;
+      o.y = (short)-o.y;
+      o.z = (short)-o.z;
+    }
+    for (float& d : h_dir) d = -d;
+  }
   // merge identical walks (the 12 phi = 180 deg directions are one walk)
   struct Key {
     std::vector<short4> o;
@@ -277,14 +314,18 @@ ch_status ensure_stencils(ch_plan* P, const float* spacing, const int* dims, cud
   for (int k = 0; k < 3 && ok; ++k)
     ok = S.spacing[k] == spacing[k] && S.cap[k] >= dims[k];
   if (ok) return CH_OK;
+  if (P->live_batches > 0)
+    return fail(CH_ERR_INVALID_ARG, "the plan's stencils cannot be rebuilt while captured batches use them "
+                                    "(ch_batch_destroy them, or prepare the plan for the largest grid first)");
   int cap[3];
   for (int k = 0; k < 3; ++k) cap[k] = std::max(dims[k], S.valid && S.spacing[k] == spacing[k] ? S.cap[k] : 0);
   return build_stencils(P, spacing, cap, s);
 }
 
-ConeDirs cone_dirs(const ch_plan* P) {
-  const StencilSet& S = P->st;
+ConeDirs cone_dirs(const StencilSet& S, const ch_tuning& t) {
   ConeDirs D;
+  D.group = t.dir_group;
+  D.order = t.unit_order;
   D.n_dirs = S.n_dirs;
   D.tap_base = S.tap_base.as<int>();
   D.tap_len = S.tap_len.as<int>();
@@ -474,6 +515,50 @@ struct BeamJob {
   ch_beam beam;
 };
 
+// The 39 TMA tensor maps of one padded [x][y][zp] volume: one per window
+// shape and x extent (boxes P z x rows y x ex x, zero fill outside).
+ch_status encode_windows(PFN_cuTensorMapEncodeTiled_v12000 enc, ConeBeam& C, float* vol, const GridDev& g) {
+  cuuint64_t gdim[3] = {(cuuint64_t)g.n[2], (cuuint64_t)g.n[1], (cuuint64_t)g.n[0]};
+  cuuint64_t gstride[2] = {(cuuint64_t)g.zp * 4, (cuuint64_t)g.zp * g.n[1] * 4};
+  cuuint32_t estr[3] = {1, 1, 1};
+  for (int v = 0; v < N_VARIANTS; ++v) {
+    for (int ex = TX; ex <= var_max_ex(v); ++ex) {
+      cuuint32_t box[3] = {(cuuint32_t)var_p(v), (cuuint32_t)var_rows(v), (cuuint32_t)ex};
+      CUresult r = enc(&C.tmap[tmap_index(v, ex)], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)vol, gdim, gstride,
+                       box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS) return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    }
+  }
+  return CH_OK;
+}
+
+// Upload launch records through the plan's double-buffered pinned staging
+// (a true async copy, issued before the kernels that read them).
+ch_status stage_records(ch_plan* P, const ConeBeam* cb, const RangeBeam* rb, int n, cudaStream_t s) {
+  const int hb = P->rec_next;
+  P->rec_next ^= 1;
+  if (P->rec_pending[hb]) CH_CUDA(cudaEventSynchronize(P->ev_rec[hb]));
+  P->rec_pending[hb] = false;
+  const size_t cb_bytes = n * sizeof(ConeBeam), rb_bytes = n * sizeof(RangeBeam);
+  if (cb_bytes + rb_bytes > P->h_rec_bytes[hb]) {
+    if (P->h_rec[hb]) CH_CUDA(cudaFreeHost(P->h_rec[hb]));
+    P->h_rec[hb] = nullptr;
+    P->h_rec_bytes[hb] = 0;
+    CH_CUDA(cudaMallocHost(&P->h_rec[hb], cb_bytes + rb_bytes));
+    P->h_rec_bytes[hb] = cb_bytes + rb_bytes;
+  }
+  if (!P->ev_rec[hb]) CH_CUDA(cudaEventCreateWithFlags(&P->ev_rec[hb], cudaEventDisableTiming));
+  char* h = static_cast<char*>(P->h_rec[hb]);
+  std::memcpy(h, cb, cb_bytes);
+  std::memcpy(h + cb_bytes, rb, rb_bytes);
+  CH_CUDA(cudaMemcpyAsync(P->cone_beams.p, h, cb_bytes, cudaMemcpyHostToDevice, s));
+  CH_CUDA(cudaMemcpyAsync(P->range_beams.p, h + cb_bytes, rb_bytes, cudaMemcpyHostToDevice, s));
+  CH_CUDA(cudaEventRecord(P->ev_rec[hb], s));
+  P->rec_pending[hb] = true;
+  return CH_OK;
+}
+
 // Scratch arena sizes of one batch, in the order T, aabb, counters, ranges,
 // cranges, cone_beams, range_beams, list_v (the buffers run() grows).
 struct ScratchNeed {
@@ -509,14 +594,35 @@ const DevBuf* scratch_bufs(const ch_plan* P, int k) {
   return b[k];
 }
 
-ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, const int* swap_xy,
-              const ch_beam* beams, const ch_settings* settings, float* const* dose, const ch_intermediates* inter,
-              bool scatter, cudaStream_t s) {
+// A validated batch: per-beam device parameters and scratch offsets.
+struct BatchPlan {
+  std::vector<BeamJob> jobs;
+  int U = 0;
+  int total_units = 0;
+  int max_tiles = 0;
+};
+
+// Scratch a batch runs in (the plan's arena, or a captured batch's own).
+struct Scratch {
+  float* T;
+  int* aabb;
+  int* counters;
+  uint32_t* ranges;
+  uint32_t* cranges;
+  ConeBeam* cone_beams;
+  RangeBeam* range_beams;
+  int* list_v;
+};
+
+ch_status plan_batch(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, const int* swap_xy,
+                     const ch_beam* beams, const ch_settings* settings, float* const* dose, cudaStream_t s,
+                     BatchPlan& B) {
   if (!P) return fail(CH_ERR_INVALID_ARG, "plan is NULL");
   if (!P->have_kernel) return fail(CH_ERR_NO_KERNEL, "ch_plan_set_kernel has not been called");
   if (n <= 0) return fail(CH_ERR_INVALID_ARG, "no beams");
+  if (!grids || !beams || !settings) return fail(CH_ERR_INVALID_ARG, "batch arrays missing");
   CH_CUDA(cudaSetDevice(P->device));
-  std::vector<BeamJob> jobs(n);
+  B.jobs.assign(n, BeamJob{});
   int dims[3] = {0, 0, 0};
   for (int i = 0; i < n; ++i) {
     ch_status st;
@@ -535,12 +641,13 @@ ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, 
   }
   ch_status st = ensure_stencils(P, grids[0].spacing, dims, s);
   if (st != CH_OK) return st;
-  const int U = P->st.n_dirs;
-  const int n_groups = (U + DIR_GROUP - 1) / DIR_GROUP;
+  B.U = P->st.n_dirs;
+  const int n_groups = (B.U + P->tuning.dir_group - 1) / P->tuning.dir_group;
   size_t t_total = 0, r_total = 0;
-  int total_units = 0, max_tiles = 0;
+  B.total_units = 0;
+  B.max_tiles = 0;
   for (int i = 0; i < n; ++i) {
-    BeamJob& J = jobs[i];
+    BeamJob& J = B.jobs[i];
     J.grid = grids[i];
     J.beam = beams[i];
     for (int k = 0; k < 3; ++k) {
@@ -563,102 +670,69 @@ ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, 
     J.n_tiles = J.ntile[0] * J.ntile[1] * J.ntile[2];
     J.n_units = J.n_tiles * n_groups;
     J.r_off = r_total;
-    r_total += (size_t)J.n_tiles * U;
-    total_units += J.n_units;
-    max_tiles = std::max(max_tiles, J.n_tiles);
+    r_total += (size_t)J.n_tiles * B.U;
+    B.total_units += J.n_units;
+    B.max_tiles = std::max(B.max_tiles, J.n_tiles);
   }
-  const ScratchNeed need = scratch_need(n, grids, U);
-  CH_CUDA(P->T.ensure(need.bytes[0]));
-  CH_CUDA(P->aabb.ensure(need.bytes[1]));
-  CH_CUDA(P->counters.ensure(need.bytes[2]));
-  CH_CUDA(P->ranges.ensure(need.bytes[3]));
-  CH_CUDA(P->cranges.ensure(need.bytes[4]));
-  CH_CUDA(P->cone_beams.ensure(need.bytes[5]));
-  CH_CUDA(P->range_beams.ensure(need.bytes[6]));
-  CH_CUDA(P->list_v.ensure(need.bytes[7]));
-  int* counters = P->counters.as<int>();
-  int* flags = counters + 1;
-  unsigned long long* updates = reinterpret_cast<unsigned long long*>(counters + 2);
+  return CH_OK;
+}
 
-  for (auto& e : P->ev)
-    if (!e) CH_CUDA(cudaEventCreate(&e));
-  if (!scatter) {
-    // per-beam launch records
-    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
-    if (!enc) return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled is not available from the driver");
-    std::vector<ConeBeam> cb(n);
-    std::vector<RangeBeam> rb(n);
-    int unit_begin = 0;
-    for (int i = 0; i < n; ++i) {
-      const BeamJob& J = jobs[i];
-      ConeBeam& C = cb[i];
-      std::memset(&C, 0, sizeof(C));
-      cuuint64_t gdim[3] = {(cuuint64_t)J.g.n[2], (cuuint64_t)J.g.n[1], (cuuint64_t)J.g.n[0]};
-      cuuint64_t gstride[2] = {(cuuint64_t)J.g.zp * 4, (cuuint64_t)J.g.zp * J.g.n[1] * 4};
-      cuuint32_t estr[3] = {1, 1, 1};
-      for (int v = 0; v < N_VARIANTS; ++v) {
-        for (int ex = TX; ex <= var_max_ex(v); ++ex) {
-          cuuint32_t box[3] = {(cuuint32_t)var_p(v), (cuuint32_t)var_rows(v), (cuuint32_t)ex};
-          CUresult r = enc(&C.tmap[tmap_index(v, ex)], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
-                           (void*)(P->T.as<float>() + J.t_off), gdim, gstride, box, estr,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-          if (r != CUDA_SUCCESS)
-            return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
-        }
-      }
-      C.dose = J.dose;
-      C.ranges = P->ranges.as<uint32_t>() + J.r_off;
-      C.cranges = P->cranges.as<uint32_t>() + J.r_off;
-      for (int k = 0; k < 3; ++k) {
-        C.n[k] = J.g.n[k];
-        C.ntile[k] = J.ntile[k];
-      }
-      C.n_tiles = J.n_tiles;
-      C.unit_begin = unit_begin;
-      C.n_units = J.n_units;
-      unit_begin += J.n_units;
-      RangeBeam& R = rb[i];
-      std::memset(&R, 0, sizeof(R));
-      for (int k = 0; k < 3; ++k) {
-        R.n[k] = J.g.n[k];
-        R.ntile[k] = J.ntile[k];
-        R.origin[k] = J.g.origin[k];
-        R.spacing[k] = J.g.spacing[k];
-      }
-      R.n_tiles = J.n_tiles;
-      make_planes(J.beam, J.grid, J.b, R);
-      R.aabb = P->aabb.as<int>() + 8 * i;
-      R.ranges = P->ranges.as<uint32_t>() + J.r_off;
-      R.cranges = P->cranges.as<uint32_t>() + J.r_off;
-    }
-    // stage through pinned memory: the buffer used two calls ago, once its
-    // upload has read it
-    const int hb = P->rec_next;
-    P->rec_next ^= 1;
-    if (P->rec_pending[hb]) CH_CUDA(cudaEventSynchronize(P->ev_rec[hb]));
-    P->rec_pending[hb] = false;
-    const size_t cb_bytes = n * sizeof(ConeBeam), rb_bytes = n * sizeof(RangeBeam);
-    if (cb_bytes + rb_bytes > P->h_rec_bytes[hb]) {
-      if (P->h_rec[hb]) CH_CUDA(cudaFreeHost(P->h_rec[hb]));
-      P->h_rec[hb] = nullptr;
-      P->h_rec_bytes[hb] = 0;
-      CH_CUDA(cudaMallocHost(&P->h_rec[hb], cb_bytes + rb_bytes));
-      P->h_rec_bytes[hb] = cb_bytes + rb_bytes;
-    }
-    if (!P->ev_rec[hb]) CH_CUDA(cudaEventCreateWithFlags(&P->ev_rec[hb], cudaEventDisableTiming));
-    char* h = static_cast<char*>(P->h_rec[hb]);
-    std::memcpy(h, cb.data(), cb_bytes);
-    std::memcpy(h + cb_bytes, rb.data(), rb_bytes);
-    CH_CUDA(cudaMemcpyAsync(P->cone_beams.p, h, cb_bytes, cudaMemcpyHostToDevice, s));
-    CH_CUDA(cudaMemcpyAsync(P->range_beams.p, h + cb_bytes, rb_bytes, cudaMemcpyHostToDevice, s));
-    CH_CUDA(cudaEventRecord(P->ev_rec[hb], s));
-    P->rec_pending[hb] = true;
-  }
-  CH_CUDA(cudaEventRecord(P->ev[0], s));
-  launch_init_scratch(P->aabb.as<int>(), n, counters, s);
+// Launch records of every beam (39 tensor maps over its TERMA volume, tap
+// ranges, beam frustum planes) pointing into scratch S.
+ch_status make_records(const BatchPlan& B, const Scratch& S, std::vector<ConeBeam>& cb, std::vector<RangeBeam>& rb) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled is not available from the driver");
+  const int n = (int)B.jobs.size();
+  cb.assign(n, ConeBeam{});
+  rb.assign(n, RangeBeam{});
+  int unit_begin = 0;
   for (int i = 0; i < n; ++i) {
-    BeamJob& J = jobs[i];
+    const BeamJob& J = B.jobs[i];
+    ConeBeam& C = cb[i];
+    std::memset(&C, 0, sizeof(C));
+    ch_status est = encode_windows(enc, C, S.T + J.t_off, J.g);
+    if (est != CH_OK) return est;
+    C.dose = J.dose;
+    C.ranges = S.ranges + J.r_off;
+    C.cranges = S.cranges + J.r_off;
+    for (int k = 0; k < 3; ++k) {
+      C.n[k] = J.g.n[k];
+      C.ntile[k] = J.ntile[k];
+    }
+    C.n_tiles = J.n_tiles;
+    C.unit_begin = unit_begin;
+    C.n_units = J.n_units;
+    unit_begin += J.n_units;
+    RangeBeam& R = rb[i];
+    std::memset(&R, 0, sizeof(R));
+    for (int k = 0; k < 3; ++k) {
+      R.n[k] = J.g.n[k];
+      R.ntile[k] = J.ntile[k];
+      R.origin[k] = J.g.origin[k];
+      R.spacing[k] = J.g.spacing[k];
+    }
+    R.n_tiles = J.n_tiles;
+    make_planes(J.beam, J.grid, J.b, R);
+    R.aabb = S.aabb + 8 * i;
+    R.ranges = S.ranges + J.r_off;
+    R.cranges = S.cranges + J.r_off;
+  }
+  return CH_OK;
+}
+
+// The device work of a batch (records already on the device): reset,
+// prologues, dose zeroing, tap ranges, one persistent gather.  Only kernel
+// launches and memsets, so it can be captured into a CUDA graph.  ev (4
+// events, or NULL) marks the stage boundaries.
+ch_status enqueue_batch(ch_plan* P, const BatchPlan& B, const Scratch& S, const ch_intermediates* inter,
+                        const cudaEvent_t* ev, cudaStream_t s) {
+  const int n = (int)B.jobs.size();
+  int* flags = S.counters + 1;
+  unsigned long long* updates = reinterpret_cast<unsigned long long*>(S.counters + 2);
+  if (ev) CH_CUDA(cudaEventRecord(ev[0], s));
+  launch_init_scratch(S.aabb, n, S.counters, s);
+  for (int i = 0; i < n; ++i) {
+    const BeamJob& J = B.jobs[i];
     Inter in{};
     int all = 0;
     if (inter) {
@@ -672,39 +746,77 @@ ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, 
       all = (in.d_eff || in.oad || in.fluence || in.f_soften || in.f_horn) ? 1 : 0;
     }
     // the voxel list is reused beam after beam (stream order)
-    launch_prologue(J.rho, J.g, J.b, J.s, P->T.as<float>() + J.t_off, in, all, P->aabb.as<int>() + 8 * i,
-                    P->list_v.as<int>(), P->n_sm, flags, s);
+    launch_prologue(J.rho, J.g, J.b, J.s, S.T + J.t_off, in, all, S.aabb + 8 * i, S.list_v, P->n_sm, flags, s,
+                    P->tuning.terma_ctas_per_sm);
     CH_CUDA(cudaGetLastError());
   }
-  CH_CUDA(cudaEventRecord(P->ev[1], s));
+  if (ev) CH_CUDA(cudaEventRecord(ev[1], s));
   for (int i = 0; i < n; ++i)
-    CH_CUDA(cudaMemsetAsync(jobs[i].dose, 0, (size_t)jobs[i].g.n[0] * jobs[i].g.n[1] * jobs[i].g.n[2] * 4, s));
-  const ConeDirs D = cone_dirs(P);
+    CH_CUDA(cudaMemsetAsync(B.jobs[i].dose, 0, (size_t)B.jobs[i].g.n[0] * B.jobs[i].g.n[1] * B.jobs[i].g.n[2] * 4,
+                            s));
+  const ConeDirs D = cone_dirs(P->st, P->tuning);
+  launch_range(S.range_beams, n, B.max_tiles, D, s);
+  CH_CUDA(cudaGetLastError());
+  if (ev) CH_CUDA(cudaEventRecord(ev[2], s));
+  launch_gather(S.cone_beams, n, D, B.total_units, P->n_sm, S.counters, updates, flags, s);
+  CH_CUDA(cudaGetLastError());
+  if (ev) CH_CUDA(cudaEventRecord(ev[3], s));
+  return CH_OK;
+}
+
+ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, const int* swap_xy,
+              const ch_beam* beams, const ch_settings* settings, float* const* dose, const ch_intermediates* inter,
+              bool scatter, cudaStream_t s) {
+  BatchPlan B;
+  ch_status st = plan_batch(P, n, grids, rho, swap_xy, beams, settings, dose, s, B);
+  if (st != CH_OK) return st;
+  const ScratchNeed need = scratch_need(n, grids, B.U);
+  CH_CUDA(P->T.ensure(need.bytes[0]));
+  CH_CUDA(P->aabb.ensure(need.bytes[1]));
+  CH_CUDA(P->counters.ensure(need.bytes[2]));
+  CH_CUDA(P->ranges.ensure(need.bytes[3]));
+  CH_CUDA(P->cranges.ensure(need.bytes[4]));
+  CH_CUDA(P->cone_beams.ensure(need.bytes[5]));
+  CH_CUDA(P->range_beams.ensure(need.bytes[6]));
+  CH_CUDA(P->list_v.ensure(need.bytes[7]));
+  const Scratch S{P->T.as<float>(),          P->aabb.as<int>(),           P->counters.as<int>(),
+                  P->ranges.as<uint32_t>(),  P->cranges.as<uint32_t>(),   P->cone_beams.as<ConeBeam>(),
+                  P->range_beams.as<RangeBeam>(), P->list_v.as<int>()};
+  for (auto& e : P->ev)
+    if (!e) CH_CUDA(cudaEventCreate(&e));
+  P->stats = ch_stats{};
+  P->stats.n_unique_dirs = B.U;
+  P->stats_pending = true;
+  P->last_stream = s;
   if (scatter) {
+    // plain path: prologues, then one per-voxel scatter launch per beam
+    int* flags = S.counters + 1;
+    CH_CUDA(cudaEventRecord(P->ev[0], s));
+    launch_init_scratch(S.aabb, n, S.counters, s);
     for (int i = 0; i < n; ++i) {
-      launch_scatter(P->T.as<float>() + jobs[i].t_off, jobs[i].g.n, jobs[i].g.zp, U, D.tap_base, D.tap_len, D.offs,
-                     D.taps, jobs[i].dose, s);
+      const BeamJob& J = B.jobs[i];
+      launch_prologue(J.rho, J.g, J.b, J.s, S.T + J.t_off, Inter{}, 0, S.aabb + 8 * i, S.list_v, P->n_sm, flags, s,
+                      P->tuning.terma_ctas_per_sm);
+      CH_CUDA(cudaGetLastError());
+    }
+    CH_CUDA(cudaEventRecord(P->ev[1], s));
+    const ConeDirs D = cone_dirs(P->st, P->tuning);
+    for (int i = 0; i < n; ++i) {
+      const BeamJob& J = B.jobs[i];
+      CH_CUDA(cudaMemsetAsync(J.dose, 0, (size_t)J.g.n[0] * J.g.n[1] * J.g.n[2] * 4, s));
+      launch_scatter(S.T + J.t_off, J.g.n, J.g.zp, B.U, D.tap_base, D.tap_len, D.offs, D.taps, J.dose, s);
       CH_CUDA(cudaGetLastError());
     }
     CH_CUDA(cudaEventRecord(P->ev[2], s));
     CH_CUDA(cudaEventRecord(P->ev[3], s));
-    P->stats = ch_stats{};
-    P->stats.n_unique_dirs = U;
-    P->stats_pending = true;
-    P->last_stream = s;
     return CH_OK;
   }
-  launch_range(P->range_beams.as<RangeBeam>(), n, max_tiles, D, s);
-  CH_CUDA(cudaGetLastError());
-  CH_CUDA(cudaEventRecord(P->ev[2], s));
-  launch_gather(P->cone_beams.as<ConeBeam>(), n, D, total_units, P->n_sm, counters, updates, flags, s);
-  CH_CUDA(cudaGetLastError());
-  CH_CUDA(cudaEventRecord(P->ev[3], s));
-  P->stats = ch_stats{};
-  P->stats.n_unique_dirs = U;
-  P->stats.n_units = total_units;
-  P->stats_pending = true;
-  P->last_stream = s;
+  std::vector<ConeBeam> cb;
+  std::vector<RangeBeam> rb;
+  if ((st = make_records(B, S, cb, rb)) != CH_OK) return st;
+  if ((st = stage_records(P, cb.data(), rb.data(), n, s)) != CH_OK) return st;
+  if ((st = enqueue_batch(P, B, S, inter, P->ev, s)) != CH_OK) return st;
+  P->stats.n_units = B.total_units;
   return CH_OK;
 }
 
@@ -777,6 +889,7 @@ void ch_plan_destroy(ch_plan* plan) {
 
 ch_status ch_plan_set_kernel(ch_plan* P, const ch_kernel* k) {
   if (!P || !k || !k->cum || !k->theta || !k->phi) return fail(CH_ERR_INVALID_ARG, "kernel tables missing");
+  if (P->live_batches > 0) return fail(CH_ERR_INVALID_ARG, "kernel tables cannot change while captured batches exist");
   if (k->n_phi <= 0 || k->n_r < 2 || k->n_theta <= 0 || k->n_phi > 1024 || k->n_theta > 1024)
     return fail(CH_ERR_INVALID_ARG, "kernel table sizes out of range");
   if (k->n_r < 5996) return fail(CH_ERR_INVALID_ARG, "kernel table needs 5996 radial samples (0.05..60 cm)");
@@ -792,6 +905,7 @@ ch_status ch_plan_set_kernel(ch_plan* P, const ch_kernel* k) {
   P->n_theta = k->n_theta;
   P->have_kernel = true;
   P->st.valid = false;
+  P->st_adj.valid = false;
   return CH_OK;
 }
 
@@ -850,7 +964,7 @@ ch_status ch_dose_static(ch_plan* P, const ch_grid* grid, const float* rho, int 
   const int ntile[3] = {(g.n[0] + TX - 1) / TX, (g.n[1] + TY - 1) / TY, (g.n[2] + TZ - 1) / TZ};
   const int n_tiles = ntile[0] * ntile[1] * ntile[2];
   const int U = S.n_dirs;
-  const int n_units = n_tiles * ((U + DIR_GROUP - 1) / DIR_GROUP);
+  const int n_units = n_tiles * ((U + P->tuning.dir_group - 1) / P->tuning.dir_group);
   size_t off = 0;
   const size_t o_T = off;
   off = align_up(off + (size_t)g.n[0] * g.n[1] * g.zp * sizeof(float), 256);
@@ -883,7 +997,8 @@ ch_status ch_dose_static(ch_plan* P, const ch_grid* grid, const float* rho, int 
   // aabb and the list count must start from their reset values; TERMA is
   // rewritten in full by the prologue and the range tables by range_kernel
   launch_init_scratch(aabb, 1, counters, s);
-  launch_prologue(rho, g, b, sd, T, Inter{}, 0, aabb, reinterpret_cast<int*>(base + o_lv), P->n_sm, flags, s);
+  launch_prologue(rho, g, b, sd, T, Inter{}, 0, aabb, reinterpret_cast<int*>(base + o_lv), P->n_sm, flags, s,
+                  P->tuning.terma_ctas_per_sm);
   CH_CUDA(cudaGetLastError());
   CH_CUDA(cudaMemsetAsync(dose, 0, N * sizeof(float), s));
 
@@ -928,12 +1043,279 @@ ch_status ch_dose_static(ch_plan* P, const ch_grid* grid, const float* rho, int 
   R.cranges = reinterpret_cast<uint32_t*>(base + o_cr);
   CH_CUDA(cudaMemcpyAsync(base + o_cb, &C, sizeof(C), cudaMemcpyHostToDevice, s));
   CH_CUDA(cudaMemcpyAsync(base + o_rb, &R, sizeof(R), cudaMemcpyHostToDevice, s));
-  const ConeDirs D = cone_dirs(P);
+  const ConeDirs D = cone_dirs(P->st, P->tuning);
   launch_range(reinterpret_cast<const RangeBeam*>(base + o_rb), 1, n_tiles, D, s);
   CH_CUDA(cudaGetLastError());
   launch_gather(reinterpret_cast<const ConeBeam*>(base + o_cb), 1, D, n_units, P->n_sm, counters, updates, flags, s);
   CH_CUDA(cudaGetLastError());
   return CH_OK;
+}
+
+// ------------------------------------------------- cone operator, adjoint --
+namespace {
+
+GridDev grid_dev(const ch_grid& grid, int swap_xy) {
+  GridDev g{};
+  for (int k = 0; k < 3; ++k) {
+    g.n[k] = grid.n[k];
+    g.origin[k] = grid.origin[k];
+    g.spacing[k] = grid.spacing[k];
+  }
+  g.zp = round_up(grid.n[2], 4);
+  g.swap_xy = swap_xy;
+  return g;
+}
+
+// Apply the cone stage to `in_dense` ([x][y][z], copied into the padded
+// operator buffer): out = C in (forward stencils) or C^T in (mirrored).
+// Tap ranges are cut against the nonzero box of the input (box, computed
+// here into box[0..5]) and, if out_box is set, only output tiles meeting
+// out_box are computed.  No frustum: the input is arbitrary.  `box` and the
+// counters must have been reset (launch_init_scratch) by the caller.
+ch_status cone_operator(ch_plan* P, const ch_grid& grid, const float* in_dense, float* out, bool transpose,
+                        int* box, const int* out_box, cudaStream_t s) {
+  const GridDev g = grid_dev(grid, 0);
+  const StencilSet& S = transpose ? P->st_adj : P->st;
+  const int U = S.n_dirs;
+  const ScratchNeed need = scratch_need(1, &grid, U);
+  CH_CUDA(P->ranges.ensure(need.bytes[3]));
+  CH_CUDA(P->cranges.ensure(need.bytes[4]));
+  CH_CUDA(P->cone_beams.ensure(need.bytes[5]));
+  CH_CUDA(P->range_beams.ensure(need.bytes[6]));
+  CH_CUDA(P->adj_in.ensure((size_t)g.n[0] * g.n[1] * g.zp * sizeof(float)));
+  int* counters = P->counters.as<int>();
+  int* flags = counters + 1;
+  unsigned long long* updates = reinterpret_cast<unsigned long long*>(counters + 2);
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled is not available from the driver");
+  const int ntile[3] = {(g.n[0] + TX - 1) / TX, (g.n[1] + TY - 1) / TY, (g.n[2] + TZ - 1) / TZ};
+  const int n_tiles = ntile[0] * ntile[1] * ntile[2];
+  const int n_units = n_tiles * ((U + P->tuning.dir_group - 1) / P->tuning.dir_group);
+  ConeBeam C;
+  std::memset(&C, 0, sizeof(C));
+  ch_status st = encode_windows(enc, C, P->adj_in.as<float>(), g);
+  if (st != CH_OK) return st;
+  C.dose = out;
+  C.ranges = P->ranges.as<uint32_t>();
+  C.cranges = P->cranges.as<uint32_t>();
+  for (int k = 0; k < 3; ++k) {
+    C.n[k] = g.n[k];
+    C.ntile[k] = ntile[k];
+  }
+  C.n_tiles = n_tiles;
+  C.unit_begin = 0;
+  C.n_units = n_units;
+  RangeBeam R;
+  std::memset(&R, 0, sizeof(R));
+  for (int k = 0; k < 3; ++k) {
+    R.n[k] = g.n[k];
+    R.ntile[k] = ntile[k];
+    R.origin[k] = g.origin[k];
+    R.spacing[k] = g.spacing[k];
+  }
+  R.n_tiles = n_tiles;
+  R.n_planes = 0;
+  R.aabb = box;
+  R.out_aabb = out_box;
+  R.ranges = P->ranges.as<uint32_t>();
+  R.cranges = P->cranges.as<uint32_t>();
+  if ((st = stage_records(P, &C, &R, 1, s)) != CH_OK) return st;
+  // input into the padded layout the window tensor maps read
+  CH_CUDA(cudaMemcpy2DAsync(P->adj_in.p, (size_t)g.zp * sizeof(float), in_dense, (size_t)g.n[2] * sizeof(float),
+                            (size_t)g.n[2] * sizeof(float), (size_t)g.n[0] * g.n[1], cudaMemcpyDeviceToDevice, s));
+  launch_nonzero_box(in_dense, g.n[0], g.n[1], g.n[2], box, s);
+  CH_CUDA(cudaGetLastError());
+  CH_CUDA(cudaMemsetAsync(out, 0, (size_t)g.n[0] * g.n[1] * g.n[2] * sizeof(float), s));
+  const ConeDirs D = cone_dirs(S, P->tuning);
+  launch_range(P->range_beams.as<RangeBeam>(), 1, n_tiles, D, s);
+  CH_CUDA(cudaGetLastError());
+  launch_gather(P->cone_beams.as<ConeBeam>(), 1, D, n_units, P->n_sm, counters, updates, flags, s);
+  CH_CUDA(cudaGetLastError());
+  return CH_OK;
+}
+
+ch_status check_beamlets(const ch_beamlets* bl) {
+  if (!bl) return fail(CH_ERR_INVALID_ARG, "beamlet grid is NULL");
+  if (bl->rows < 1 || bl->cols < 1 || (long long)bl->rows * bl->cols > CH_MAX_BEAMLETS)
+    return fail(CH_ERR_INVALID_ARG, "beamlet grid must hold 1.." + std::to_string(CH_MAX_BEAMLETS) + " beamlets");
+  if (bl->cell_rows < 1 || bl->cell_cols < 1 || bl->r0 < 0 || bl->c0 < 0 ||
+      (long long)bl->rows * bl->cell_rows > 65536 || (long long)bl->cols * bl->cell_cols > 65536)
+    return fail(CH_ERR_INVALID_ARG, "beamlet cells out of range");
+  return CH_OK;
+}
+
+}  // namespace
+
+ch_status ch_cone(ch_plan* P, const ch_grid* grid, const float* in, float* out, int transpose, void* stream) {
+  if (!P) return fail(CH_ERR_INVALID_ARG, "plan is NULL");
+  if (!P->have_kernel) return fail(CH_ERR_NO_KERNEL, "ch_plan_set_kernel has not been called");
+  ch_status st = check_grid(grid);
+  if (st != CH_OK) return st;
+  if (!in || !out) return fail(CH_ERR_INVALID_ARG, "input or output pointer is NULL");
+  if (in == out) return fail(CH_ERR_INVALID_ARG, "input and output must be different buffers");
+  cudaStream_t s = (cudaStream_t)stream;
+  CH_CUDA(cudaSetDevice(P->device));
+  if ((st = ensure_stencils(P, grid->spacing, grid->n, s)) != CH_OK) return st;
+  CH_CUDA(P->aabb.ensure(8 * sizeof(int)));
+  CH_CUDA(P->counters.ensure(8 * sizeof(int)));
+  launch_init_scratch(P->aabb.as<int>(), 1, P->counters.as<int>(), s);
+  st = cone_operator(P, *grid, in, out, transpose != 0, P->aabb.as<int>(), nullptr, s);
+  if (st != CH_OK) return st;
+  P->stats_pending = false;
+  return CH_OK;
+}
+
+ch_status ch_block_from_beamlets(const ch_beamlets* bl, const float* weights, float* crop, void* stream) {
+  ch_status st = check_beamlets(bl);
+  if (st != CH_OK) return st;
+  if (!weights || !crop) return fail(CH_ERR_INVALID_ARG, "weights or crop pointer is NULL");
+  BeamletDev d{bl->rows, bl->cols, bl->cell_rows, bl->cell_cols, bl->r0, bl->c0};
+  launch_beamlet_fill(weights, d, crop, (cudaStream_t)stream);
+  CH_CUDA(cudaGetLastError());
+  return CH_OK;
+}
+
+ch_status ch_dose_adjoint(ch_plan* P, const ch_grid* grid, const float* rho, int swap_xy, const ch_beam* beam,
+                          const ch_beamlets* bl, const ch_settings* settings, const float* grad_dose,
+                          float* grad_weights, float* grad_terma, void* stream) {
+  if (!P) return fail(CH_ERR_INVALID_ARG, "plan is NULL");
+  if (!P->have_kernel) return fail(CH_ERR_NO_KERNEL, "ch_plan_set_kernel has not been called");
+  ch_status st;
+  if ((st = check_grid(grid)) != CH_OK) return st;
+  if ((st = check_beam(beam)) != CH_OK) return st;
+  if ((st = check_settings(settings)) != CH_OK) return st;
+  if ((st = check_beamlets(bl)) != CH_OK) return st;
+  if (!rho || !grad_dose || !grad_weights) return fail(CH_ERR_INVALID_ARG, "density or gradient pointer is NULL");
+  if (swap_xy && grid->n[0] != grid->n[1]) return fail(CH_ERR_INVALID_ARG, "swap_xy needs a square x/y grid");
+  if (beam->block_r0 != bl->r0 || beam->block_c0 != bl->c0 || beam->block_rows != bl->rows * bl->cell_rows ||
+      beam->block_cols != bl->cols * bl->cell_cols || beam->block_uniform)
+    return fail(CH_ERR_INVALID_ARG, "the beam's block crop must be the beamlet grid (ch_block_from_beamlets)");
+  cudaStream_t s = (cudaStream_t)stream;
+  CH_CUDA(cudaSetDevice(P->device));
+  if ((st = ensure_stencils(P, grid->spacing, grid->n, s)) != CH_OK) return st;
+  const GridDev g = grid_dev(*grid, swap_xy);
+  const size_t N = (size_t)g.n[0] * g.n[1] * g.n[2];
+  const ScratchNeed need = scratch_need(1, grid, P->st.n_dirs);
+  CH_CUDA(P->T.ensure(need.bytes[0]));
+  CH_CUDA(P->aabb.ensure(16 * sizeof(int)));
+  CH_CUDA(P->counters.ensure(need.bytes[2]));
+  CH_CUDA(P->list_v.ensure(need.bytes[7]));
+  CH_CUDA(P->adj_out.ensure(N * sizeof(float)));
+  CH_CUDA(P->adj_w.ensure((size_t)bl->rows * bl->cols * sizeof(double)));
+  int* box = P->aabb.as<int>();          // [0..7] TERMA box + list count, [8..15] input box
+  int* counters = P->counters.as<int>();
+  int* flags = counters + 1;
+  const BeamDev b = make_beam(*beam, *grid);
+  const SettingsDev sd = make_settings(*settings);
+  launch_init_scratch(box, 2, counters, s);
+  // forward prologue: TERMA, its box and the list of voxels the beam reaches
+  launch_prologue(rho, g, b, sd, P->T.as<float>(), Inter{}, 0, box, P->list_v.as<int>(), P->n_sm, flags, s, P->tuning.terma_ctas_per_sm);
+  CH_CUDA(cudaGetLastError());
+  // transposed cone: dL/dT = C^T dL/dD, only where TERMA is nonzero
+  float* tbar = grad_terma ? grad_terma : P->adj_out.as<float>();
+  if ((st = cone_operator(P, *grid, grad_dose, tbar, true, box + 8, box, s)) != CH_OK) return st;
+  // transposed blocking and fluence: dL/dw
+  CH_CUDA(cudaMemsetAsync(P->adj_w.p, 0, (size_t)bl->rows * bl->cols * sizeof(double), s));
+  const BeamletDev d{bl->rows, bl->cols, bl->cell_rows, bl->cell_cols, bl->r0, bl->c0};
+  CH_CUDA(launch_blocked_adjoint(g, b, d, settings->samples, P->T.as<float>(), tbar, box + 6, P->list_v.as<int>(),
+                                 P->adj_w.as<double>(), P->n_sm, flags, s));
+  launch_to_float(P->adj_w.as<double>(), grad_weights, bl->rows * bl->cols, s);
+  CH_CUDA(cudaGetLastError());
+  P->stats_pending = false;
+  P->last_stream = s;
+  return CH_OK;
+}
+
+// ------------------------------------------------------- captured batch --
+struct ch_batch {
+  ch_plan* P = nullptr;
+  int n = 0;
+  int total_units = 0;
+  DevBuf T, aabb, counters, ranges, cranges, cone_beams, range_beams, list_v;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ~ch_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (DevBuf* b : {&T, &aabb, &counters, &ranges, &cranges, &cone_beams, &range_beams, &list_v}) b->release();
+  }
+};
+
+ch_status ch_batch_create(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, const int* swap_xy,
+                          const ch_beam* beams, const ch_settings* settings, float* const* dose, void* stream,
+                          ch_batch** out) {
+  if (!out) return fail(CH_ERR_INVALID_ARG, "batch out-pointer is NULL");
+  *out = nullptr;
+  cudaStream_t s = (cudaStream_t)stream;
+  BatchPlan B;
+  ch_status st = plan_batch(P, n, grids, rho, swap_xy, beams, settings, dose, s, B);
+  if (st != CH_OK) return st;
+  std::unique_ptr<ch_batch> bt(new ch_batch());
+  bt->P = P;
+  bt->n = n;
+  bt->total_units = B.total_units;
+  const ScratchNeed need = scratch_need(n, grids, B.U);
+  DevBuf* bufs[8] = {&bt->T, &bt->aabb, &bt->counters, &bt->ranges, &bt->cranges, &bt->cone_beams,
+                     &bt->range_beams, &bt->list_v};
+  for (int k = 0; k < 8; ++k) CH_CUDA(bufs[k]->ensure(need.bytes[k]));
+  const Scratch S{bt->T.as<float>(),          bt->aabb.as<int>(),          bt->counters.as<int>(),
+                  bt->ranges.as<uint32_t>(),  bt->cranges.as<uint32_t>(),  bt->cone_beams.as<ConeBeam>(),
+                  bt->range_beams.as<RangeBeam>(), bt->list_v.as<int>()};
+  std::vector<ConeBeam> cb;
+  std::vector<RangeBeam> rb;
+  if ((st = make_records(B, S, cb, rb)) != CH_OK) return st;
+  // the records are fixed for the batch's life: upload them once, outside the graph
+  CH_CUDA(cudaStreamSynchronize(s));
+  CH_CUDA(cudaMemcpy(bt->cone_beams.p, cb.data(), n * sizeof(ConeBeam), cudaMemcpyHostToDevice));
+  CH_CUDA(cudaMemcpy(bt->range_beams.p, rb.data(), n * sizeof(RangeBeam), cudaMemcpyHostToDevice));
+  // capture the device work on a private stream
+  cudaStream_t cs;
+  CH_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(cs);
+    return fail(CH_ERR_DEVICE, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(e));
+  }
+  st = enqueue_batch(P, B, S, nullptr, nullptr, cs);
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(cs, &g);
+  cudaStreamDestroy(cs);
+  if (st != CH_OK) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  if (e != cudaSuccess) return fail(CH_ERR_DEVICE, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+  bt->graph = g;
+  CH_CUDA(cudaGraphInstantiate(&bt->exec, g, 0));
+  P->live_batches += 1;
+  *out = bt.release();
+  return CH_OK;
+}
+
+ch_status ch_batch_launch(ch_batch* bt, void* stream) {
+  if (!bt || !bt->exec) return fail(CH_ERR_INVALID_ARG, "batch is NULL");
+  CH_CUDA(cudaSetDevice(bt->P->device));
+  CH_CUDA(cudaGraphLaunch(bt->exec, (cudaStream_t)stream));
+  return CH_OK;
+}
+
+ch_status ch_batch_sync(ch_batch* bt, void* stream) {
+  if (!bt) return fail(CH_ERR_INVALID_ARG, "batch is NULL");
+  CH_CUDA(cudaSetDevice(bt->P->device));
+  CH_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  int c[2];
+  CH_CUDA(cudaMemcpy(c, bt->counters.p, sizeof(c), cudaMemcpyDeviceToHost));
+  if (c[1] & FLAG_TIMEOUT) return fail(CH_ERR_TIMEOUT, "a bounded device wait expired in the cone stage");
+  if (c[1] & FLAG_PARALLEL_RAY) return fail(CH_ERR_PARALLEL_RAY, "no intersection or line is within plane");
+  return CH_OK;
+}
+
+void ch_batch_destroy(ch_batch* bt) {
+  if (!bt) return;
+  cudaSetDevice(bt->P->device);
+  cudaDeviceSynchronize();      // no replay may still be reading the batch's buffers
+  bt->P->live_batches -= 1;
+  delete bt;
 }
 
 ch_status ch_block_from_mlc(const ch_mlc* m, float* out, int rows, int cols, int r0, int c0, void* stream) {
@@ -989,6 +1371,24 @@ ch_status ch_cone_directions(ch_plan* P, float* out, void* stream) {
   return CH_OK;
 }
 
+ch_status ch_plan_set_tuning(ch_plan* P, const ch_tuning* t) {
+  if (!P || !t) return fail(CH_ERR_INVALID_ARG, "plan or tuning is NULL");
+  // (captured batches keep the schedule they were captured with)
+  if (t->dir_group < 1 || t->dir_group > MAX_DIR_GROUP)
+    return fail(CH_ERR_INVALID_ARG, "dir_group out of range (1.." + std::to_string(MAX_DIR_GROUP) + ")");
+  if (t->unit_order != 0 && t->unit_order != 1) return fail(CH_ERR_INVALID_ARG, "unit_order must be 0 or 1");
+  if (t->terma_ctas_per_sm < 1 || t->terma_ctas_per_sm > 32)
+    return fail(CH_ERR_INVALID_ARG, "terma_ctas_per_sm out of range (1..32)");
+  P->tuning = *t;
+  return CH_OK;
+}
+
+ch_status ch_plan_get_tuning(ch_plan* P, ch_tuning* t) {
+  if (!P || !t) return fail(CH_ERR_INVALID_ARG, "plan or tuning is NULL");
+  *t = P->tuning;
+  return CH_OK;
+}
+
 ch_status ch_plan_prepare(ch_plan* P, const ch_grid* grid, void* stream) {
   if (!P) return fail(CH_ERR_INVALID_ARG, "plan is NULL");
   if (!P->have_kernel) return fail(CH_ERR_NO_KERNEL, "ch_plan_set_kernel has not been called");
@@ -1001,11 +1401,11 @@ ch_status ch_plan_prepare(ch_plan* P, const ch_grid* grid, void* stream) {
 ch_status ch_plan_memory(ch_plan* P, size_t* tables, size_t* scratch) {
   if (!P) return fail(CH_ERR_INVALID_ARG, "plan is NULL");
   size_t b = P->K.bytes + P->theta.bytes + P->phi.bytes;
-  const StencilSet& S = P->st;
-  for (const DevBuf* d : {&S.tap_base, &S.tap_len, &S.taps, &S.offs, &S.tvals, &S.chunk_base, &S.n_chunks,
-                          &S.chunk_start, &S.chunk_rec, &S.dirs, &S.raw_dirs})
-    b += d->bytes;
-  size_t a = 0;
+  for (const StencilSet* S : {&P->st, &P->st_adj})
+    for (const DevBuf* d : {&S->tap_base, &S->tap_len, &S->taps, &S->offs, &S->tvals, &S->chunk_base, &S->n_chunks,
+                            &S->chunk_start, &S->chunk_rec, &S->dirs, &S->raw_dirs})
+      b += d->bytes;
+  size_t a = P->adj_in.bytes + P->adj_out.bytes + P->adj_w.bytes;
   for (int k = 0; k < 8; ++k) a += scratch_bufs(P, k)->bytes;
   if (tables) *tables = b;
   if (scratch) *scratch = a;
@@ -1036,7 +1436,7 @@ ch_status ch_plan_trim(ch_plan* P) {
   CH_CUDA(cudaSetDevice(P->device));
   // cudaFree waits for the device, so no call of this plan is still reading the arena
   for (DevBuf* b : {&P->T, &P->aabb, &P->counters, &P->ranges, &P->cranges, &P->cone_beams, &P->range_beams,
-                    &P->list_v})
+                    &P->list_v, &P->adj_in, &P->adj_out, &P->adj_w})
     b->release();
   P->stats_pending = false;
   return CH_OK;

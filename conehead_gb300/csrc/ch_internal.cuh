@@ -44,7 +44,8 @@ constexpr int MAX_CHUNK_TAPS = 64;    // taps per chunk (their table is staged w
 constexpr int N_SLOTS = 2;
 constexpr int CONE_CONSUMER_WARPS = TY / 2;
 constexpr int CONE_THREADS = (CONE_CONSUMER_WARPS + 1) * 32;
-constexpr int DIR_GROUP = 16;         // unique directions per work unit
+constexpr int DIR_GROUP = 16;         // unique directions per work unit (default; ch_tuning.dir_group)
+constexpr int MAX_DIR_GROUP = 32;     // the producer fetches one direction's ranges per lane
 
 // Bounded device-side waits (iterations of try_wait / spin).
 constexpr long long WAIT_LIMIT = 1ll << 26;
@@ -162,6 +163,8 @@ struct ConeDirs {
   const int4* chunk_rec;   // 2 per chunk: {first, last, variant, span_x | span_y << 16},
                            //              {max O_x, max O_y, max O_z, 0} over the chunk
   const float* dirs;       // unit direction (x, y, z)
+  int group;               // unique directions per work unit (1..MAX_DIR_GROUP)
+  int order;               // units: 0 = tile outer, group inner; 1 = group outer, tile inner
 };
 
 struct RangeBeam {
@@ -170,9 +173,16 @@ struct RangeBeam {
   int n_planes;
   float pa[4][3];
   float pk0[4];
-  const int* aabb;
+  const int* aabb;          // box of the nonzero input (lo/hi pairs per axis)
+  const int* out_aabb;      // if set, output tiles outside this box get no taps
   uint32_t* ranges;        // [n_tiles][n_dirs]: first | last tap << 16, or RANGE_EMPTY
   uint32_t* cranges;       // [n_tiles][n_dirs]: first | last chunk << 16 (direction-local)
+};
+
+// Regular beamlet grid on the block map: beamlet (i, j) covers map rows
+// r0 + i*cell_rows .. + cell_rows and columns c0 + j*cell_cols .. + cell_cols.
+struct BeamletDev {
+  int rows, cols, cell_rows, cell_cols, r0, c0;
 };
 
 struct Inter {
@@ -184,7 +194,7 @@ struct Inter {
 void upload_unit_partials();
 void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const SettingsDev& s, float* T,
                      const Inter& inter, int all_voxels, int* aabb, int* list_v, int n_sm, int* flags,
-                     cudaStream_t st);
+                     cudaStream_t st, int ctas_per_sm = 8);
 void launch_stencil(const float* theta, int n_theta, const float* phi, int n_phi, const double* K, int n_r,
                     const float* spacing, const int* cap, int max_len, short4* off, float* t, float* dk,
                     int* len, float* dirs, cudaStream_t st);
@@ -199,5 +209,11 @@ void launch_gather(const ConeBeam* beams_dev, int n_beams, const ConeDirs& D, in
                    int* unit_counter, unsigned long long* updates, int* flags, cudaStream_t st);
 void launch_init_scratch(int* aabb, int n_beams, int* counters, cudaStream_t st);
 void launch_mlc_raster(const ch_mlc& m, float* out, int rows, int cols, int r0, int c0, cudaStream_t st);
+void launch_nonzero_box(const float* x, int n0, int n1, int n2, int* box, cudaStream_t st);
+void launch_beamlet_fill(const float* w, const BeamletDev& bl, float* crop, cudaStream_t st);
+void launch_to_float(const double* in, float* out, int n, cudaStream_t st);
+cudaError_t launch_blocked_adjoint(const GridDev& g, const BeamDev& b, const BeamletDev& bl, int S, const float* T,
+                                   const float* tbar, const int* list_count, const int* list_v, double* wbar,
+                                   int n_sm, int* flags, cudaStream_t st);
 
 }  // namespace ch

@@ -129,12 +129,18 @@ __global__ void range_kernel(const RangeBeam* __restrict__ rbs, ConeDirs D) {
   const int tile = (int)(id / D.n_dirs), u = (int)(id % D.n_dirs);
   const int lo0 = R.aabb[0], hi0 = R.aabb[1], lo1 = R.aabb[2], hi1 = R.aabb[3], lo2 = R.aabb[4], hi2 = R.aabb[5];
   uint32_t out = RANGE_EMPTY;
-  if (lo0 <= hi0) {
-    const int tx = tile / (R.ntile[1] * R.ntile[2]);
-    const int ty = (tile / R.ntile[2]) % R.ntile[1];
-    const int tz = tile % R.ntile[2];
-    const int vlo[3] = {tx * TX, ty * TY, tz * TZ};
-    const int vhi[3] = {min(vlo[0] + TX, R.n[0]) - 1, min(vlo[1] + TY, R.n[1]) - 1, min(vlo[2] + TZ, R.n[2]) - 1};
+  const int tx = tile / (R.ntile[1] * R.ntile[2]);
+  const int ty = (tile / R.ntile[2]) % R.ntile[1];
+  const int tz = tile % R.ntile[2];
+  const int vlo[3] = {tx * TX, ty * TY, tz * TZ};
+  const int vhi[3] = {min(vlo[0] + TX, R.n[0]) - 1, min(vlo[1] + TY, R.n[1]) - 1, min(vlo[2] + TZ, R.n[2]) - 1};
+  bool wanted = lo0 <= hi0;
+  if (R.out_aabb && wanted) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      wanted = wanted && vhi[k] >= R.out_aabb[2 * k] && vlo[k] <= R.out_aabb[2 * k + 1];
+  }
+  if (wanted) {
     const int blo[3] = {lo0, lo1, lo2}, bhi[3] = {hi0, hi1, hi2};
     const int base = D.tap_base[u], L = D.tap_len[u];
     const short4* O = D.offs + base;
@@ -195,7 +201,7 @@ __device__ __forceinline__ void producer(const ConeBeam* __restrict__ beams, int
                                          int* flags, float* win, int4* slot_taps, ChunkDesc* desc,
                                          uint64_t* full, uint64_t* empty) {
   const int lane = threadIdx.x & 31;
-  const int n_groups = (D.n_dirs + DIR_GROUP - 1) / DIR_GROUP;
+  const int n_groups = (D.n_dirs + D.group - 1) / D.group;
   int k = 0;
   bool ok = true;
   ChunkDesc pend;
@@ -231,15 +237,16 @@ __device__ __forceinline__ void producer(const ConeBeam* __restrict__ beams, int
     while (bi + 1 < n_beams && beams[bi + 1].unit_begin <= unit) ++bi;
     const ConeBeam& B = beams[bi];
     const int lu = unit - B.unit_begin;
-    const int tile = lu / n_groups, g = lu % n_groups;
+    const int tile = D.order == 0 ? lu / n_groups : lu % B.n_tiles;
+    const int g = D.order == 0 ? lu % n_groups : lu / B.n_tiles;
     const int tx0 = (tile / (B.ntile[1] * B.ntile[2])) * TX;
     const int ty0 = ((tile / B.ntile[2]) % B.ntile[1]) * TY;
     const int tz0 = (tile % B.ntile[2]) * TZ;
-    // lanes 0..15 fetch the ranges of the group's directions in parallel
-    const int u0 = g * DIR_GROUP;
+    // lanes 0..group-1 fetch the ranges of the group's directions in parallel
+    const int u0 = g * D.group;
     uint32_t r = RANGE_EMPTY, cr = 0;
     int cb = 0, tb = 0;
-    if (lane < DIR_GROUP && u0 + lane < D.n_dirs) {
+    if (lane < D.group && u0 + lane < D.n_dirs) {
       const long long ri = (long long)tile * D.n_dirs + u0 + lane;
       r = __ldg(B.ranges + ri);
       if (r != RANGE_EMPTY) {

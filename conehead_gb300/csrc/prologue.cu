@@ -100,8 +100,11 @@ __device__ __forceinline__ bool project_exact(const BeamDev& b, const float* rd,
 // Exact transmission of one sub-sample (reference path end to end).  Kept
 // out of line: it is rare, and inlining it at every sample site would bloat
 // the kernel past the instruction cache.
-__device__ __noinline__ float sample_exact(const BeamDev& b, const GridDev& g, const float* pos, const float* off,
-                              int ix, int iy, int iz, int& bad) {
+// Block cell (floor(100 px), floor(100 pz)) of one sub-sample by the exact
+// reference arithmetic; false (and bad = 1) for a ray parallel to the plane.
+__device__ __forceinline__ bool sample_cell_exact(const BeamDev& b, const GridDev& g, const float* pos,
+                                                  const float* off, int ix, int iy, int iz, int& bad, int& fi,
+                                                  int& fk) {
   const int ii[3] = {ix, iy, iz};
   float ps[3];
 #pragma unroll
@@ -116,9 +119,18 @@ __device__ __noinline__ float sample_exact(const BeamDev& b, const GridDev& g, c
   float px, pz;
   if (!project_exact(b, rd, px, pz)) {
     bad = 1;
-    return 0.0f;
+    return false;
   }
-  return cell_value(b, floor_cell(fmul(px, 100.0f)), floor_cell(fmul(pz, 100.0f)));
+  fi = floor_cell(fmul(px, 100.0f));
+  fk = floor_cell(fmul(pz, 100.0f));
+  return true;
+}
+
+__device__ __noinline__ float sample_exact(const BeamDev& b, const GridDev& g, const float* pos, const float* off,
+                              int ix, int iy, int iz, int& bad) {
+  int fi, fk;
+  if (!sample_cell_exact(b, g, pos, off, ix, iy, iz, bad, fi, fk)) return 0.0f;
+  return cell_value(b, fi, fk);
 }
 
 // ------------------------------------------------------------ blocking --
@@ -435,6 +447,117 @@ __global__ void __launch_bounds__(256) terma_kernel(const float* __restrict__ rh
   }
 }
 
+// ----------------------------------------------------- beamlet adjoint --
+// Beamlet holding block cell (fi, fk) under the lookup rule of cell_value
+// (cell + 1999, index -1 wrapping to the last row/column), or -1.
+__device__ __forceinline__ int beamlet_of(const BeamDev& b, const BeamletDev& bl, int fi, int fk) {
+  const int c0 = fi + 2000, c1 = fk + 2000;
+  if (c0 < 0 || c0 > 3999 || c1 < 0 || c1 > 3999) return -1;
+  int r = c0 - 1, c = c1 - 1;
+  if (r < 0) r += b.full_rows;
+  if (c < 0) c += b.full_cols;
+  r -= bl.r0;
+  c -= bl.c0;
+  if (r < 0 || c < 0 || r >= bl.rows * bl.cell_rows || c >= bl.cols * bl.cell_cols) return -1;
+  return (r / bl.cell_rows) * bl.cols + c / bl.cell_cols;
+}
+
+// Beamlet of sub-sample (ix, iy, iz): the float32 projection decides when
+// every cell within SAMPLE_DELTA of it lies in one beamlet, otherwise the
+// exact float64 mirror finds the reference's cell.  (The forward pass may
+// settle a sample on value alone; the derivative needs the beamlet.)
+__device__ int sample_beamlet(const BeamDev& b, const BeamletDev& bl, const GridDev& g, const float* pos,
+                              const float* off, float rx, float ry, float rz, int ix, int iy, int iz, int& bad) {
+  if (!b.geom_f32) {
+    const float p0 = pos[0] + rx, p1 = pos[1] + ry, p2 = pos[2] + rz;
+    const float np_ = b.vyf[0] * p0 + b.vyf[1] * p1 + b.vyf[2] * p2;
+    const float m0p = b.m0f[0] * p0 + b.m0f[1] * p1 + b.m0f[2] * p2;
+    const float m2p = b.m2f[0] * p0 + b.m2f[1] * p1 + b.m2f[2] * p2;
+    const float ndr = b.a_nS - np_;
+    if (fabsf(ndr) > 0.2f * fabsf(b.a_K)) {
+      const float si = __fdividef(b.a_K, ndr);
+      const float ux = (b.a_c0 + si * (b.a_m0S - m0p)) * 100.0f;
+      const float uz = (b.a_c2 + si * (b.a_m2S - m2p)) * 100.0f;
+      const int i0 = floor_cell(ux - SAMPLE_DELTA), i1 = floor_cell(ux + SAMPLE_DELTA);
+      const int k0 = floor_cell(uz - SAMPLE_DELTA), k1 = floor_cell(uz + SAMPLE_DELTA);
+      const int id = beamlet_of(b, bl, i0, k0);
+      if ((i0 == i1 && k0 == k1) ||
+          (beamlet_of(b, bl, i1, k0) == id && beamlet_of(b, bl, i0, k1) == id && beamlet_of(b, bl, i1, k1) == id))
+        return id;
+    }
+  }
+  int fi, fk;
+  if (!sample_cell_exact(b, g, pos, off, ix, iy, iz, bad, fi, fk)) return -1;
+  return beamlet_of(b, bl, fi, fk);
+}
+
+// dL/dw for blocked(v) = sum_s w[beamlet(s)] / S^3 and T = blocked^2 * H
+// (fluence and TERMA each carry one factor of blocked): over the voxels of
+// the prologue's list with T != 0, g(v) = tbar(v) * 2 T(v) / blocked(v) is
+// spread over the beamlets of its S^3 sub-samples.  Per-CTA float64
+// histograms in shared memory, one global float64 add per touched beamlet.
+__global__ void __launch_bounds__(256) blocked_adjoint_kernel(GridDev g, BeamDev b, BeamletDev bl, int S,
+                                                              const float* __restrict__ T,
+                                                              const float* __restrict__ tbar,
+                                                              const int* __restrict__ list_count,
+                                                              const int* __restrict__ list_v,
+                                                              double* __restrict__ wbar, int* __restrict__ flags) {
+  extern __shared__ double hist[];
+  const int nb = bl.rows * bl.cols;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) hist[i] = 0.0;
+  __syncthreads();
+  const int count = *list_count;
+  int bad = 0;
+  float off[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) off[k] = fdiv(g.spacing[k], (float)S);
+  const double inv = 1.0 / ((double)S * (double)S * (double)S);
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
+    const int v = list_v[e];
+    const int z = v % g.n[2];
+    const int r = v / g.n[2];
+    const int y = r % g.n[1];
+    const int x = r / g.n[1];
+    const float t = T[((size_t)x * g.n[1] + y) * g.zp + z];
+    const float tb = tbar[v];
+    if (t == 0.0f || tb == 0.0f) continue;
+    float pos[3];
+    pos[0] = voxel_centre(g.origin[0], g.spacing[0], x);
+    pos[1] = voxel_centre(g.origin[1], g.spacing[1], y);
+    pos[2] = voxel_centre(g.origin[2], g.spacing[2], z);
+    const double blocked = blocked_fraction(b, g, S, pos, bad);
+    if (!(blocked > 0.0)) continue;
+    const double gv = (double)tb * 2.0 * (double)t / blocked * inv;
+    for (int ix = 0; ix < S; ++ix)
+      for (int iy = 0; iy < S; ++iy)
+        for (int iz = 0; iz < S; ++iz) {
+          const float rx = off[0] * ((float)ix + 0.5f) - g.spacing[0] * 0.5f;
+          const float ry = off[1] * ((float)iy + 0.5f) - g.spacing[1] * 0.5f;
+          const float rz = off[2] * ((float)iz + 0.5f) - g.spacing[2] * 0.5f;
+          const int id = sample_beamlet(b, bl, g, pos, off, rx, ry, rz, ix, iy, iz, bad);
+          if (id >= 0) atomicAdd(hist + id, gv);
+        }
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flags, FLAG_PARALLEL_RAY);
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb; i += blockDim.x)
+    if (hist[i] != 0.0) atomicAdd(wbar + i, hist[i]);
+}
+
+cudaError_t launch_blocked_adjoint(const GridDev& g, const BeamDev& b, const BeamletDev& bl, int S, const float* T,
+                                   const float* tbar, const int* list_count, const int* list_v, double* wbar,
+                                   int n_sm, int* flags, cudaStream_t st) {
+  const size_t smem = (size_t)bl.rows * bl.cols * sizeof(double);
+  if (smem > (48u << 10)) {
+    // per device and cheap: set it on every launch that needs it
+    cudaError_t e = cudaFuncSetAttribute(blocked_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  blocked_adjoint_kernel<<<n_sm * 2, 256, smem, st>>>(g, b, bl, S, T, tbar, list_count, list_v, wbar, flags);
+  return cudaGetLastError();
+}
+
 void upload_unit_partials() {
   double p[28];
   p[0] = 0.0;
@@ -445,14 +568,15 @@ void upload_unit_partials() {
 
 void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const SettingsDev& s, float* T,
                      const Inter& inter, int all_voxels, int* aabb, int* list_v, int n_sm, int* flags,
-                     cudaStream_t st) {
+                     cudaStream_t st, int ctas_per_sm) {
   const long long N = (long long)g.n[0] * g.n[1] * g.n[2];
   const int threads = 256;
   const long long blocks = (N + threads - 1) / threads;
   int* list_count = aabb + 6;
   cull_kernel<<<(unsigned)blocks, threads, 0, st>>>(g, b, T, inter, all_voxels, list_count, list_v);
   const long long want = (N + threads - 1) / threads;
-  const int grid = (int)(want < (long long)n_sm * 8 ? want : (long long)n_sm * 8);
+  const long long cap = (long long)n_sm * ctas_per_sm;
+  const int grid = (int)(want < cap ? want : cap);
   terma_kernel<<<grid > 0 ? grid : 1, threads, 0, st>>>(rho, g, b, s, T, inter, all_voxels, list_count, list_v,
                                                         aabb, flags);
 }

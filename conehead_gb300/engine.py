@@ -204,6 +204,25 @@ class DoseEngine:
     def sync(self):
         N.check(self.L.ch_plan_sync(self.plan, self.stream()), "ch_plan_sync")
 
+    # ---------------------------------------------------------- schedule --
+    def set_tuning(self, dir_group=16, unit_order=0, terma_ctas_per_sm=8):
+        t = N.Tuning(int(dir_group), int(unit_order), int(terma_ctas_per_sm))
+        N.check(self.L.ch_plan_set_tuning(self.plan, ctypes.byref(t)), "ch_plan_set_tuning")
+
+    def get_tuning(self):
+        t = N.Tuning()
+        N.check(self.L.ch_plan_get_tuning(self.plan, ctypes.byref(t)), "ch_plan_get_tuning")
+        return {k: getattr(t, k) for k, _ in N.Tuning._fields_}
+
+    def prepare(self, size, spacing):
+        """Build the stencils for grids up to ``size`` at ``spacing`` now."""
+        g = N.grid_struct(size, (0.0, 0.0, 0.0), spacing)
+        N.check(self.L.ch_plan_prepare(self.plan, ctypes.byref(g), self.stream()), "ch_plan_prepare")
+
+    def capture(self, jobs):
+        """A CapturedBatch of these jobs (one CUDA graph, replayed by launch())."""
+        return CapturedBatch(self, jobs)
+
     def stats(self):
         s = N.Stats()
         N.check(self.L.ch_plan_stats(self.plan, ctypes.byref(s)), "ch_plan_stats")
@@ -217,6 +236,48 @@ class DoseEngine:
         N.check(self.L.ch_cone_directions(self.plan, out.data_ptr(), self.stream()), "ch_cone_directions")
         self.sync()
         return out.cpu().numpy()
+
+
+class CapturedBatch:
+    """ch_batch: the jobs' device work captured once into a CUDA graph.
+
+    ``launch()`` recomputes every job's dose from the current contents of its
+    density and block-map tensors; geometry, settings and grids are fixed.
+    The jobs' tensors must stay alive and in place while the batch exists.
+    """
+
+    def __init__(self, engine, jobs):
+        self.eng = engine
+        self.jobs = list(jobs)
+        n = len(self.jobs)
+        grids = (N.Grid * n)(*[j.grid for j in self.jobs])
+        beams = (N.Beam * n)(*[j.beam for j in self.jobs])
+        sets = (N.Settings * n)(*[j.settings for j in self.jobs])
+        rho = (ctypes.c_void_p * n)(*[j.rho.data_ptr() for j in self.jobs])
+        dose = (ctypes.c_void_p * n)(*[j.dose.data_ptr() for j in self.jobs])
+        swap = (ctypes.c_int * n)(*[j.swap_xy for j in self.jobs])
+        h = ctypes.c_void_p()
+        N.check(engine.L.ch_batch_create(engine.plan, n, grids, rho, swap, beams, sets, dose, engine.stream(),
+                                         ctypes.byref(h)), "ch_batch_create")
+        self.handle = h
+
+    def launch(self):
+        N.check(self.eng.L.ch_batch_launch(self.handle, self.eng.stream()), "ch_batch_launch")
+        return [j.dose for j in self.jobs]
+
+    def sync(self):
+        N.check(self.eng.L.ch_batch_sync(self.handle, self.eng.stream()), "ch_batch_sync")
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.eng.L.ch_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def dda_trace(size, spacing, starts, dirs, cap=1024, device=0):

@@ -210,6 +210,48 @@ typedef struct {
 ch_status ch_block_from_mlc(const ch_mlc* mlc, float* out_dev, int rows, int cols, int r0, int c0,
                             void* stream);
 
+/* ---------------------------------------------------------------- adjoint
+ * Beamlet fluence: a rows x cols grid of beamlets on the block map, beamlet
+ * (i, j) covering map rows r0 + i*cell_rows .. r0 + (i+1)*cell_rows - 1 and
+ * columns c0 + j*cell_cols .. (0.1 mm cells; 0.5 cm beamlets are 50 x 50).
+ * Its block crop holds weight w[i][j] in every cell of beamlet (i, j).  None
+ * of this is in the reference; the dose of a beamlet map is exactly the
+ * reference's dose for that block map. */
+#define CH_MAX_BEAMLETS 16384
+typedef struct {
+  int rows, cols;
+  int cell_rows, cell_cols;
+  int r0, c0;
+} ch_beamlets;
+
+/* Fill the block crop ([rows*cell_rows][cols*cell_cols], device) of a
+ * beamlet grid from weights_dev (float32 [rows][cols], device).  Pass it as
+ * ch_beam.block with block_r0 = r0, block_c0 = c0. */
+ch_status ch_block_from_beamlets(const ch_beamlets* beamlets, const float* weights_dev, float* crop_dev,
+                                 void* stream);
+
+/* The cone stage as an operator on any volume (device, float32 [x][y][z]):
+ * out = C in, or out = C^T in with transpose = 1, where C maps TERMA to dose
+ * exactly as ch_dose's cone stage does (conehead/conehead.py:385-488).  The
+ * transpose gathers along the mirrored walks.  in and out must differ. */
+ch_status ch_cone(ch_plan* plan, const ch_grid* grid, const float* in_dev, float* out_dev, int transpose,
+                  void* stream);
+
+/* Gradient of a dose objective with respect to beamlet weights: given
+ * grad_dose = dL/d(dose) (device, [x][y][z]) for the dose ch_dose computes
+ * from this beam (whose block crop is the beamlet grid's), writes
+ * grad_weights = dL/dw (device, float32 [rows][cols]) and, if grad_terma is
+ * not NULL, dL/d(TERMA) ([x][y][z]).  Steps: the forward prologue, the
+ * transposed cone (C^T grad_dose, computed only where TERMA is nonzero), and
+ * the transposed blocking: blocked(v) = sum over the S^3 sub-samples of
+ * w[beamlet] / S^3 and TERMA = blocked^2 * H(v) (fluence and TERMA each carry
+ * one factor), so dL/dw gets 2 TERMA/blocked * dL/dTERMA / S^3 from every
+ * sub-sample in its beamlet.  No counterpart in the reference. */
+ch_status ch_dose_adjoint(ch_plan* plan, const ch_grid* grid, const float* rho_dev, int swap_xy,
+                          const ch_beam* beam, const ch_beamlets* beamlets, const ch_settings* settings,
+                          const float* grad_dose_dev, float* grad_weights_dev, float* grad_terma_dev,
+                          void* stream);
+
 /* Test hook: n_rays DDA traces on the device.  starts int32 [n][3],
  * dirs float32 [n][3] (used as given, no normalisation), grid dims/spacing
  * from `grid`.  Writes voxels int32 [n][cap][3], t float32 [n][cap] and
@@ -221,6 +263,41 @@ ch_status ch_dda_trace(const ch_grid* grid, int n_rays, const int* starts_dev,
 /* Test hook: the cone directions the device computes for (theta_i, phi_j),
  * float32 [n_theta][n_phi][3] into out_dev. */
 ch_status ch_cone_directions(ch_plan* plan, float* out_dev, void* stream);
+
+/* Schedule of the cone and TERMA passes (results do not depend on it, up
+ * to the float order of the dose sums).  dir_group: unique directions per
+ * cone work unit, 1..32 (default 16); unit_order: 0 = a tile's direction
+ * groups are consecutive units (default), 1 = a direction group's tiles are;
+ * terma_ctas_per_sm: CTAs per SM of the TERMA pass, 1..32 (default 8).
+ * Picked per workload by conehead_gb300.autotune. */
+typedef struct {
+  int dir_group;
+  int unit_order;
+  int terma_ctas_per_sm;
+} ch_tuning;
+
+ch_status ch_plan_set_tuning(ch_plan* plan, const ch_tuning* tuning);
+ch_status ch_plan_get_tuning(ch_plan* plan, ch_tuning* tuning);
+
+/* A batch captured once into a CUDA graph and replayed with one launch.
+ * ch_batch_create validates the beams like ch_dose_batch, builds every
+ * launch record into device memory the batch owns (with its own scratch),
+ * and captures the device work -- every beam's prologue, the tap ranges and
+ * the one persistent cone launch -- into a graph.  Each ch_batch_launch
+ * recomputes all doses from the current contents of the density and
+ * block-map buffers (which may change in place between launches; the
+ * geometry, settings, grids and schedule are fixed at capture).
+ * ch_batch_sync waits on `stream` and reports device-side failures.  While
+ * batches exist the plan's kernel tables and stencils are frozen: prepare the
+ * plan for the largest grid first (ch_plan_prepare).  ch_batch_destroy waits
+ * for the device.  No counterpart in the reference. */
+typedef struct ch_batch ch_batch;
+ch_status ch_batch_create(ch_plan* plan, int n_beams, const ch_grid* grids, const float* const* rho_dev,
+                          const int* swap_xy, const ch_beam* beams, const ch_settings* settings,
+                          float* const* dose_dev, void* stream, ch_batch** batch);
+ch_status ch_batch_launch(ch_batch* batch, void* stream);
+ch_status ch_batch_sync(ch_batch* batch, void* stream);
+void ch_batch_destroy(ch_batch* batch);
 
 /* Build the plan's direction stencils for this grid's voxel spacing and
  * size ahead of the first dose call (otherwise the first call that brings

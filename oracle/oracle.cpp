@@ -476,9 +476,50 @@ void cone(const or_grid& g, const double* terma, const double* K, int n_r,
   }
 }
 
+// Transpose of cone(): out[s] = sum over directions and DDA steps m of the
+// walk from s of dK_j[m] * r[v_m] -- the same walks as the scatter, reading
+// where it writes.  It is the dL/dTERMA of the beamlet adjoint (no
+// counterpart in the reference).  float64 sums in both modes.
+template <typename F>
+void cone_transpose(const or_grid& g, const double* r, const double* K, int n_r, const float* thetas,
+                    int n_theta, const float* phis, int n_phi, double* out) {
+  const int* n = g.n;
+  std::vector<F> dirs((size_t)n_theta * n_phi * 3);
+  for (int i = 0; i < n_theta; ++i)
+    for (int j = 0; j < n_phi; ++j)
+      cone_direction<F>(thetas[i], phis[j], &dirs[((size_t)i * n_phi + j) * 3]);
+#pragma omp parallel for collapse(2) schedule(dynamic, 1)
+  for (int x = 0; x < n[0]; ++x)
+    for (int y = 0; y < n[1]; ++y)
+      for (int z = 0; z < n[2]; ++z) {
+        const int start[3] = {x, y, z};
+        double acc = 0.0;
+        for (int i = 0; i < n_theta; ++i)
+          for (int j = 0; j < n_phi; ++j) {
+            const F* d = &dirs[((size_t)i * n_phi + j) * 3];
+            const double* Kj = K + (size_t)j * n_r;
+            int prev_idx = -1;
+            dda_walk<F>(start, d, g.spacing, n, [&](const int* c, F t) {
+              const int ki = kernel_index((double)t);
+              const double dk = prev_idx < 0 ? Kj[ki] : Kj[ki] - Kj[prev_idx];
+              prev_idx = ki;
+              acc += dk * r[idx3(n, c[0], c[1], c[2])];
+            });
+          }
+        out[idx3(n, x, y, z)] = acc;
+      }
+}
+
 }  // namespace
 
 extern "C" {
+
+// Transposed collapsed-cone stage (see cone_transpose); `out` overwritten.
+void or_cone_transpose(const or_grid* g, const double* r, const double* K, int n_r, const float* thetas,
+                       int n_theta, const float* phis, int n_phi, int mode, double* out) {
+  if (mode == 0) cone_transpose<float>(*g, r, K, n_r, thetas, n_theta, phis, n_phi, out);
+  else cone_transpose<double>(*g, r, K, n_r, thetas, n_theta, phis, n_phi, out);
+}
 
 // Prologue: blocked, d_eff, oad, fluence, f_soften, f_horn and TERMA.
 // All outputs are float64 arrays of n0*n1*n2 (any of the first six may be

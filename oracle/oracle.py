@@ -69,6 +69,8 @@ def lib():
         L.or_cone.argtypes = [P(_Grid), dp, dp, ctypes.c_int, P(ctypes.c_float), ctypes.c_int,
                               P(ctypes.c_float), ctypes.c_int, ctypes.c_int, dp]
         L.or_cone.restype = None
+        L.or_cone_transpose.argtypes = L.or_cone.argtypes
+        L.or_cone_transpose.restype = None
         L.or_dda.argtypes = [P(ctypes.c_int), P(ctypes.c_float), P(ctypes.c_int), dp,
                              ctypes.c_int, ctypes.c_int, P(ctypes.c_int), dp]
         L.or_dda.restype = ctypes.c_int
@@ -168,6 +170,21 @@ def cone(terma, size, spacing, K, thetas, phis, mode=MODE_F32):
                   K.shape[1], _ptr(th, ctypes.c_float), len(th), _ptr(ph, ctypes.c_float),
                   len(ph), int(mode), _ptr(dose, ctypes.c_double))
     return dose
+
+
+def cone_transpose(r, size, spacing, K, thetas, phis, mode=MODE_F64):
+    """Transposed collapsed-cone stage of a dose-shaped grid; float64."""
+    size = [int(n) for n in size]
+    R = np.ascontiguousarray(r, dtype=np.float64)
+    K = np.ascontiguousarray(K, dtype=np.float64)
+    th = np.ascontiguousarray(thetas, dtype=np.float32)
+    ph = np.ascontiguousarray(phis, dtype=np.float32)
+    g = grid_struct(size, (0, 0, 0), spacing)
+    out = np.zeros(size, dtype=np.float64)
+    lib().or_cone_transpose(ctypes.byref(g), _ptr(R, ctypes.c_double), _ptr(K, ctypes.c_double),
+                            K.shape[1], _ptr(th, ctypes.c_float), len(th), _ptr(ph, ctypes.c_float),
+                            len(ph), int(mode), _ptr(out, ctypes.c_double))
+    return out
 
 
 def calculate(source, block, phantom, settings, mode=MODE_F32, kernel_dir=None):
