@@ -531,10 +531,18 @@ def main(argv=None):
     ap.add_argument("--batch-iters", type=int, default=5)
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only", choices=["serving", "adjoint", "batched"], default=None,
+                    help="run one extra measurement alone and print its JSON (for profiling)")
     args = ap.parse_args(argv)
     args.warmup = max(3, args.warmup)      # at least three untimed warm-up steps
     if args.impl == "reference":
         return run_reference(args)
+    if args.only:
+        import torch
+        dev = torch.device("cuda", 0)
+        fn = {"serving": serving_extras, "adjoint": adjoint_extras, "batched": batched_extras}[args.only]
+        print(json.dumps({args.only: fn(args, dev)}))
+        return 0
     return run_ours(args)
 
 

@@ -89,6 +89,7 @@ struct StencilSet {
   size_t total_taps = 0;
   DevBuf tap_base, tap_len, taps, offs, tvals, chunk_base, n_chunks, chunk_start, chunk_rec, dirs;
   DevBuf raw_dirs;           // float [n_theta*n_phi][3] as the device computed them
+  DevBuf walk_row, walk_mult;  // per unique walk: kernel row (cone polar angle) and multiplicity
 };
 
 struct ch_plan {
@@ -96,9 +97,11 @@ struct ch_plan {
   int n_sm = 0;
   ch_tuning tuning{DIR_GROUP, 0, 8};
   int live_batches = 0;      // captured batches reading this plan's stencils
+  int reweights = 0;         // spectrum switches served by reweighting the stencils
   bool have_kernel = false;
   int n_phi = 0, n_r = 0, n_theta = 0;
   DevBuf K, theta, phi;
+  std::vector<float> h_theta, h_phi;   // the direction tables the stencils were built from
   StencilSet st;
   StencilSet st_adj;         // the same walks mirrored (offsets and directions negated): the transposed cone
   // scratch
@@ -125,7 +128,7 @@ struct ch_plan {
       b->release();
     for (StencilSet* S : {&st, &st_adj})
       for (DevBuf* b : {&S->tap_base, &S->tap_len, &S->taps, &S->offs, &S->tvals, &S->chunk_base, &S->n_chunks,
-                        &S->chunk_start, &S->chunk_rec, &S->dirs, &S->raw_dirs})
+                        &S->chunk_start, &S->chunk_rec, &S->dirs, &S->raw_dirs, &S->walk_row, &S->walk_mult})
         b->release();
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
@@ -198,14 +201,17 @@ ch_status assemble_stencils(ch_plan* P, StencilSet& S, int sign, int n_raw, int 
     for (float& d : h_dir) d = -d;
   }
   // merge identical walks (the 12 phi = 180 deg directions are one walk)
+  // walks merge when their offsets and kernel row (cone polar angle) agree:
+  // their weights then agree for every spectrum, so the merge, the chunks
+  // and the windows do not depend on the kernel and a new spectrum only
+  // reweights the taps (reweight_taps)
   struct Key {
     std::vector<short4> o;
-    std::vector<float> w;
+    int row;
     bool operator<(const Key& k) const {
+      if (row != k.row) return row < k.row;
       if (o.size() != k.o.size()) return o.size() < k.o.size();
-      int c = std::memcmp(o.data(), k.o.data(), o.size() * sizeof(short4));
-      if (c) return c < 0;
-      return std::memcmp(w.data(), k.w.data(), w.size() * sizeof(float)) < 0;
+      return std::memcmp(o.data(), k.o.data(), o.size() * sizeof(short4)) < 0;
     }
   };
   std::map<Key, int> seen;
@@ -215,7 +221,7 @@ ch_status assemble_stencils(ch_plan* P, StencilSet& S, int sign, int n_raw, int 
     if (L <= 0) continue;
     Key k;
     k.o.assign(h_off.begin() + (size_t)d * max_len, h_off.begin() + (size_t)d * max_len + L);
-    k.w.assign(h_dk.begin() + (size_t)d * max_len, h_dk.begin() + (size_t)d * max_len + L);
+    k.row = d % P->n_phi;
     auto it = seen.find(k);
     if (it == seen.end()) {
       seen.emplace(std::move(k), (int)uniq_first.size());
@@ -296,6 +302,10 @@ ch_status assemble_stencils(ch_plan* P, StencilSet& S, int sign, int n_raw, int 
   CH_CUDA(up(S.chunk_start, chunk_start.data(), chunk_start.size() * sizeof(int)));
   CH_CUDA(up(S.chunk_rec, chunk_rec.data(), chunk_rec.size() * sizeof(int4)));
   CH_CUDA(up(S.dirs, dirs.data(), dirs.size() * sizeof(float)));
+  std::vector<int> walk_row(U);
+  for (int u = 0; u < U; ++u) walk_row[u] = uniq_first[u] % P->n_phi;
+  CH_CUDA(up(S.walk_row, walk_row.data(), walk_row.size() * sizeof(int)));
+  CH_CUDA(up(S.walk_mult, mult.data(), mult.size() * sizeof(int)));
   CH_CUDA(cudaStreamSynchronize(s));
   S.valid = true;
   S.n_dirs = U;
@@ -894,18 +904,38 @@ ch_status ch_plan_set_kernel(ch_plan* P, const ch_kernel* k) {
     return fail(CH_ERR_INVALID_ARG, "kernel table sizes out of range");
   if (k->n_r < 5996) return fail(CH_ERR_INVALID_ARG, "kernel table needs 5996 radial samples (0.05..60 cm)");
   CH_CUDA(cudaSetDevice(P->device));
+  // same cone directions and radial sampling: the stencils stay, only their
+  // tap weights change (a spectrum switch costs one small kernel, no rebuild)
+  const bool same_dirs = P->have_kernel && k->n_theta == P->n_theta && k->n_phi == P->n_phi && k->n_r == P->n_r &&
+                         std::equal(k->theta, k->theta + k->n_theta, P->h_theta.begin()) &&
+                         std::equal(k->phi, k->phi + k->n_phi, P->h_phi.begin());
   CH_CUDA(P->K.ensure((size_t)k->n_phi * k->n_r * sizeof(double)));
   CH_CUDA(P->theta.ensure((size_t)k->n_theta * sizeof(float)));
   CH_CUDA(P->phi.ensure((size_t)k->n_phi * sizeof(float)));
+  CH_CUDA(cudaDeviceSynchronize());   // no call of this plan may still read the old tables
   CH_CUDA(cudaMemcpy(P->K.p, k->cum, (size_t)k->n_phi * k->n_r * sizeof(double), cudaMemcpyHostToDevice));
   CH_CUDA(cudaMemcpy(P->theta.p, k->theta, (size_t)k->n_theta * sizeof(float), cudaMemcpyHostToDevice));
   CH_CUDA(cudaMemcpy(P->phi.p, k->phi, (size_t)k->n_phi * sizeof(float), cudaMemcpyHostToDevice));
   P->n_phi = k->n_phi;
   P->n_r = k->n_r;
   P->n_theta = k->n_theta;
+  P->h_theta.assign(k->theta, k->theta + k->n_theta);
+  P->h_phi.assign(k->phi, k->phi + k->n_phi);
   P->have_kernel = true;
-  P->st.valid = false;
-  P->st_adj.valid = false;
+  if (same_dirs && P->st.valid) {
+    for (StencilSet* S : {&P->st, &P->st_adj}) {
+      if (!S->valid) continue;
+      launch_reweight(P->K.as<double>(), P->n_r, S->n_dirs, S->tap_base.as<int>(), S->tap_len.as<int>(),
+                      S->tvals.as<float>(), S->walk_row.as<int>(), S->walk_mult.as<int>(), S->taps.as<int4>(),
+                      nullptr);
+      CH_CUDA(cudaGetLastError());
+    }
+    CH_CUDA(cudaStreamSynchronize(nullptr));
+    P->reweights += 1;
+  } else {
+    P->st.valid = false;
+    P->st_adj.valid = false;
+  }
   return CH_OK;
 }
 
@@ -1073,7 +1103,7 @@ GridDev grid_dev(const ch_grid& grid, int swap_xy) {
 // out_box are computed.  No frustum: the input is arbitrary.  `box` and the
 // counters must have been reset (launch_init_scratch) by the caller.
 ch_status cone_operator(ch_plan* P, const ch_grid& grid, const float* in_dense, float* out, bool transpose,
-                        int* box, const int* out_box, cudaStream_t s) {
+                        int* box, const int* out_box, cudaStream_t s, const RangeBeam* out_planes = nullptr) {
   const GridDev g = grid_dev(grid, 0);
   const StencilSet& S = transpose ? P->st_adj : P->st;
   const int U = S.n_dirs;
@@ -1119,6 +1149,13 @@ ch_status cone_operator(ch_plan* P, const ch_grid& grid, const float* in_dense, 
   R.out_aabb = out_box;
   R.ranges = P->ranges.as<uint32_t>();
   R.cranges = P->cranges.as<uint32_t>();
+  if (out_planes) {
+    R.n_out_planes = out_planes->n_planes;
+    for (int j = 0; j < 4; ++j) {
+      for (int k = 0; k < 3; ++k) R.opa[j][k] = out_planes->pa[j][k];
+      R.opk0[j] = out_planes->pk0[j];
+    }
+  }
   if ((st = stage_records(P, &C, &R, 1, s)) != CH_OK) return st;
   // input into the padded layout the window tensor maps read
   CH_CUDA(cudaMemcpy2DAsync(P->adj_in.p, (size_t)g.zp * sizeof(float), in_dense, (size_t)g.n[2] * sizeof(float),
@@ -1213,7 +1250,10 @@ ch_status ch_dose_adjoint(ch_plan* P, const ch_grid* grid, const float* rho, int
   CH_CUDA(cudaGetLastError());
   // transposed cone: dL/dT = C^T dL/dD, only where TERMA is nonzero
   float* tbar = grad_terma ? grad_terma : P->adj_out.as<float>();
-  if ((st = cone_operator(P, *grid, grad_dose, tbar, true, box + 8, box, s)) != CH_OK) return st;
+  RangeBeam frustum;
+  std::memset(&frustum, 0, sizeof(frustum));
+  make_planes(*beam, *grid, b, frustum);
+  if ((st = cone_operator(P, *grid, grad_dose, tbar, true, box + 8, box, s, &frustum)) != CH_OK) return st;
   // transposed blocking and fluence: dL/dw
   CH_CUDA(cudaMemsetAsync(P->adj_w.p, 0, (size_t)bl->rows * bl->cols * sizeof(double), s));
   const BeamletDev d{bl->rows, bl->cols, bl->cell_rows, bl->cell_cols, bl->r0, bl->c0};
@@ -1403,7 +1443,7 @@ ch_status ch_plan_memory(ch_plan* P, size_t* tables, size_t* scratch) {
   size_t b = P->K.bytes + P->theta.bytes + P->phi.bytes;
   for (const StencilSet* S : {&P->st, &P->st_adj})
     for (const DevBuf* d : {&S->tap_base, &S->tap_len, &S->taps, &S->offs, &S->tvals, &S->chunk_base, &S->n_chunks,
-                            &S->chunk_start, &S->chunk_rec, &S->dirs, &S->raw_dirs})
+                            &S->chunk_start, &S->chunk_rec, &S->dirs, &S->raw_dirs, &S->walk_row, &S->walk_mult})
       b += d->bytes;
   size_t a = P->adj_in.bytes + P->adj_out.bytes + P->adj_w.bytes;
   for (int k = 0; k < 8; ++k) a += scratch_bufs(P, k)->bytes;

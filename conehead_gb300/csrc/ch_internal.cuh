@@ -175,6 +175,9 @@ struct RangeBeam {
   float pk0[4];
   const int* aabb;          // box of the nonzero input (lo/hi pairs per axis)
   const int* out_aabb;      // if set, output tiles outside this box get no taps
+  int n_out_planes;         // output tiles wholly outside one of these planes
+  float opa[4][3];          // (the beam frustum, for the transposed cone of
+  float opk0[4];            // the adjoint) get no taps either
   uint32_t* ranges;        // [n_tiles][n_dirs]: first | last tap << 16, or RANGE_EMPTY
   uint32_t* cranges;       // [n_tiles][n_dirs]: first | last chunk << 16 (direction-local)
 };
@@ -198,6 +201,8 @@ void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const
 void launch_stencil(const float* theta, int n_theta, const float* phi, int n_phi, const double* K, int n_r,
                     const float* spacing, const int* cap, int max_len, short4* off, float* t, float* dk,
                     int* len, float* dirs, cudaStream_t st);
+void launch_reweight(const double* K, int n_r, int n_walks, const int* tap_base, const int* tap_len,
+                     const float* tvals, const int* walk_row, const int* walk_mult, int4* taps, cudaStream_t st);
 void launch_dda_trace(const int* n, const float* sp, int n_rays, const int* starts, const float* dirs, int cap,
                       int* vox, float* t, int* len, cudaStream_t st);
 void launch_scatter(const float* T, const int* n, int zp, int n_dirs, const int* tap_base, const int* tap_len,

@@ -140,6 +140,17 @@ __global__ void range_kernel(const RangeBeam* __restrict__ rbs, ConeDirs D) {
     for (int k = 0; k < 3; ++k)
       wanted = wanted && vhi[k] >= R.out_aabb[2 * k] && vlo[k] <= R.out_aabb[2 * k + 1];
   }
+  for (int j = 0; j < R.n_out_planes && wanted; ++j) {
+    // the planes hold p . (spacing * i) + k0 <= 0 for voxels that can be in
+    // the beam; a tile whose minimum is above 0 is wholly outside
+    float minv = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float b = R.opa[j][k] * R.spacing[k];
+      minv += fminf(b * (float)vlo[k], b * (float)vhi[k]);
+    }
+    wanted = minv + R.opk0[j] <= 1e-3f;
+  }
   if (wanted) {
     const int blo[3] = {lo0, lo1, lo2}, bhi[3] = {hi0, hi1, hi2};
     const int base = D.tap_base[u], L = D.tap_len[u];

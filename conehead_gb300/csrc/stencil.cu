@@ -86,6 +86,33 @@ __global__ void stencil_kernel(const float* __restrict__ theta, int n_theta, con
   len_out[id] = m;
 }
 
+// New spectrum, same walks: tap weights w = mult * f32(K[row][ki] - K[row][prev])
+// recomputed from the stored t values exactly as stencil_kernel forms them.
+// One thread per unique walk.
+__global__ void reweight_kernel(const double* __restrict__ K, int n_r, int n_walks, const int* __restrict__ tap_base,
+                                const int* __restrict__ tap_len, const float* __restrict__ tvals,
+                                const int* __restrict__ walk_row, const int* __restrict__ walk_mult,
+                                int4* __restrict__ taps) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= n_walks) return;
+  const double* Kj = K + (size_t)walk_row[u] * n_r;
+  const float mult = (float)walk_mult[u];
+  const int b = tap_base[u], L = tap_len[u];
+  int prev = -1;
+  for (int m = 0; m < L; ++m) {
+    const int ki = kernel_index(tvals[b + m]);
+    const double dk = prev < 0 ? Kj[ki] : dsub(Kj[ki], Kj[prev]);
+    prev = ki;
+    taps[b + m].w = __float_as_int(__fmul_rn(d2f(dk), mult));
+  }
+}
+
+void launch_reweight(const double* K, int n_r, int n_walks, const int* tap_base, const int* tap_len,
+                     const float* tvals, const int* walk_row, const int* walk_mult, int4* taps, cudaStream_t st) {
+  reweight_kernel<<<(n_walks + 127) / 128, 128, 0, st>>>(K, n_r, n_walks, tap_base, tap_len, tvals, walk_row,
+                                                         walk_mult, taps);
+}
+
 void launch_stencil(const float* theta, int n_theta, const float* phi, int n_phi, const double* K, int n_r,
                     const float* spacing, const int* cap, int max_len, short4* off, float* t, float* dk,
                     int* len, float* dirs, cudaStream_t st) {

@@ -241,8 +241,9 @@ ch_status ch_cone(ch_plan* plan, const ch_grid* grid, const float* in_dev, float
  * grad_dose = dL/d(dose) (device, [x][y][z]) for the dose ch_dose computes
  * from this beam (whose block crop is the beamlet grid's), writes
  * grad_weights = dL/dw (device, float32 [rows][cols]) and, if grad_terma is
- * not NULL, dL/d(TERMA) ([x][y][z]).  Steps: the forward prologue, the
- * transposed cone (C^T grad_dose, computed only where TERMA is nonzero), and
+ * not NULL, dL/d(TERMA) ([x][y][z]; computed where TERMA can be nonzero --
+ * inside its box and the beam frustum -- and 0 elsewhere).  Steps: the
+ * forward prologue, the transposed cone (C^T grad_dose on those voxels), and
  * the transposed blocking: blocked(v) = sum over the S^3 sub-samples of
  * w[beamlet] / S^3 and TERMA = blocked^2 * H(v) (fluence and TERMA each carry
  * one factor), so dL/dw gets 2 TERMA/blocked * dL/dTERMA / S^3 from every
