@@ -400,11 +400,15 @@ def run_ours(args):
         peaks = json.load(open(pk_path))
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     achieved = alg_bytes / (cone_ms * 1e-3) / 1e9
+    # DRAM bytes of one cone launch: the ncu capture's bytes per beam (it reads
+    # each beam's TERMA once) times the beams of this launch
     traffic = None
-    tr_path = os.path.join(HERE, "profiles", "cone_gather_traffic.json")
-    if os.path.exists(tr_path):
-        tr = json.load(open(tr_path))
-        traffic = tr.get("bytes_per_beam", 0) * B if tr.get("bytes_per_beam") else None
+    tr_path = os.path.join(HERE, "profiles", "cone_gather_128cube_dram.json")
+    if os.path.exists(tr_path) and args.grid == 128:
+        with open(tr_path) as f:
+            tr = json.load(f)
+        if tr.get("dram_bytes_per_beam"):
+            traffic = tr["dram_bytes_per_beam"] * B
     props = torch.cuda.get_device_properties(dev)
     sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     lds_ceiling = props.multi_processor_count * 32 * sm_mhz * 1e6     # one 4-byte LDS lane per update
