@@ -44,7 +44,11 @@ class Settings(ctypes.Structure):
     _fields_ = [(k, ctypes.c_double) for k in SETTING_KEYS] + [
         ("samples", ctypes.c_int), ("n_energy", ctypes.c_int),
         ("E", ctypes.c_float * CH_MAX_ENERGY), ("w", ctypes.c_float * CH_MAX_ENERGY),
-        ("mu", ctypes.c_float * CH_MAX_ENERGY)]
+        ("mu", ctypes.c_float * CH_MAX_ENERGY), ("options", ctypes.c_int)]
+
+
+CH_OPT_RADIOLOGICAL_DISTANCE = 1
+CH_OPT_CONES_IN_BEAM_FRAME = 2
 
 
 class Kernel(ctypes.Structure):
@@ -187,7 +191,27 @@ def settings_struct(settings):
         s.E[i] = float(E[i])
         s.w[i] = float(w[i])
         s.mu[i] = float(mu[i])
+    s.options = physics_options(settings)
     return s
+
+
+def physics_options(settings):
+    """CH_OPT_* bits from the extension keys of a settings dict (absent in the
+    reference's dicts, so reference settings give 0):
+    "coneDistance": "geometric" (default) | "radiological";
+    "coneFrame": "room" (default) | "beam"."""
+    opts = 0
+    dist = settings.get("coneDistance", "geometric")
+    if dist not in ("geometric", "radiological"):
+        raise ValueError(f"coneDistance must be 'geometric' or 'radiological', not {dist!r}")
+    if dist == "radiological":
+        opts |= CH_OPT_RADIOLOGICAL_DISTANCE
+    frame = settings.get("coneFrame", "room")
+    if frame not in ("room", "beam"):
+        raise ValueError(f"coneFrame must be 'room' or 'beam', not {frame!r}")
+    if frame == "beam":
+        opts |= CH_OPT_CONES_IN_BEAM_FRAME
+    return opts
 
 
 def block_crop(block_values):

@@ -92,12 +92,26 @@ struct StencilSet {
   DevBuf walk_row, walk_mult;  // per unique walk: kernel row (cone polar angle) and multiplicity
 };
 
+struct FrameStencils {
+  ConeFrame frame{};
+  StencilSet fwd, adj;
+  uint64_t last_use = 0;
+  ~FrameStencils() {
+    for (StencilSet* S : {&fwd, &adj})
+      for (DevBuf* b : {&S->tap_base, &S->tap_len, &S->taps, &S->offs, &S->tvals, &S->chunk_base, &S->n_chunks,
+                        &S->chunk_start, &S->chunk_rec, &S->dirs, &S->raw_dirs, &S->walk_row, &S->walk_mult})
+        b->release();
+  }
+};
+
 struct ch_plan {
   int device = 0;
   int n_sm = 0;
   ch_tuning tuning{DIR_GROUP, 0, 8};
   int live_batches = 0;      // captured batches reading this plan's stencils
   int reweights = 0;         // spectrum switches served by reweighting the stencils
+  std::vector<std::unique_ptr<FrameStencils>> frames;   // beam-frame cone stencils by orientation
+  uint64_t use_clock = 0;
   bool have_kernel = false;
   int n_phi = 0, n_r = 0, n_theta = 0;
   DevBuf K, theta, phi;
@@ -148,8 +162,8 @@ ch_status assemble_stencils(ch_plan* P, StencilSet& S, int sign, int n_raw, int 
                             const std::vector<float>& h_dir_in, const float* spacing, const int* cap,
                             cudaStream_t s);
 
-ch_status build_stencils(ch_plan* P, const float* spacing, const int* cap, cudaStream_t s) {
-  StencilSet& S = P->st;
+ch_status build_stencils(ch_plan* P, const float* spacing, const int* cap, cudaStream_t s,
+                         const ConeFrame& frame, StencilSet& S, StencilSet& S_adj) {
   const int n_raw = P->n_theta * P->n_phi;
   const int max_len = cap[0] + cap[1] + cap[2] + 2;
   DevBuf off, tv, dk, len;
@@ -160,7 +174,7 @@ ch_status build_stencils(ch_plan* P, const float* spacing, const int* cap, cudaS
   CH_CUDA(S.raw_dirs.ensure((size_t)n_raw * 3 * sizeof(float)));
   launch_stencil(P->theta.as<float>(), P->n_theta, P->phi.as<float>(), P->n_phi, P->K.as<double>(), P->n_r,
                  spacing, cap, max_len, off.as<short4>(), tv.as<float>(), dk.as<float>(), len.as<int>(),
-                 S.raw_dirs.as<float>(), s);
+                 S.raw_dirs.as<float>(), frame, s);
   CH_CUDA(cudaGetLastError());
   std::vector<short4> h_off((size_t)n_raw * max_len);
   std::vector<float> h_t((size_t)n_raw * max_len), h_dk((size_t)n_raw * max_len), h_dir((size_t)n_raw * 3);
@@ -176,9 +190,9 @@ ch_status build_stencils(ch_plan* P, const float* spacing, const int* cap, cudaS
   dk.release();
   len.release();
 
-  ch_status st = assemble_stencils(P, P->st, +1, n_raw, max_len, h_off, h_t, h_dk, h_len, h_dir, spacing, cap, s);
+  ch_status st = assemble_stencils(P, S, +1, n_raw, max_len, h_off, h_t, h_dk, h_len, h_dir, spacing, cap, s);
   if (st != CH_OK) return st;
-  return assemble_stencils(P, P->st_adj, -1, n_raw, max_len, h_off, h_t, h_dk, h_len, h_dir, spacing, cap, s);
+  return assemble_stencils(P, S_adj, -1, n_raw, max_len, h_off, h_t, h_dk, h_len, h_dir, spacing, cap, s);
 }
 
 // Tap tables, chunks and launch data of one stencil set from the raw walks.
@@ -329,7 +343,44 @@ ch_status ensure_stencils(ch_plan* P, const float* spacing, const int* dims, cud
                                     "(ch_batch_destroy them, or prepare the plan for the largest grid first)");
   int cap[3];
   for (int k = 0; k < 3; ++k) cap[k] = std::max(dims[k], S.valid && S.spacing[k] == spacing[k] ? S.cap[k] : 0);
-  return build_stencils(P, spacing, cap, s);
+  ConeFrame room{};
+  return build_stencils(P, spacing, cap, s, room, P->st, P->st_adj);
+}
+
+// Stencils of the cones rotated into one beam's frame (CH_OPT_CONES_IN_BEAM_FRAME),
+// cached per orientation (least recently used out past kMaxFrames).
+constexpr size_t kMaxFrames = 16;
+ch_status frame_stencils(ch_plan* P, const float* spacing, const int* dims, const double* xform, cudaStream_t s,
+                         StencilSet** out) {
+  P->use_clock += 1;
+  for (auto& f : P->frames) {
+    bool ok = f->fwd.valid && std::memcmp(f->frame.m, xform, sizeof(f->frame.m)) == 0;
+    for (int k = 0; k < 3 && ok; ++k) ok = f->fwd.spacing[k] == spacing[k] && f->fwd.cap[k] >= dims[k];
+    if (ok) {
+      f->last_use = P->use_clock;
+      *out = &f->fwd;
+      return CH_OK;
+    }
+  }
+  if (P->live_batches > 0)
+    return fail(CH_ERR_INVALID_ARG, "beam-frame stencils cannot be built while captured batches exist");
+  if (P->frames.size() >= kMaxFrames) {
+    auto lru = std::min_element(P->frames.begin(), P->frames.end(),
+                                [](const std::unique_ptr<FrameStencils>& a, const std::unique_ptr<FrameStencils>& b) {
+                                  return a->last_use < b->last_use;
+                                });
+    P->frames.erase(lru);
+  }
+  std::unique_ptr<FrameStencils> f(new FrameStencils());
+  f->frame.on = 1;
+  std::memcpy(f->frame.m, xform, sizeof(f->frame.m));
+  int cap[3] = {dims[0], dims[1], dims[2]};
+  ch_status st = build_stencils(P, spacing, cap, s, f->frame, f->fwd, f->adj);
+  if (st != CH_OK) return st;
+  f->last_use = P->use_clock;
+  *out = &f->fwd;
+  P->frames.push_back(std::move(f));
+  return CH_OK;
 }
 
 ConeDirs cone_dirs(const StencilSet& S, const ch_tuning& t) {
@@ -380,6 +431,8 @@ ch_status check_settings(const ch_settings* s) {
   if (!s) return fail(CH_ERR_INVALID_ARG, "settings is NULL");
   if (s->samples < 1 || s->samples > 16) return fail(CH_ERR_INVALID_ARG, "fluenceResampling out of range (1..16)");
   if (s->n_energy < 0 || s->n_energy > CH_MAX_ENERGY) return fail(CH_ERR_INVALID_ARG, "too many energy bins");
+  if (s->options & ~(CH_OPT_RADIOLOGICAL_DISTANCE | CH_OPT_CONES_IN_BEAM_FRAME))
+    return fail(CH_ERR_INVALID_ARG, "unknown physics option bits");
   return CH_OK;
 }
 
@@ -607,6 +660,7 @@ const DevBuf* scratch_bufs(const ch_plan* P, int k) {
 // A validated batch: per-beam device parameters and scratch offsets.
 struct BatchPlan {
   std::vector<BeamJob> jobs;
+  const StencilSet* set = nullptr;   // the stencils of every beam of the batch
   int U = 0;
   int total_units = 0;
   int max_tiles = 0;
@@ -626,7 +680,7 @@ struct Scratch {
 
 ch_status plan_batch(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, const int* swap_xy,
                      const ch_beam* beams, const ch_settings* settings, float* const* dose, cudaStream_t s,
-                     BatchPlan& B) {
+                     BatchPlan& B, const StencilSet* set = nullptr) {
   if (!P) return fail(CH_ERR_INVALID_ARG, "plan is NULL");
   if (!P->have_kernel) return fail(CH_ERR_NO_KERNEL, "ch_plan_set_kernel has not been called");
   if (n <= 0) return fail(CH_ERR_INVALID_ARG, "no beams");
@@ -649,9 +703,14 @@ ch_status plan_batch(ch_plan* P, int n, const ch_grid* grids, const float* const
       dims[k] = std::max(dims[k], grids[i].n[k]);
     }
   }
-  ch_status st = ensure_stencils(P, grids[0].spacing, dims, s);
-  if (st != CH_OK) return st;
-  B.U = P->st.n_dirs;
+  if (set) {
+    B.set = set;                 // the caller prepared it (beam-frame cones)
+  } else {
+    ch_status st = ensure_stencils(P, grids[0].spacing, dims, s);
+    if (st != CH_OK) return st;
+    B.set = &P->st;
+  }
+  B.U = B.set->n_dirs;
   const int n_groups = (B.U + P->tuning.dir_group - 1) / P->tuning.dir_group;
   size_t t_total = 0, r_total = 0;
   B.total_units = 0;
@@ -730,6 +789,24 @@ ch_status make_records(const BatchPlan& B, const Scratch& S, std::vector<ConeBea
   return CH_OK;
 }
 
+// Device view of the optional intermediates; all = 1 when a per-voxel output
+// other than blocked/TERMA is wanted (every voxel is then evaluated).
+Inter make_inter(const ch_intermediates* inter, int& all) {
+  Inter in{};
+  all = 0;
+  if (inter) {
+    in.blocked = inter->blocked;
+    in.d_eff = inter->d_eff;
+    in.oad = inter->oad;
+    in.fluence = inter->fluence;
+    in.f_soften = inter->f_soften;
+    in.f_horn = inter->f_horn;
+    in.terma = inter->terma;
+    all = (in.d_eff || in.oad || in.fluence || in.f_soften || in.f_horn) ? 1 : 0;
+  }
+  return in;
+}
+
 // The device work of a batch (records already on the device): reset,
 // prologues, dose zeroing, tap ranges, one persistent gather.  Only kernel
 // launches and memsets, so it can be captured into a CUDA graph.  ev (4
@@ -743,18 +820,8 @@ ch_status enqueue_batch(ch_plan* P, const BatchPlan& B, const Scratch& S, const 
   launch_init_scratch(S.aabb, n, S.counters, s);
   for (int i = 0; i < n; ++i) {
     const BeamJob& J = B.jobs[i];
-    Inter in{};
     int all = 0;
-    if (inter) {
-      in.blocked = inter->blocked;
-      in.d_eff = inter->d_eff;
-      in.oad = inter->oad;
-      in.fluence = inter->fluence;
-      in.f_soften = inter->f_soften;
-      in.f_horn = inter->f_horn;
-      in.terma = inter->terma;
-      all = (in.d_eff || in.oad || in.fluence || in.f_soften || in.f_horn) ? 1 : 0;
-    }
+    const Inter in = make_inter(inter, all);
     // the voxel list is reused beam after beam (stream order)
     launch_prologue(J.rho, J.g, J.b, J.s, S.T + J.t_off, in, all, S.aabb + 8 * i, S.list_v, P->n_sm, flags, s,
                     P->tuning.terma_ctas_per_sm);
@@ -764,7 +831,7 @@ ch_status enqueue_batch(ch_plan* P, const BatchPlan& B, const Scratch& S, const 
   for (int i = 0; i < n; ++i)
     CH_CUDA(cudaMemsetAsync(B.jobs[i].dose, 0, (size_t)B.jobs[i].g.n[0] * B.jobs[i].g.n[1] * B.jobs[i].g.n[2] * 4,
                             s));
-  const ConeDirs D = cone_dirs(P->st, P->tuning);
+  const ConeDirs D = cone_dirs(*B.set, P->tuning);
   launch_range(S.range_beams, n, B.max_tiles, D, s);
   CH_CUDA(cudaGetLastError());
   if (ev) CH_CUDA(cudaEventRecord(ev[2], s));
@@ -774,11 +841,12 @@ ch_status enqueue_batch(ch_plan* P, const BatchPlan& B, const Scratch& S, const 
   return CH_OK;
 }
 
-ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, const int* swap_xy,
-              const ch_beam* beams, const ch_settings* settings, float* const* dose, const ch_intermediates* inter,
-              bool scatter, cudaStream_t s) {
+ch_status run_group(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, const int* swap_xy,
+                    const ch_beam* beams, const ch_settings* settings, float* const* dose,
+                    const ch_intermediates* inter, bool scatter, bool radiological, const StencilSet* set,
+                    cudaStream_t s) {
   BatchPlan B;
-  ch_status st = plan_batch(P, n, grids, rho, swap_xy, beams, settings, dose, s, B);
+  ch_status st = plan_batch(P, n, grids, rho, swap_xy, beams, settings, dose, s, B, set);
   if (st != CH_OK) return st;
   const ScratchNeed need = scratch_need(n, grids, B.U);
   CH_CUDA(P->T.ensure(need.bytes[0]));
@@ -805,16 +873,23 @@ ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, 
     launch_init_scratch(S.aabb, n, S.counters, s);
     for (int i = 0; i < n; ++i) {
       const BeamJob& J = B.jobs[i];
-      launch_prologue(J.rho, J.g, J.b, J.s, S.T + J.t_off, Inter{}, 0, S.aabb + 8 * i, S.list_v, P->n_sm, flags, s,
+      int all = 0;
+      const Inter in = make_inter(inter, all);
+      launch_prologue(J.rho, J.g, J.b, J.s, S.T + J.t_off, in, all, S.aabb + 8 * i, S.list_v, P->n_sm, flags, s,
                       P->tuning.terma_ctas_per_sm);
       CH_CUDA(cudaGetLastError());
     }
     CH_CUDA(cudaEventRecord(P->ev[1], s));
-    const ConeDirs D = cone_dirs(P->st, P->tuning);
+    const ConeDirs D = cone_dirs(*B.set, P->tuning);
     for (int i = 0; i < n; ++i) {
       const BeamJob& J = B.jobs[i];
       CH_CUDA(cudaMemsetAsync(J.dose, 0, (size_t)J.g.n[0] * J.g.n[1] * J.g.n[2] * 4, s));
-      launch_scatter(S.T + J.t_off, J.g.n, J.g.zp, B.U, D.tap_base, D.tap_len, D.offs, D.taps, J.dose, s);
+      if (radiological)
+        launch_scatter_radiological(S.T + J.t_off, J.rho, J.g.n, J.g.zp, J.g.swap_xy, B.U, D.tap_base, D.tap_len,
+                                    D.offs, D.tvals, B.set->walk_row.as<int>(), B.set->walk_mult.as<int>(),
+                                    P->K.as<double>(), P->n_r, J.dose, s);
+      else
+        launch_scatter(S.T + J.t_off, J.g.n, J.g.zp, B.U, D.tap_base, D.tap_len, D.offs, D.taps, J.dose, s);
       CH_CUDA(cudaGetLastError());
     }
     CH_CUDA(cudaEventRecord(P->ev[2], s));
@@ -827,6 +902,37 @@ ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, 
   if ((st = stage_records(P, cb.data(), rb.data(), n, s)) != CH_OK) return st;
   if ((st = enqueue_batch(P, B, S, inter, P->ev, s)) != CH_OK) return st;
   P->stats.n_units = B.total_units;
+  return CH_OK;
+}
+
+// Beams with physics options run one at a time, each with its own stencils
+// (beam-frame cones) and path (radiological distance: the scatter); plain
+// beams keep the fused batch.
+ch_status run(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, const int* swap_xy,
+              const ch_beam* beams, const ch_settings* settings, float* const* dose, const ch_intermediates* inter,
+              bool scatter, cudaStream_t s) {
+  bool any = false;
+  for (int i = 0; i < n && settings && beams; ++i) any |= settings[i].options != 0;
+  if (!any) return run_group(P, n, grids, rho, swap_xy, beams, settings, dose, inter, scatter, false, nullptr, s);
+  if (!P) return fail(CH_ERR_INVALID_ARG, "plan is NULL");
+  if (!P->have_kernel) return fail(CH_ERR_NO_KERNEL, "ch_plan_set_kernel has not been called");
+  if (!grids) return fail(CH_ERR_INVALID_ARG, "batch arrays missing");
+  CH_CUDA(cudaSetDevice(P->device));
+  for (int i = 0; i < n; ++i) {
+    ch_status st = check_grid(&grids[i]);
+    if (st != CH_OK) return st;
+    if ((st = check_settings(&settings[i])) != CH_OK) return st;
+    const int opt = settings[i].options;
+    StencilSet* set = nullptr;
+    if (opt & CH_OPT_CONES_IN_BEAM_FRAME) {
+      if ((st = frame_stencils(P, grids[i].spacing, grids[i].n, beams[i].xform, s, &set)) != CH_OK) return st;
+    }
+    const bool radio = (opt & CH_OPT_RADIOLOGICAL_DISTANCE) != 0;
+    st = run_group(P, 1, &grids[i], rho ? &rho[i] : nullptr, swap_xy ? &swap_xy[i] : nullptr, &beams[i],
+                   &settings[i], dose ? &dose[i] : nullptr, n == 1 ? inter : nullptr, scatter || radio, radio, set,
+                   s);
+    if (st != CH_OK) return st;
+  }
   return CH_OK;
 }
 
@@ -936,6 +1042,7 @@ ch_status ch_plan_set_kernel(ch_plan* P, const ch_kernel* k) {
     P->st.valid = false;
     P->st_adj.valid = false;
   }
+  P->frames.clear();          // beam-frame stencils are rebuilt on demand
   return CH_OK;
 }
 
@@ -970,6 +1077,7 @@ ch_status ch_dose_static(ch_plan* P, const ch_grid* grid, const float* rho, int 
   if ((st = check_settings(settings)) != CH_OK) return st;
   if (!rho || !dose) return fail(CH_ERR_INVALID_ARG, "density or dose pointer is NULL");
   if (swap_xy && grid->n[0] != grid->n[1]) return fail(CH_ERR_INVALID_ARG, "swap_xy needs a square x/y grid");
+  if (settings->options) return fail(CH_ERR_INVALID_ARG, "ch_dose_static runs the reference physics only (options = 0)");
   // everything that allocates must already exist on the plan
   const StencilSet& S = P->st;
   bool ready = S.valid && P->counters.p;
@@ -1222,6 +1330,7 @@ ch_status ch_dose_adjoint(ch_plan* P, const ch_grid* grid, const float* rho, int
   if ((st = check_beam(beam)) != CH_OK) return st;
   if ((st = check_settings(settings)) != CH_OK) return st;
   if ((st = check_beamlets(bl)) != CH_OK) return st;
+  if (settings->options) return fail(CH_ERR_INVALID_ARG, "the adjoint covers the reference physics only (options = 0)");
   if (!rho || !grad_dose || !grad_weights) return fail(CH_ERR_INVALID_ARG, "density or gradient pointer is NULL");
   if (swap_xy && grid->n[0] != grid->n[1]) return fail(CH_ERR_INVALID_ARG, "swap_xy needs a square x/y grid");
   if (beam->block_r0 != bl->r0 || beam->block_c0 != bl->c0 || beam->block_rows != bl->rows * bl->cell_rows ||
@@ -1287,6 +1396,8 @@ ch_status ch_batch_create(ch_plan* P, int n, const ch_grid* grids, const float* 
   if (!out) return fail(CH_ERR_INVALID_ARG, "batch out-pointer is NULL");
   *out = nullptr;
   cudaStream_t s = (cudaStream_t)stream;
+  for (int i = 0; settings && i < n; ++i)
+    if (settings[i].options) return fail(CH_ERR_INVALID_ARG, "captured batches run the reference physics only (options = 0)");
   BatchPlan B;
   ch_status st = plan_batch(P, n, grids, rho, swap_xy, beams, settings, dose, s, B);
   if (st != CH_OK) return st;
@@ -1445,6 +1556,12 @@ ch_status ch_plan_memory(ch_plan* P, size_t* tables, size_t* scratch) {
     for (const DevBuf* d : {&S->tap_base, &S->tap_len, &S->taps, &S->offs, &S->tvals, &S->chunk_base, &S->n_chunks,
                             &S->chunk_start, &S->chunk_rec, &S->dirs, &S->raw_dirs, &S->walk_row, &S->walk_mult})
       b += d->bytes;
+  for (const auto& f : P->frames)
+    for (const StencilSet* S : {&f->fwd, &f->adj})
+      for (const DevBuf* d : {&S->tap_base, &S->tap_len, &S->taps, &S->offs, &S->tvals, &S->chunk_base,
+                              &S->n_chunks, &S->chunk_start, &S->chunk_rec, &S->dirs, &S->raw_dirs, &S->walk_row,
+                              &S->walk_mult})
+        b += d->bytes;
   size_t a = P->adj_in.bytes + P->adj_out.bytes + P->adj_w.bytes;
   for (int k = 0; k < 8; ++k) a += scratch_bufs(P, k)->bytes;
   if (tables) *tables = b;

@@ -198,9 +198,19 @@ void upload_unit_partials();
 void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const SettingsDev& s, float* T,
                      const Inter& inter, int all_voxels, int* aabb, int* list_v, int n_sm, int* flags,
                      cudaStream_t st, int ctas_per_sm = 8);
+// Frame of the cone directions: off = the room frame (the reference), on =
+// rotated by a beam's world->beam matrix m (row major, xform of ch_beam).
+struct ConeFrame {
+  int on;
+  double m[9];
+};
 void launch_stencil(const float* theta, int n_theta, const float* phi, int n_phi, const double* K, int n_r,
                     const float* spacing, const int* cap, int max_len, short4* off, float* t, float* dk,
-                    int* len, float* dirs, cudaStream_t st);
+                    int* len, float* dirs, const ConeFrame& frame, cudaStream_t st);
+void launch_scatter_radiological(const float* T, const float* rho, const int* n, int zp, int swap_xy, int n_dirs,
+                                 const int* tap_base, const int* tap_len, const short4* offs, const float* tvals,
+                                 const int* walk_row, const int* walk_mult, const double* K, int n_r, float* dose,
+                                 cudaStream_t st);
 void launch_reweight(const double* K, int n_r, int n_walks, const int* tap_base, const int* tap_len,
                      const float* tvals, const int* walk_row, const int* walk_mult, int4* taps, cudaStream_t st);
 void launch_dda_trace(const int* n, const float* sp, int n_rays, const int* starts, const float* dirs, int cap,

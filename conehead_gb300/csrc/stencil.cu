@@ -44,12 +44,24 @@ __global__ void stencil_kernel(const float* __restrict__ theta, int n_theta, con
                                int n_phi, const double* __restrict__ K, int n_r, float sx, float sy, float sz,
                                int cap0, int cap1, int cap2, int max_len, short4* __restrict__ off_out,
                                float* __restrict__ t_out, float* __restrict__ dk_out,
-                               int* __restrict__ len_out, float* __restrict__ dir_out) {
+                               int* __restrict__ len_out, float* __restrict__ dir_out, ConeFrame frame) {
   const int id = blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= n_theta * n_phi) return;
   const int i = id / n_phi, j = id % n_phi;
   float d[3];
   cone_direction(theta[i], phi[j], d);
+  if (frame.on) {
+    // cones in the beam frame: d_room[k] = sum_i xform[i][k] d[i] (the rows of
+    // the beam's world->beam rotation are its axes); float64, one rounding
+    float r[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      r[k] = d2f(dadd(dadd(dmul(frame.m[k], (double)d[0]), dmul(frame.m[3 + k], (double)d[1])),
+                      dmul(frame.m[6 + k], (double)d[2])));
+    d[0] = r[0];
+    d[1] = r[1];
+    d[2] = r[2];
+  }
   dir_out[3 * id + 0] = d[0];
   dir_out[3 * id + 1] = d[1];
   dir_out[3 * id + 2] = d[2];
@@ -115,11 +127,11 @@ void launch_reweight(const double* K, int n_r, int n_walks, const int* tap_base,
 
 void launch_stencil(const float* theta, int n_theta, const float* phi, int n_phi, const double* K, int n_r,
                     const float* spacing, const int* cap, int max_len, short4* off, float* t, float* dk,
-                    int* len, float* dirs, cudaStream_t st) {
+                    int* len, float* dirs, const ConeFrame& frame, cudaStream_t st) {
   const int n = n_theta * n_phi;
   stencil_kernel<<<(n + 127) / 128, 128, 0, st>>>(theta, n_theta, phi, n_phi, K, n_r, spacing[0], spacing[1],
                                                  spacing[2], cap[0], cap[1], cap[2], max_len, off, t, dk, len,
-                                                 dirs);
+                                                 dirs, frame);
 }
 
 // ------------------------------------------------------------- DDA hook --
@@ -190,6 +202,60 @@ __global__ void __launch_bounds__(128) scatter_kernel(const float* __restrict__ 
       atomicAdd(dose + ((long long)tx * n1 + ty) * n2 + tz, Tv * __int_as_float(taps[b + m].w));
     }
   }
+}
+
+// Radiological cone distance (an extension, CH_OPT_RADIOLOGICAL_DISTANCE):
+// the same walks as scatter_kernel, but the kernel is read at the
+// density-scaled path length from the source voxel centre,
+//   r_m = sum_{k <= m} rho(v_k) * (t_k - t_{k-1}),   t_{-1} = 0,
+// accumulated in float32 in walk order like the radiological depth of the
+// TERMA pass (conehead/conehead.py:209-254).  With rho = 1 this is the
+// geometric walk tap for tap.  Densities are read with the x/y convention
+// of the prologue (swap_xy).  Each unique walk carries its multiplicity.
+__global__ void __launch_bounds__(128) scatter_radiological_kernel(
+    const float* __restrict__ T, const float* __restrict__ rho, int n0, int n1, int n2, int zp, int swap_xy,
+    int n_dirs, const int* __restrict__ tap_base, const int* __restrict__ tap_len, const short4* __restrict__ offs,
+    const float* __restrict__ tvals, const int* __restrict__ walk_row, const int* __restrict__ walk_mult,
+    const double* __restrict__ K, int n_r, float* __restrict__ dose) {
+  const long long N = (long long)n0 * n1 * n2;
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= N) return;
+  const int z = (int)(v % n2);
+  const long long r = v / n2;
+  const int y = (int)(r % n1), x = (int)(r / n1);
+  const float Tv = T[((long long)x * n1 + y) * zp + z];
+  if (Tv == 0.0f) return;
+  for (int u = 0; u < n_dirs; ++u) {
+    const int b = tap_base[u], L = tap_len[u];
+    const double* Kj = K + (size_t)walk_row[u] * n_r;
+    const float mult = (float)walk_mult[u];
+    float rad = 0.0f, tprev = 0.0f;
+    int prev = -1;
+    for (int m = 0; m < L; ++m) {
+      const short4 o = offs[b + m];
+      const int tx = x + o.x, ty = y + o.y, tz = z + o.z;
+      if (tx < 0 || tx >= n0 || ty < 0 || ty >= n1 || tz < 0 || tz >= n2) break;
+      const long long ri = swap_xy ? ((long long)ty * n0 + tx) * n2 + tz : ((long long)tx * n1 + ty) * n2 + tz;
+      const float t = tvals[b + m];
+      rad = fadd(rad, fmul(__ldg(rho + ri), fsub(t, tprev)));
+      tprev = t;
+      const int ki = kernel_index(rad);
+      if (prev == 5995 && ki == 5995) break;
+      const double dk = prev < 0 ? Kj[ki] : dsub(Kj[ki], Kj[prev]);
+      prev = ki;
+      atomicAdd(dose + ((long long)tx * n1 + ty) * n2 + tz, Tv * __fmul_rn(d2f(dk), mult));
+    }
+  }
+}
+
+void launch_scatter_radiological(const float* T, const float* rho, const int* n, int zp, int swap_xy, int n_dirs,
+                                 const int* tap_base, const int* tap_len, const short4* offs, const float* tvals,
+                                 const int* walk_row, const int* walk_mult, const double* K, int n_r, float* dose,
+                                 cudaStream_t st) {
+  const long long N = (long long)n[0] * n[1] * n[2];
+  scatter_radiological_kernel<<<(unsigned)((N + 127) / 128), 128, 0, st>>>(
+      T, rho, n[0], n[1], n[2], zp, swap_xy, n_dirs, tap_base, tap_len, offs, tvals, walk_row, walk_mult, K, n_r,
+      dose);
 }
 
 void launch_scatter(const float* T, const int* n, int zp, int n_dirs, const int* tap_base, const int* tap_len,

@@ -87,7 +87,26 @@ typedef struct {
   float E[CH_MAX_ENERGY];
   float w[CH_MAX_ENERGY];
   float mu[CH_MAX_ENERGY];
+  int options;          /* 0 = the reference's physics; CH_OPT_* bits below */
 } ch_settings;
+
+/* Physics extensions, off by default (not in the reference, so no parity
+ * claim; each equals the reference where it must, see the tests).
+ *
+ * CH_OPT_RADIOLOGICAL_DISTANCE: the kernel is read at the density-scaled
+ *   path length along each cone line, r = sum rho(v) * (segment in v), from
+ *   the source voxel centre, instead of the geometric distance.  Equal to the
+ *   reference in water (rho = 1).  The weights then depend on the densities
+ *   between source and target, so these beams run the per-source scatter
+ *   path (ch_dose_scatter's structure), not the stencil gather.
+ * CH_OPT_CONES_IN_BEAM_FRAME: the 12 x 48 cone directions are rotated with
+ *   the beam (d = xform^T d_ref: the kernel's polar axis follows the central
+ *   axis of the beam, the collimator turns the azimuths), instead of staying
+ *   in the room frame (conehead/conehead.py:386 leaves source_transform
+ *   unused).  Equal to the reference at gantry and collimator 0.  Stencils are
+ *   built per beam orientation and cached in the plan. */
+#define CH_OPT_RADIOLOGICAL_DISTANCE 1
+#define CH_OPT_CONES_IN_BEAM_FRAME 2
 
 /* Host tables of the polyenergetic kernel: cumulative K[n_phi][n_r]
  * (float64, radii 0.05 + 0.01 k cm), azimuths theta[n_theta] and cone polar

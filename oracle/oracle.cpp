@@ -422,15 +422,36 @@ inline int kernel_index(double t) {
   return (int)i;
 }
 
+// Options of the physics extensions (not in the reference): rho != null reads
+// the kernel at the radiological path length along each cone line
+// (density-scaled distance); frame != null rotates the cone directions by a
+// beam's world->beam matrix (cones in the beam frame).
+struct ConeExt {
+  const float* rho = nullptr;
+  int swap_xy = 0;
+  const double* frame = nullptr;   // row-major 3x3
+};
+
+template <typename F>
+void rotate_direction(const double* m, F* d) {
+  F r[3];
+  for (int k = 0; k < 3; ++k) r[k] = (F)(m[k] * (double)d[0] + m[3 + k] * (double)d[1] + m[6 + k] * (double)d[2]);
+  d[0] = r[0];
+  d[1] = r[1];
+  d[2] = r[2];
+}
+
 template <typename F>
 void cone(const or_grid& g, const double* terma, const double* K, int n_r,
-          const float* thetas, int n_theta, const float* phis, int n_phi, double* dose) {
+          const float* thetas, int n_theta, const float* phis, int n_phi, double* dose, const ConeExt& ext = {}) {
   const int* n = g.n;
   const int64_t N = (int64_t)n[0] * n[1] * n[2];
   std::vector<F> dirs((size_t)n_theta * n_phi * 3);
   for (int i = 0; i < n_theta; ++i)
-    for (int j = 0; j < n_phi; ++j)
+    for (int j = 0; j < n_phi; ++j) {
       cone_direction<F>(thetas[i], phis[j], &dirs[((size_t)i * n_phi + j) * 3]);
+      if (ext.frame) rotate_direction<F>(ext.frame, &dirs[((size_t)i * n_phi + j) * 3]);
+    }
   int nthr = 1;
 #ifdef _OPENMP
   nthr = omp_get_max_threads();
@@ -456,8 +477,18 @@ void cone(const or_grid& g, const double* terma, const double* K, int n_r,
               const F* d = &dirs[((size_t)i * n_phi + j) * 3];
               const double* Kj = K + (size_t)j * n_r;
               int prev_idx = -1;
+              F rad = 0, tprev = 0;
               dda_walk<F>(start, d, g.spacing, n, [&](const int* c, F t) {
-                const int ki = kernel_index((double)t);
+                F tk = t;
+                if (ext.rho) {
+                  // path length scaled by the density of each voxel crossed
+                  const int64_t ri = ext.swap_xy ? ((int64_t)c[1] * n[0] + c[0]) * n[2] + c[2]
+                                                 : ((int64_t)c[0] * n[1] + c[1]) * n[2] + c[2];
+                  rad = rad + (F)ext.rho[ri] * (t - tprev);
+                  tprev = t;
+                  tk = rad;
+                }
+                const int ki = kernel_index((double)tk);
                 const double dk = prev_idx < 0 ? Kj[ki] : Kj[ki] - Kj[prev_idx];
                 prev_idx = ki;
                 double contrib;
@@ -513,6 +544,21 @@ void cone_transpose(const or_grid& g, const double* r, const double* K, int n_r,
 }  // namespace
 
 extern "C" {
+
+// Cone stage with the physics extensions (see ConeExt): rho (float32, the
+// phantom's densities, read with swap_xy like the TERMA pass) for the
+// radiological distance, frame (3x3 row-major world->beam matrix) for cones
+// in the beam frame; either may be null.
+void or_cone_ext(const or_grid* g, const double* terma, const double* K, int n_r, const float* thetas,
+                 int n_theta, const float* phis, int n_phi, int mode, const float* rho, int swap_xy,
+                 const double* frame, double* dose) {
+  ConeExt ext;
+  ext.rho = rho;
+  ext.swap_xy = swap_xy;
+  ext.frame = frame;
+  if (mode == 0) cone<float>(*g, terma, K, n_r, thetas, n_theta, phis, n_phi, dose, ext);
+  else cone<double>(*g, terma, K, n_r, thetas, n_theta, phis, n_phi, dose, ext);
+}
 
 // Transposed collapsed-cone stage (see cone_transpose); `out` overwritten.
 void or_cone_transpose(const or_grid* g, const double* r, const double* K, int n_r, const float* thetas,

@@ -69,6 +69,10 @@ def lib():
         L.or_cone.argtypes = [P(_Grid), dp, dp, ctypes.c_int, P(ctypes.c_float), ctypes.c_int,
                               P(ctypes.c_float), ctypes.c_int, ctypes.c_int, dp]
         L.or_cone.restype = None
+        L.or_cone_ext.argtypes = [P(_Grid), dp, dp, ctypes.c_int, P(ctypes.c_float), ctypes.c_int,
+                                  P(ctypes.c_float), ctypes.c_int, ctypes.c_int, P(ctypes.c_float), ctypes.c_int,
+                                  dp, dp]
+        L.or_cone_ext.restype = None
         L.or_cone_transpose.argtypes = L.or_cone.argtypes
         L.or_cone_transpose.restype = None
         L.or_dda.argtypes = [P(ctypes.c_int), P(ctypes.c_float), P(ctypes.c_int), dp,
@@ -169,6 +173,26 @@ def cone(terma, size, spacing, K, thetas, phis, mode=MODE_F32):
     lib().or_cone(ctypes.byref(g), _ptr(T, ctypes.c_double), _ptr(K, ctypes.c_double),
                   K.shape[1], _ptr(th, ctypes.c_float), len(th), _ptr(ph, ctypes.c_float),
                   len(ph), int(mode), _ptr(dose, ctypes.c_double))
+    return dose
+
+
+def cone_ext(terma, size, spacing, K, thetas, phis, mode=MODE_F32, rho=None, swap_xy=False, frame=None):
+    """Cone stage with the physics extensions: ``rho`` (densities) for the
+    radiological cone distance, ``frame`` (3x3 world->beam matrix) for cones
+    in the beam frame."""
+    size = [int(n) for n in size]
+    T = np.ascontiguousarray(terma, dtype=np.float64)
+    K = np.ascontiguousarray(K, dtype=np.float64)
+    th = np.ascontiguousarray(thetas, dtype=np.float32)
+    ph = np.ascontiguousarray(phis, dtype=np.float32)
+    g = grid_struct(size, (0, 0, 0), spacing)
+    dose = np.zeros(size, dtype=np.float64)
+    r = None if rho is None else np.ascontiguousarray(rho, dtype=np.float32)
+    f = None if frame is None else np.ascontiguousarray(np.asarray(frame, dtype=np.float64).reshape(9))
+    lib().or_cone_ext(ctypes.byref(g), _ptr(T, ctypes.c_double), _ptr(K, ctypes.c_double), K.shape[1],
+                      _ptr(th, ctypes.c_float), len(th), _ptr(ph, ctypes.c_float), len(ph), int(mode),
+                      None if r is None else _ptr(r, ctypes.c_float), int(bool(swap_xy)),
+                      None if f is None else _ptr(f, ctypes.c_double), _ptr(dose, ctypes.c_double))
     return dose
 
 

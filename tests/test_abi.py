@@ -51,7 +51,7 @@ def test_status_strings(library):
 
 def test_struct_sizes_match_header_layout():
     # ch_settings: 11 doubles + 2 ints + 3 x 32 floats
-    assert ctypes.sizeof(N.Settings) == 11 * 8 + 2 * 4 + 3 * 32 * 4
+    assert ctypes.sizeof(N.Settings) == 11 * 8 + 2 * 4 + 3 * 32 * 4 + 8   # options + padding to 8
     assert ctypes.sizeof(N.Grid) == 36
     assert N.Beam.block.offset == 3 * 8 + 3 * 8 + 9 * 8 + 8 + 2 * 4
 
