@@ -16,7 +16,14 @@ namespace ch {
 // registers; 8 consumer warps cover the 16 y rows.
 constexpr int TZ = 16, TY = 16, TX = 16;
 constexpr int TILE_VOX = TZ * TY * TX;
-constexpr int OUT_PER_THREAD = TX;
+// the tile's 16 x outputs may be split between X_SPLIT consumer warps (more
+// warps per SM to hide shared-memory latency, but every warp fetches the taps
+// itself); measured at 128^3, 1 is faster (33.3 vs 35.3 ms per 16 beams)
+#ifndef CH_X_SPLIT
+#define CH_X_SPLIT 1
+#endif
+constexpr int X_SPLIT = CH_X_SPLIT;
+constexpr int OUT_PER_THREAD = TX / X_SPLIT;
 // Shared-memory window of a chunk: [x][row][z] with z pitch P and `rows` y
 // rows per x slice.  Three shapes ("variants") trade z reach for x reach in
 // one fixed slot; the chunker picks the cheapest that holds the chunk.  Every
@@ -42,7 +49,7 @@ constexpr int N_TMAPS = n_maps_before(2) + (var_max_ex(2) - TX + 1);
 __host__ __device__ constexpr int tmap_index(int v, int ex) { return n_maps_before(v) + (ex - TX); }
 constexpr int MAX_CHUNK_TAPS = 64;    // taps per chunk (their table is staged with the window)
 constexpr int N_SLOTS = 2;
-constexpr int CONE_CONSUMER_WARPS = TY / 2;
+constexpr int CONE_CONSUMER_WARPS = (TY / 2) * X_SPLIT;
 constexpr int CONE_THREADS = (CONE_CONSUMER_WARPS + 1) * 32;
 constexpr int DIR_GROUP = 16;         // unique directions per work unit (default; ch_tuning.dir_group)
 constexpr int MAX_DIR_GROUP = 32;     // the producer fetches one direction's ranges per lane

@@ -355,9 +355,11 @@ __device__ __forceinline__ void consumer(const ConeBeam* __restrict__ beams, con
                                          const float* win, const int4* slot_taps, const ChunkDesc* desc,
                                          uint64_t* full, uint64_t* empty) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int rw = warp % (TY / 2);                                // row pair of this warp
+  const int xo = (warp / (TY / 2)) * OUT_PER_THREAD;             // first x of this warp
   const int zl = lane & 15;                                      // z within the tile
-  const int yl = (warp & 1) + 4 * (warp >> 1) + 2 * (lane >> 4); // y within the tile
-  float acc[OUT_PER_THREAD];                                     // x = 0 .. TX-1
+  const int yl = (rw & 1) + 4 * (rw >> 1) + 2 * (lane >> 4);     // y within the tile
+  float acc[OUT_PER_THREAD];                                     // x = xo .. xo + OUT_PER_THREAD - 1
 #pragma unroll
   for (int i = 0; i < OUT_PER_THREAD; ++i) acc[i] = 0.0f;
   for (int k = 0;; ++k) {
@@ -372,7 +374,7 @@ __device__ __forceinline__ void consumer(const ConeBeam* __restrict__ beams, con
     const int4* tp = slot_taps + (size_t)s * MAX_CHUNK_TAPS;
     const int nt = d.b - d.a + 1;
     const int rows = var_rows(d.var), P = var_p(d.var);
-    const int base0 = ((d.tx0 - d.x0w) * rows + (d.ty0 + yl - d.y0w)) * P + (d.tz0 + zl - d.z0w);
+    const int base0 = ((d.tx0 + xo - d.x0w) * rows + (d.ty0 + yl - d.y0w)) * P + (d.tz0 + zl - d.z0w);
     if (d.var == 0) consume_chunk<0>(w, tp, nt, base0, acc);
     else if (d.var == 1) consume_chunk<1>(w, tp, nt, base0, acc);
     else consume_chunk<2>(w, tp, nt, base0, acc);
@@ -382,11 +384,11 @@ __device__ __forceinline__ void consumer(const ConeBeam* __restrict__ beams, con
       const ConeBeam& B = beams[d.beam];
       const int y = d.ty0 + yl, z = d.tz0 + zl;
       if (y < B.n[1] && z < B.n[2]) {
-        float* out = B.dose + ((long long)d.tx0 * B.n[1] + y) * B.n[2] + z;
+        float* out = B.dose + ((long long)(d.tx0 + xo) * B.n[1] + y) * B.n[2] + z;
         const long long xs = (long long)B.n[1] * B.n[2];
 #pragma unroll
         for (int i = 0; i < OUT_PER_THREAD; ++i)
-          if (d.tx0 + i < B.n[0]) atomicAdd(out + i * xs, acc[i]);
+          if (d.tx0 + xo + i < B.n[0]) atomicAdd(out + i * xs, acc[i]);
       }
 #pragma unroll
       for (int i = 0; i < OUT_PER_THREAD; ++i) acc[i] = 0.0f;
