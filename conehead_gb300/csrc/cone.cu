@@ -9,7 +9,7 @@
 // taps m whose sources can hold TERMA: the source box of the tile must meet
 // the TERMA bounding box (exact, per axis, on the monotone offsets) and the
 // beam frustum widened by half a voxel plus the tile (conservative, through
-// the continuous ray: |O_k[m] - t_m d_k / s_k| <= 1).  Every skipped tap
+// the continuous ray: |O_k[m] - t_m d_k / s_k| <= 1/2).  Every skipped tap
 // therefore reads only zero TERMA, so the result is exact.
 //
 // cone_gather_kernel is persistent and warp specialised:
@@ -172,7 +172,10 @@ __global__ void range_kernel(const RangeBeam* __restrict__ rbs, ConeDirs D) {
       mlo = max(mlo, lower_bound(L, klo, key));
       mhi = min(mhi, lower_bound(L, khi + 0.5f, key) - 1);
     }
-    // beam frustum planes through the continuous ray
+    // beam frustum planes through the continuous ray.  t_m is the parameter
+    // where the ray leaves voxel O[m], so the ray point lies on that voxel's
+    // closed box: |O_k[m] - t_m d_k / s_k| <= 1/2 per axis, hence the slack of
+    // half the plane's L1 weight (plus a float margin)
     for (int j = 0; j < R.n_planes && mlo <= mhi; ++j) {
       float minv = 0.0f, l1 = 0.0f, g = 0.0f;
 #pragma unroll
@@ -182,7 +185,7 @@ __global__ void range_kernel(const RangeBeam* __restrict__ rbs, ConeDirs D) {
         l1 += fabsf(b);
         g += R.pa[j][k] * dir[k];
       }
-      const float h = minv + R.pk0[j] - l1 - 1e-3f * (l1 + 1.0f);
+      const float h = minv + R.pk0[j] - 0.5f * l1 - 1e-3f * (l1 + 1.0f);
       auto tkey = [&](int m) { return tv[m]; };
       if (g > 0.0f) {
         mlo = max(mlo, lower_bound(L, h / g, tkey));
