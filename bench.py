@@ -198,8 +198,10 @@ def serving_extras(args, dev):
     """Poisson-arrival serving runs, one per rate; results dropped as they land."""
     import torch
     from conehead_gb300.serving import DoseServer, GpuExecutor, drive, poisson_workload
+    from conehead_gb300.conehead import engine
     sizes = (64, 96, 128, 192)
-    ex = GpuExecutor(dev.index, n_slots=2)
+    # the schedule the headline run tuned (the default if it did not tune)
+    ex = GpuExecutor(dev.index, n_slots=2, tuning=engine(dev.index).get_tuning())
     for n in sizes:
         ex.add_phantom(f"p{n}", workload(n, args.spacing, seed=n))
     ex.prepare(SETTINGS, (args.spacing,) * 3, (max(sizes),) * 3)
@@ -366,6 +368,12 @@ def run_ours(args):
     for s in range(args.warmup):
         eng.run_batch(step_jobs(s))
     eng.sync()
+    # schedule for this workload from the autotuner (untimed, cached per device and workload)
+    schedule = {"tuning": eng.get_tuning(), "source": "default"}
+    if not args.no_autotune:
+        from conehead_gb300.autotune import autotune
+        r = autotune(eng, step_jobs(0))
+        schedule = {"tuning": r["tuning"], "source": "autotune (cached)" if r["cached"] else "autotune"}
     stats = []
     step_ms = []
     clocks = ClockSampler(local)
@@ -507,6 +515,7 @@ def run_ours(args):
             "e2e": e2e,
             "clocks": clk,
             "gpu_launches": args.steps * (2 * B + 3),
+            "schedule": schedule,
         }
         line.update(extras)
         print(json.dumps(line))
@@ -533,6 +542,7 @@ def main(argv=None):
     ap.add_argument("--adjoint-iters", type=int, default=5, help="timed gradient evaluations (0: skip)")
     ap.add_argument("--batch-beams", type=int, default=64, help="beams of the captured mixed batch (0: skip)")
     ap.add_argument("--batch-iters", type=int, default=5)
+    ap.add_argument("--no-autotune", action="store_true", help="time the default schedule")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only", choices=["serving", "adjoint", "batched"], default=None,

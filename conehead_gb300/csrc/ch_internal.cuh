@@ -52,7 +52,7 @@ constexpr int N_SLOTS = 2;
 constexpr int CONE_CONSUMER_WARPS = (TY / 2) * X_SPLIT;
 constexpr int CONE_THREADS = (CONE_CONSUMER_WARPS + 1) * 32;
 constexpr int DIR_GROUP = 16;         // unique directions per work unit (default; ch_tuning.dir_group)
-constexpr int MAX_DIR_GROUP = 32;     // the producer fetches one direction's ranges per lane
+constexpr int MAX_DIR_GROUP = 1024;   // the producer walks a unit's directions 32 at a time
 
 // Bounded device-side waits (iterations of try_wait / spin).
 constexpr long long WAIT_LIMIT = 1ll << 26;

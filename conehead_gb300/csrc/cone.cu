@@ -256,63 +256,66 @@ __device__ __forceinline__ void producer(const ConeBeam* __restrict__ beams, int
     const int tx0 = (tile / (B.ntile[1] * B.ntile[2])) * TX;
     const int ty0 = ((tile / B.ntile[2]) % B.ntile[1]) * TY;
     const int tz0 = (tile % B.ntile[2]) * TZ;
-    // lanes 0..group-1 fetch the ranges of the group's directions in parallel
+    // the unit's directions, 32 at a time: lanes fetch their ranges in parallel
     const int u0 = g * D.group;
-    uint32_t r = RANGE_EMPTY, cr = 0;
-    int cb = 0, tb = 0;
-    if (lane < D.group && u0 + lane < D.n_dirs) {
-      const long long ri = (long long)tile * D.n_dirs + u0 + lane;
-      r = __ldg(B.ranges + ri);
-      if (r != RANGE_EMPTY) {
-        cr = __ldg(B.cranges + ri);
-        cb = __ldg(D.chunk_base + u0 + lane);
-        tb = __ldg(D.tap_base + u0 + lane);
-      }
-    }
-    unsigned act = __ballot_sync(0xffffffffu, r != RANGE_EMPTY);
+    const int u_end = min(u0 + D.group, D.n_dirs);
     unsigned long long work = 0;
-    while (act && ok) {
-      const int j = __ffs(act) - 1;
-      act &= act - 1;
-      const uint32_t rj = __shfl_sync(0xffffffffu, r, j), crj = __shfl_sync(0xffffffffu, cr, j);
-      const int cbj = __shfl_sync(0xffffffffu, cb, j), tbj = __shfl_sync(0xffffffffu, tb, j);
-      const int mlo = (int)(rj & 0xffffu), mhi = (int)(rj >> 16);
-      const int c_first = (int)(crj & 0xffffu), c_last = (int)(crj >> 16);
-      for (int c0 = c_first; c0 <= c_last && ok; c0 += 32) {
-        // lanes fetch up to 32 chunk records at once
-        int4 r0 = make_int4(0, 0, 0, 0), r1 = make_int4(0, 0, 0, 0);
-        if (c0 + lane <= c_last) {
-          r0 = __ldg(D.chunk_rec + 2 * (cbj + c0 + lane));
-          r1 = __ldg(D.chunk_rec + 2 * (cbj + c0 + lane) + 1);
+    for (int ub = u0; ub < u_end && ok; ub += 32) {
+      uint32_t r = RANGE_EMPTY, cr = 0;
+      int cb = 0, tb = 0;
+      if (ub + lane < u_end) {
+        const long long ri = (long long)tile * D.n_dirs + ub + lane;
+        r = __ldg(B.ranges + ri);
+        if (r != RANGE_EMPTY) {
+          cr = __ldg(B.cranges + ri);
+          cb = __ldg(D.chunk_base + ub + lane);
+          tb = __ldg(D.tap_base + ub + lane);
         }
-        const int nrec = min(32, c_last - c0 + 1);
-        for (int q = 0; q < nrec && ok; ++q) {
-          const int a0 = __shfl_sync(0xffffffffu, r0.x, q), b0 = __shfl_sync(0xffffffffu, r0.y, q);
-          const int var = __shfl_sync(0xffffffffu, r0.z, q), sxy = __shfl_sync(0xffffffffu, r0.w, q);
-          const int mox = __shfl_sync(0xffffffffu, r1.x, q), moy = __shfl_sync(0xffffffffu, r1.y, q);
-          const int moz = __shfl_sync(0xffffffffu, r1.z, q);
-          ChunkDesc d;
-          d.u = u0 + j;
-          d.a = max(a0, mlo);
-          d.b = min(b0, mhi);
-          // window of the whole chunk (covers the clipped taps too)
-          d.x0w = tx0 - mox;
-          d.y0w = ty0 - moy;
-          d.z0w = (tz0 - moz) & ~3;
-          d.tx0 = tx0;
-          d.ty0 = ty0;
-          d.tz0 = tz0;
-          d.beam = bi;
-          d.flags = 0;
-          d.ex = TX + (sxy & 0xffff);
-          d.nyb = 0;
-          d.var = var;
-          d.tb = tbj;
-          d.pad = 0;
-          work += (unsigned long long)(d.b - d.a + 1);
-          if (have) ok = emit(pend);
-          pend = d;
-          have = true;
+      }
+      unsigned act = __ballot_sync(0xffffffffu, r != RANGE_EMPTY);
+      while (act && ok) {
+        const int j = __ffs(act) - 1;
+        act &= act - 1;
+        const uint32_t rj = __shfl_sync(0xffffffffu, r, j), crj = __shfl_sync(0xffffffffu, cr, j);
+        const int cbj = __shfl_sync(0xffffffffu, cb, j), tbj = __shfl_sync(0xffffffffu, tb, j);
+        const int mlo = (int)(rj & 0xffffu), mhi = (int)(rj >> 16);
+        const int c_first = (int)(crj & 0xffffu), c_last = (int)(crj >> 16);
+        for (int c0 = c_first; c0 <= c_last && ok; c0 += 32) {
+          // lanes fetch up to 32 chunk records at once
+          int4 r0 = make_int4(0, 0, 0, 0), r1 = make_int4(0, 0, 0, 0);
+          if (c0 + lane <= c_last) {
+            r0 = __ldg(D.chunk_rec + 2 * (cbj + c0 + lane));
+            r1 = __ldg(D.chunk_rec + 2 * (cbj + c0 + lane) + 1);
+          }
+          const int nrec = min(32, c_last - c0 + 1);
+          for (int q = 0; q < nrec && ok; ++q) {
+            const int a0 = __shfl_sync(0xffffffffu, r0.x, q), b0 = __shfl_sync(0xffffffffu, r0.y, q);
+            const int var = __shfl_sync(0xffffffffu, r0.z, q), sxy = __shfl_sync(0xffffffffu, r0.w, q);
+            const int mox = __shfl_sync(0xffffffffu, r1.x, q), moy = __shfl_sync(0xffffffffu, r1.y, q);
+            const int moz = __shfl_sync(0xffffffffu, r1.z, q);
+            ChunkDesc d;
+            d.u = ub + j;
+            d.a = max(a0, mlo);
+            d.b = min(b0, mhi);
+            // window of the whole chunk (covers the clipped taps too)
+            d.x0w = tx0 - mox;
+            d.y0w = ty0 - moy;
+            d.z0w = (tz0 - moz) & ~3;
+            d.tx0 = tx0;
+            d.ty0 = ty0;
+            d.tz0 = tz0;
+            d.beam = bi;
+            d.flags = 0;
+            d.ex = TX + (sxy & 0xffff);
+            d.nyb = 0;
+            d.var = var;
+            d.tb = tbj;
+            d.pad = 0;
+            work += (unsigned long long)(d.b - d.a + 1);
+            if (have) ok = emit(pend);
+            pend = d;
+            have = true;
+          }
         }
       }
     }

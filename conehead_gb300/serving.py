@@ -240,12 +240,15 @@ class GpuExecutor:
     stencils for the largest grid up front so no request pays for it.
     """
 
-    def __init__(self, device=0, n_slots=2, copy_to_host=True):
+    def __init__(self, device=0, n_slots=2, copy_to_host=True, tuning=None):
         import torch
         from .engine import DoseEngine
         self.torch = torch
         self.device = torch.device("cuda", int(device))
         self.engines = [DoseEngine(device) for _ in range(n_slots)]
+        if tuning:
+            for e in self.engines:
+                e.set_tuning(**tuning)      # the cone/TERMA schedule (conehead_gb300.autotune)
         self.streams = [torch.cuda.Stream(self.device) for _ in range(n_slots)]
         self.events = [None] * n_slots
         self.n_slots = n_slots

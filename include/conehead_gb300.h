@@ -286,7 +286,8 @@ ch_status ch_cone_directions(ch_plan* plan, float* out_dev, void* stream);
 
 /* Schedule of the cone and TERMA passes (results do not depend on it, up
  * to the float order of the dose sums).  dir_group: unique directions per
- * cone work unit, 1..32 (default 16); unit_order: 0 = a tile's direction
+ * cone work unit, 1..1024 (default 16; at least the number of unique
+ * directions makes one unit per tile); unit_order: 0 = a tile's direction
  * groups are consecutive units (default), 1 = a direction group's tiles are;
  * terma_ctas_per_sm: CTAs per SM of the TERMA pass, 1..32 (default 8).
  * Picked per workload by conehead_gb300.autotune. */
