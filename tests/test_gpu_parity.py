@@ -1,7 +1,7 @@
 """GPU parity: the CUDA path (through the C ABI) against the oracle and the
 reference's own goldens.
 
-Bars (north-star): DDA voxel sequences and the geometric intermediates
+Bars (the acceptance bars of this engine): DDA voxel sequences and the geometric intermediates
 (blocked, d_eff, oad, f_soften, f_horn) bit-exact against the float32-
 mirrored oracle / reference; float32 dose within 0.5% of Dmax in every
 voxel above 1% of Dmax against both oracle modes (the observed maximum is
@@ -19,7 +19,7 @@ from conftest import GOLDEN
 
 pytestmark = pytest.mark.gpu
 
-DOSE_BAR = 5e-3          # fraction of Dmax (spec bar)
+DOSE_BAR = 5e-3          # fraction of Dmax: the 0.5% acceptance bar
 DOSE_F32 = 2e-4          # observed-scale bound vs the float32-mirrored oracle
 
 
