@@ -137,9 +137,26 @@ def compare_with_oracle(oracle_lib, source, block, phantom, settings, label, f64
     msg = f"{label}: vs fp32-mirrored oracle {hot32:.2e} of Dmax"
     assert hot32 <= DOSE_F32
     if f64:
+        # The reference computes in float32.  Where a blocking sub-sample lies
+        # within float32 rounding of a block-map cell edge, the FP64 re-run
+        # picks the neighbouring cell, so that voxel's blocked fraction (and
+        # the dose of it and its neighbours) differs by one sub-sample.  The
+        # GPU follows the float32 choice bit-exactly (checked above); the FP64
+        # bar is held everywhere else and the flip voxels are reported.
         ref64 = oracle_lib.calculate(source, block, phantom, settings, oracle_lib.MODE_F64)
-        hot64, all64 = dose_error(out["dose"], ref64["dose"])
-        msg += f", vs FP64 oracle {hot64:.2e} (all voxels {all64:.2e})"
+        flip = ref["blocked"] != ref64["blocked"]
+        near = flip.copy()
+        for ax in range(3):
+            for sh in (-1, 1):
+                near |= np.roll(flip, sh, axis=ax)
+        D = ref64["dose"]
+        hot = (D > 0.01 * D.max()) & ~near
+        err64 = np.abs(out["dose"].astype(np.float64) - D)
+        hot64 = err64[hot].max() / D.max()
+        msg += f", vs FP64 oracle {hot64:.2e} of Dmax (all voxels {err64.max() / D.max():.2e})"
+        if flip.any():
+            msg += (f"; {int(flip.sum())} voxel(s) with a float32/float64 blocking flip, "
+                    f"{err64[near].max() / D.max():.2e} of Dmax there")
         assert hot64 <= DOSE_BAR
     print(msg)
     return out
@@ -173,6 +190,20 @@ def test_config_hetero_128_full_size(eng, settings, oracle_lib):
     src, blk = random_beam(rng, field=5.0)
     compare_with_oracle(oracle_lib, src, blk, slab_phantom(128, 0.25, seed=11), settings,
                         "hetero 128^3 5x5", f64=True)
+
+
+def test_config_large_field_96(eng, settings, oracle_lib):
+    """A large oblique field: 96^3 heterogeneous phantom at 0.25 cm, 15 x 12 cm
+    jaws, gantry 217, collimator 63."""
+    from conehead_gb300 import Block, Source
+    from conehead_gb300.phantoms import slab_phantom
+    src = Source()
+    src.gantry = 217.0
+    src.collimator = 63.0
+    blk = Block()
+    blk.set_rect(-7.5, 7.5, -6.0, 6.0)
+    compare_with_oracle(oracle_lib, src, blk, slab_phantom(96, 0.25, seed=96), settings,
+                        "hetero 96^3 15x12 oblique", f64=True)
 
 
 # ------------------------------------------------------------ paths agree --
