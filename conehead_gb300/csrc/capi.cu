@@ -88,8 +88,18 @@ struct StencilSet {
   int n_raw = 0;             // theta x phi
   size_t total_taps = 0;
   DevBuf tap_base, tap_len, taps, offs, tvals, chunk_base, n_chunks, chunk_start, chunk_rec, dirs;
+  DevBuf runs, run_base, tap_run, run_tap, axis;   // run records of the gather (ConeDirs)
   DevBuf raw_dirs;           // float [n_theta*n_phi][3] as the device computed them
   DevBuf walk_row, walk_mult;  // per unique walk: kernel row (cone polar angle) and multiplicity
+  std::vector<DevBuf*> bufs() {
+    return {&tap_base, &tap_len, &taps, &offs, &tvals, &chunk_base, &n_chunks, &chunk_start, &chunk_rec, &dirs,
+            &runs, &run_base, &tap_run, &run_tap, &axis, &raw_dirs, &walk_row, &walk_mult};
+  }
+  size_t bytes() const {
+    size_t b = 0;
+    for (DevBuf* d : const_cast<StencilSet*>(this)->bufs()) b += d->bytes;
+    return b;
+  }
 };
 
 struct FrameStencils {
@@ -98,9 +108,7 @@ struct FrameStencils {
   uint64_t last_use = 0;
   ~FrameStencils() {
     for (StencilSet* S : {&fwd, &adj})
-      for (DevBuf* b : {&S->tap_base, &S->tap_len, &S->taps, &S->offs, &S->tvals, &S->chunk_base, &S->n_chunks,
-                        &S->chunk_start, &S->chunk_rec, &S->dirs, &S->raw_dirs, &S->walk_row, &S->walk_mult})
-        b->release();
+      for (DevBuf* b : S->bufs()) b->release();
   }
 };
 
@@ -141,9 +149,7 @@ struct ch_plan {
                       &adj_in, &adj_out, &adj_w})
       b->release();
     for (StencilSet* S : {&st, &st_adj})
-      for (DevBuf* b : {&S->tap_base, &S->tap_len, &S->taps, &S->offs, &S->tvals, &S->chunk_base, &S->n_chunks,
-                        &S->chunk_start, &S->chunk_rec, &S->dirs, &S->raw_dirs, &S->walk_row, &S->walk_mult})
-        b->release();
+      for (DevBuf* b : S->bufs()) b->release();
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     for (int i = 0; i < 2; ++i) {
@@ -246,8 +252,34 @@ ch_status assemble_stencils(ch_plan* P, StencilSet& S, int sign, int n_raw, int 
     }
   }
   const int U = (int)uniq_first.size();
-  std::vector<int> tap_base(U), tap_len(U), chunk_base(U), n_chunks(U), chunk_start;
-  std::vector<int4> chunk_rec;
+  // Run axis of each walk: the one of x and y whose runs (consecutive taps
+  // stepping along it, at most RUN_MAX) cost the fewest shared-memory reads
+  // (15 + n line values and one or two record reads per run).  Walks are
+  // ordered x-axis first so that a work unit changes layout at most once.
+  auto split_runs = [&](const short4* o, int L, int ax, std::vector<int>* starts) {
+    long cost = 0;
+    int m = 0;
+    while (m < L) {
+      int n = 1;
+      while (m + n < L && n < RUN_MAX && (&o[m + n].x)[ax] != (&o[m + n - 1].x)[ax]) ++n;
+      if (starts) starts->push_back(m);
+      cost += 15 + n + (n > 2 ? 2 : 1);
+      m += n;
+    }
+    return cost;
+  };
+  std::vector<int> walk_axis(U), order;
+  for (int u = 0; u < U; ++u) {
+    const int d = uniq_first[u];
+    const short4* o = &h_off[(size_t)d * max_len];
+    walk_axis[u] = split_runs(o, h_len[d], 1, nullptr) < split_runs(o, h_len[d], 0, nullptr) ? 1 : 0;
+  }
+  for (int ax = 0; ax < 2; ++ax)
+    for (int u = 0; u < U; ++u)
+      if (walk_axis[u] == ax) order.push_back(u);
+  std::vector<int> tap_base(U), tap_len(U), chunk_base(U), n_chunks(U), chunk_start, run_base(U), axis(U);
+  std::vector<int> umult(U), urow(U), tap_run, run_tap;
+  std::vector<int4> chunk_rec, runs;
   std::vector<int4> taps;
   std::vector<short4> offs;
   std::vector<float> tvals, dirs((size_t)U * 3);
@@ -258,7 +290,7 @@ ch_status assemble_stencils(ch_plan* P, StencilSet& S, int sign, int n_raw, int 
     long best_vol = 0;
     for (int v = 0; v < N_VARIANTS; ++v) {
       if (sx > var_span_x(v) || sy > var_span_y(v) || sz > var_span_z(v)) continue;
-      const long vol = (long)var_p(v) * ((TY + sy + BOX_Y - 1) / BOX_Y * BOX_Y) * (TX + sx);
+      const long vol = (long)var_p(v) * var_rows(v) * (TX + sx);
       if (best < 0 || vol < best_vol) {
         best = v;
         best_vol = vol;
@@ -266,41 +298,77 @@ ch_status assemble_stencils(ch_plan* P, StencilSet& S, int sign, int n_raw, int 
     }
     return best;
   };
+  auto toff = [](const short4& o, int v) { return ((int)o.x * var_rows(v) + (int)o.y) * var_p(v) + (int)o.z; };
   for (int u = 0; u < U; ++u) {
-    const int d = uniq_first[u], L = h_len[d];
+    const int src = order[u];
+    const int d = uniq_first[src], L = h_len[d];
     const short4* o = &h_off[(size_t)d * max_len];
+    const int ax = walk_axis[src];
+    umult[u] = mult[src];
+    urow[u] = d % P->n_phi;
+    axis[u] = ax;
     tap_base[u] = (int)taps.size();
     tap_len[u] = L;
     for (int k = 0; k < 3; ++k) dirs[(size_t)u * 3 + k] = h_dir[(size_t)d * 3 + k];
+    std::vector<float> w(L);
     for (int m = 0; m < L; ++m) {
       int4 t;
       int* tv4 = &t.x;
-      for (int v = 0; v < N_VARIANTS; ++v)
-        tv4[v] = ((int)o[m].x * var_rows(v) + (int)o[m].y) * var_p(v) + (int)o[m].z;
-      const float w = h_dk[(size_t)d * max_len + m] * (float)mult[u];
-      std::memcpy(&t.w, &w, 4);
+      for (int v = 0; v < N_VARIANTS; ++v) tv4[v] = toff(o[m], v);
+      w[m] = h_dk[(size_t)d * max_len + m] * (float)mult[src];
+      std::memcpy(&t.w, &w[m], 4);
       taps.push_back(t);
       offs.push_back(o[m]);
       tvals.push_back(h_t[(size_t)d * max_len + m]);
     }
-    // greedy chunks: grow while some window variant still holds the sources
+    std::vector<int> rs;
+    split_runs(o, L, ax, &rs);
+    const int R = (int)rs.size();
+    rs.push_back(L);
+    // greedy chunks of whole runs: grow while some window variant still holds the sources
     chunk_base[u] = (int)chunk_start.size();
-    int a = 0;
-    while (a < L) {
-      int b = a;
-      while (b + 1 < L && b + 1 - a < MAX_CHUNK_TAPS &&
-             pick_variant(std::abs(o[b + 1].x - o[a].x), std::abs(o[b + 1].y - o[a].y),
-                          std::abs(o[b + 1].z - o[a].z)) >= 0)
-        ++b;
-      chunk_start.push_back(a);
-      const int sx = std::abs(o[b].x - o[a].x), sy = std::abs(o[b].y - o[a].y), sz = std::abs(o[b].z - o[a].z);
-      chunk_rec.push_back(make_int4(a, b, pick_variant(sx, sy, sz), sx | (sy << 16)));
-      chunk_rec.push_back(make_int4(std::max<int>(o[a].x, o[b].x), std::max<int>(o[a].y, o[b].y),
-                                    std::max<int>(o[a].z, o[b].z), 0));
-      a = b + 1;
+    run_base[u] = (int)(runs.size() / RUN_REC_INT4);
+    std::vector<int> run_var(R);
+    int ra = 0;
+    while (ra < R) {
+      int rb = ra;
+      const int a = rs[ra];
+      while (rb + 1 < R && rb + 1 - ra < MAX_CHUNK_RUNS) {
+        const int e = rs[rb + 2] - 1;
+        if (pick_variant(std::abs(o[e].x - o[a].x), std::abs(o[e].y - o[a].y), std::abs(o[e].z - o[a].z)) < 0) break;
+        ++rb;
+      }
+      const int e = rs[rb + 1] - 1;
+      const int sx = std::abs(o[e].x - o[a].x), sy = std::abs(o[e].y - o[a].y), sz = std::abs(o[e].z - o[a].z);
+      const int var = pick_variant(sx, sy, sz);
+      chunk_start.push_back(ra);
+      chunk_rec.push_back(make_int4(ra, rb, var, sx | (sy << 16)));
+      chunk_rec.push_back(make_int4(std::max<int>(o[a].x, o[e].x), std::max<int>(o[a].y, o[e].y),
+                                    std::max<int>(o[a].z, o[e].z), 0));
+      for (int r = ra; r <= rb; ++r) run_var[r] = var;
+      ra = rb + 1;
     }
     n_chunks[u] = (int)chunk_start.size() - chunk_base[u];
+    // run records: the base is the run's tap furthest along the axis, and
+    // the tap c steps behind it takes weight slot c (it reads line value i + c)
+    for (int r = 0; r < R; ++r) {
+      const int m0 = rs[r], n = rs[r + 1] - rs[r];
+      const int g = (int)(runs.size() / RUN_REC_INT4);
+      int mb = m0;
+      for (int m = m0; m < m0 + n; ++m)
+        if ((&o[m].x)[ax] > (&o[mb].x)[ax]) mb = m;
+      int words[8] = {toff(o[mb], run_var[r]), n, 0, 0, 0, 0, 0, 0};
+      for (int m = m0; m < m0 + n; ++m) {
+        const int c = (&o[mb].x)[ax] - (&o[m].x)[ax];
+        std::memcpy(&words[2 + c], &w[m], 4);
+        tap_run.push_back(g * 8 + 2 + c);
+      }
+      runs.push_back(make_int4(words[0], words[1], words[2], words[3]));
+      runs.push_back(make_int4(words[4], words[5], words[6], words[7]));
+      run_tap.push_back(tap_base[u] + m0);
+    }
   }
+  run_tap.push_back((int)taps.size());
   auto up = [&](DevBuf& b, const void* h, size_t n) -> cudaError_t {
     cudaError_t e = b.ensure(std::max<size_t>(n, 16));
     if (e != cudaSuccess) return e;
@@ -311,15 +379,18 @@ ch_status assemble_stencils(ch_plan* P, StencilSet& S, int sign, int n_raw, int 
   CH_CUDA(up(S.taps, taps.data(), taps.size() * sizeof(int4)));
   CH_CUDA(up(S.offs, offs.data(), offs.size() * sizeof(short4)));
   CH_CUDA(up(S.tvals, tvals.data(), tvals.size() * sizeof(float)));
+  CH_CUDA(up(S.runs, runs.data(), runs.size() * sizeof(int4)));
+  CH_CUDA(up(S.run_base, run_base.data(), run_base.size() * sizeof(int)));
+  CH_CUDA(up(S.tap_run, tap_run.data(), tap_run.size() * sizeof(int)));
+  CH_CUDA(up(S.run_tap, run_tap.data(), run_tap.size() * sizeof(int)));
+  CH_CUDA(up(S.axis, axis.data(), axis.size() * sizeof(int)));
   CH_CUDA(up(S.chunk_base, chunk_base.data(), chunk_base.size() * sizeof(int)));
   CH_CUDA(up(S.n_chunks, n_chunks.data(), n_chunks.size() * sizeof(int)));
   CH_CUDA(up(S.chunk_start, chunk_start.data(), chunk_start.size() * sizeof(int)));
   CH_CUDA(up(S.chunk_rec, chunk_rec.data(), chunk_rec.size() * sizeof(int4)));
   CH_CUDA(up(S.dirs, dirs.data(), dirs.size() * sizeof(float)));
-  std::vector<int> walk_row(U);
-  for (int u = 0; u < U; ++u) walk_row[u] = uniq_first[u] % P->n_phi;
-  CH_CUDA(up(S.walk_row, walk_row.data(), walk_row.size() * sizeof(int)));
-  CH_CUDA(up(S.walk_mult, mult.data(), mult.size() * sizeof(int)));
+  CH_CUDA(up(S.walk_row, urow.data(), urow.size() * sizeof(int)));
+  CH_CUDA(up(S.walk_mult, umult.data(), umult.size() * sizeof(int)));
   CH_CUDA(cudaStreamSynchronize(s));
   S.valid = true;
   S.n_dirs = U;
@@ -393,6 +464,11 @@ ConeDirs cone_dirs(const StencilSet& S, const ch_tuning& t) {
   D.taps = S.taps.as<int4>();
   D.offs = S.offs.as<short4>();
   D.tvals = S.tvals.as<float>();
+  D.runs = S.runs.as<int4>();
+  D.run_base = S.run_base.as<int>();
+  D.tap_run = S.tap_run.as<int>();
+  D.run_tap = S.run_tap.as<int>();
+  D.axis = S.axis.as<int>();
   D.chunk_base = S.chunk_base.as<int>();
   D.n_chunks = S.n_chunks.as<int>();
   D.chunk_start = S.chunk_start.as<int>();
@@ -1033,7 +1109,7 @@ ch_status ch_plan_set_kernel(ch_plan* P, const ch_kernel* k) {
       if (!S->valid) continue;
       launch_reweight(P->K.as<double>(), P->n_r, S->n_dirs, S->tap_base.as<int>(), S->tap_len.as<int>(),
                       S->tvals.as<float>(), S->walk_row.as<int>(), S->walk_mult.as<int>(), S->taps.as<int4>(),
-                      nullptr);
+                      S->tap_run.as<int>(), S->runs.as<int4>(), nullptr);
       CH_CUDA(cudaGetLastError());
     }
     CH_CUDA(cudaStreamSynchronize(nullptr));
@@ -1552,16 +1628,9 @@ ch_status ch_plan_prepare(ch_plan* P, const ch_grid* grid, void* stream) {
 ch_status ch_plan_memory(ch_plan* P, size_t* tables, size_t* scratch) {
   if (!P) return fail(CH_ERR_INVALID_ARG, "plan is NULL");
   size_t b = P->K.bytes + P->theta.bytes + P->phi.bytes;
-  for (const StencilSet* S : {&P->st, &P->st_adj})
-    for (const DevBuf* d : {&S->tap_base, &S->tap_len, &S->taps, &S->offs, &S->tvals, &S->chunk_base, &S->n_chunks,
-                            &S->chunk_start, &S->chunk_rec, &S->dirs, &S->raw_dirs, &S->walk_row, &S->walk_mult})
-      b += d->bytes;
+  for (const StencilSet* S : {&P->st, &P->st_adj}) b += S->bytes();
   for (const auto& f : P->frames)
-    for (const StencilSet* S : {&f->fwd, &f->adj})
-      for (const DevBuf* d : {&S->tap_base, &S->tap_len, &S->taps, &S->offs, &S->tvals, &S->chunk_base,
-                              &S->n_chunks, &S->chunk_start, &S->chunk_rec, &S->dirs, &S->raw_dirs, &S->walk_row,
-                              &S->walk_mult})
-        b += d->bytes;
+    for (const StencilSet* S : {&f->fwd, &f->adj}) b += S->bytes();
   size_t a = P->adj_in.bytes + P->adj_out.bytes + P->adj_w.bytes;
   for (int k = 0; k < 8; ++k) a += scratch_bufs(P, k)->bytes;
   if (tables) *tables = b;

@@ -10,28 +10,42 @@
 namespace ch {
 
 // ------------------------------------------------------------------ sizes --
-// Cone gather tile: 16 (x) x 16 (y) x 16 (z) outputs.  Half a warp covers 16
-// consecutive z of one y row, the other half the same z two rows further
-// (y + 2); each thread holds the 16 x values of its (y, z) column in
-// registers; 8 consumer warps cover the 16 y rows.
+// Cone gather tile: 16 (x) x 16 (y) x 16 (z) outputs.  The 16 outputs of a
+// tile line along the "run axis" of the walks being summed (x or y, chosen
+// per walk on the host) are split between OUT_SPLIT consumer warps, each
+// thread holding 16 / OUT_SPLIT of them in registers:
+//   run axis x: half a warp covers 16 consecutive z of one y row, the other
+//     half the same z two rows further (y + 2); 8 warps cover the 16 rows;
+//   run axis y: half a warp covers 16 consecutive z of one x slice, the other
+//     half the next slice (x + 1); 8 warps cover the 16 slices.
+// More warps hide more shared-memory latency; every warp reads the run
+// records and its own line ends.
 constexpr int TZ = 16, TY = 16, TX = 16;
 constexpr int TILE_VOX = TZ * TY * TX;
-// the tile's 16 x outputs may be split between X_SPLIT consumer warps (more
-// warps per SM to hide shared-memory latency, but every warp fetches the taps
-// itself); measured at 128^3, 1 is faster (33.3 vs 35.3 ms per 16 beams)
-#ifndef CH_X_SPLIT
-#define CH_X_SPLIT 1
+#ifndef CH_OUT_SPLIT
+#define CH_OUT_SPLIT 2
 #endif
-constexpr int X_SPLIT = CH_X_SPLIT;
-constexpr int OUT_PER_THREAD = TX / X_SPLIT;
+constexpr int OUT_SPLIT = CH_OUT_SPLIT;
+constexpr int OUT_PER_THREAD = 16 / OUT_SPLIT;
+// A run is up to RUN_MAX consecutive taps of one walk whose steps all lie
+// along the walk's run axis: its n taps read one line of 15 + n window values
+// along that axis, so a thread loads each value once for up to n taps.
+constexpr int RUN_MAX = 4;
 // Shared-memory window of a chunk: [x][row][z] with z pitch P and `rows` y
-// rows per x slice.  Three shapes ("variants") trade z reach for x reach in
-// one fixed slot; the chunker picks the cheapest that holds the chunk.  Every
-// P is 8 mod 16, so the two half-warps (rows y and y + 2, 2P = 16 mod 32) hit
-// disjoint banks.  The TMA box of variant v is P x 8 x 1 floats.
+// rows per x slice.  Three shapes ("variants") trade z reach for x and y reach
+// in one fixed slot; the chunker picks the cheapest that holds the chunk.
+// Every P is 8 mod 16, so 2P = 16 mod 32: the half-warps of the x layout
+// (rows y and y + 2) hit disjoint banks.  Every `rows` is 2 mod 4, so the
+// slice pitch rows * P is 16 mod 32: the half-warps of the y layout (slices x
+// and x + 1) hit disjoint banks too.
 constexpr int N_VARIANTS = 3;
 __host__ __device__ constexpr int var_p(int v) { return v == 0 ? 24 : (v == 1 ? 40 : 56); }
-__host__ __device__ constexpr int var_rows(int v) { return v == 0 ? 32 : 24; }
+__host__ __device__ constexpr int var_rows(int v) { return v == 0 ? 34 : (v == 1 ? 26 : 22); }
+static_assert((2 * var_p(0)) % 32 == 16 && (2 * var_p(1)) % 32 == 16 && (2 * var_p(2)) % 32 == 16,
+              "x layout: rows y and y + 2 must fall in disjoint banks");
+static_assert((var_rows(0) * var_p(0)) % 32 == 16 && (var_rows(1) * var_p(1)) % 32 == 16 &&
+                  (var_rows(2) * var_p(2)) % 32 == 16,
+              "y layout: slices x and x + 1 must fall in disjoint banks");
 constexpr int WIN_FLOATS = 27648;     // one pipeline slot (108 KiB)
 __host__ __device__ constexpr int var_max_ex(int v) { return WIN_FLOATS / (var_p(v) * var_rows(v)); }
 // largest tap-offset spread a chunk may have along each axis in variant v
@@ -39,7 +53,6 @@ __host__ __device__ constexpr int var_max_ex(int v) { return WIN_FLOATS / (var_p
 __host__ __device__ constexpr int var_span_z(int v) { return var_p(v) - TZ - 3; }
 __host__ __device__ constexpr int var_span_y(int v) { return var_rows(v) - TY; }
 __host__ __device__ constexpr int var_span_x(int v) { return var_max_ex(v) - TX; }
-constexpr int BOX_Y = 8;              // granularity of the y extent in the chunker
 // One TMA box loads a chunk's whole window: P x rows x ex floats, so every
 // (variant, x extent) pair has its own tensor map.
 __host__ __device__ constexpr int n_maps_before(int v) {
@@ -47,9 +60,14 @@ __host__ __device__ constexpr int n_maps_before(int v) {
 }
 constexpr int N_TMAPS = n_maps_before(2) + (var_max_ex(2) - TX + 1);
 __host__ __device__ constexpr int tmap_index(int v, int ex) { return n_maps_before(v) + (ex - TX); }
-constexpr int MAX_CHUNK_TAPS = 64;    // taps per chunk (their table is staged with the window)
+// Run record, two int4: {window offset of the run's base in its chunk's
+// variant, n, w0, w1} and {w2, w3, 0, 0} (float bits).  The base is the tap
+// furthest along the run axis; weight slot c belongs to the tap c steps
+// behind it, which reads line value i + c for output i.
+constexpr int RUN_REC_INT4 = 2;
+constexpr int MAX_CHUNK_RUNS = 64;    // runs per chunk (their records are staged with the window)
 constexpr int N_SLOTS = 2;
-constexpr int CONE_CONSUMER_WARPS = (TY / 2) * X_SPLIT;
+constexpr int CONE_CONSUMER_WARPS = (TY / 2) * OUT_SPLIT;
 constexpr int CONE_THREADS = (CONE_CONSUMER_WARPS + 1) * 32;
 constexpr int DIR_GROUP = 16;         // unique directions per work unit (default; ch_tuning.dir_group)
 constexpr int MAX_DIR_GROUP = 1024;   // the producer walks a unit's directions 32 at a time
@@ -161,14 +179,19 @@ struct ConeDirs {
   int n_dirs;
   const int* tap_base;
   const int* tap_len;
-  const int4* taps;        // window offset of O[m] in variants 0..2, float bits of w[m]
+  const int4* taps;        // window offset of O[m] in variants 0..2, float bits of w[m] (scatter path)
   const short4* offs;      // O[m] (x, y, z, step axis)
   const float* tvals;      // exit t of tap m
+  const int4* runs;        // RUN_REC_INT4 per run, the runs of all walks back to back
+  const int* run_base;     // first run of each walk
+  const int* tap_run;      // per tap: its global run index * 8 + 2 + its weight slot (the word of its weight)
+  const int* run_tap;      // per run: global index of its first tap (one trailing entry)
+  const int* axis;         // per walk: run axis, 0 = x, 1 = y
   const int* chunk_base;
   const int* n_chunks;
-  const int* chunk_start;  // first tap of each chunk (direction-local)
-  const int4* chunk_rec;   // 2 per chunk: {first, last, variant, span_x | span_y << 16},
-                           //              {max O_x, max O_y, max O_z, 0} over the chunk
+  const int* chunk_start;  // first run of each chunk (walk-local)
+  const int4* chunk_rec;   // 2 per chunk: {first run, last run, variant, span_x | span_y << 16},
+                           //              {max O_x, max O_y, max O_z, 0} over the chunk's taps
   const float* dirs;       // unit direction (x, y, z)
   int group;               // unique directions per work unit (1..MAX_DIR_GROUP)
   int order;               // units: 0 = tile outer, group inner; 1 = group outer, tile inner
@@ -185,8 +208,8 @@ struct RangeBeam {
   int n_out_planes;         // output tiles wholly outside one of these planes
   float opa[4][3];          // (the beam frustum, for the transposed cone of
   float opk0[4];            // the adjoint) get no taps either
-  uint32_t* ranges;        // [n_tiles][n_dirs]: first | last tap << 16, or RANGE_EMPTY
-  uint32_t* cranges;       // [n_tiles][n_dirs]: first | last chunk << 16 (direction-local)
+  uint32_t* ranges;        // [n_tiles][n_dirs]: first | last run << 16 (walk-local), or RANGE_EMPTY
+  uint32_t* cranges;       // [n_tiles][n_dirs]: first | last chunk << 16 (walk-local)
 };
 
 // Regular beamlet grid on the block map: beamlet (i, j) covers map rows
@@ -219,7 +242,8 @@ void launch_scatter_radiological(const float* T, const float* rho, const int* n,
                                  const int* walk_row, const int* walk_mult, const double* K, int n_r, float* dose,
                                  cudaStream_t st);
 void launch_reweight(const double* K, int n_r, int n_walks, const int* tap_base, const int* tap_len,
-                     const float* tvals, const int* walk_row, const int* walk_mult, int4* taps, cudaStream_t st);
+                     const float* tvals, const int* walk_row, const int* walk_mult, int4* taps, const int* tap_run,
+                     int4* runs, cudaStream_t st);
 void launch_dda_trace(const int* n, const float* sp, int n_rays, const int* starts, const float* dirs, int cap,
                       int* vox, float* t, int* len, cudaStream_t st);
 void launch_scatter(const float* T, const int* n, int zp, int n_dirs, const int* tap_base, const int* tap_len,

@@ -38,12 +38,14 @@ namespace ch {
 constexpr long long MBAR_LIMIT = 1ll << 22;
 constexpr int DESC_LAST = 1, DESC_DONE = 2;
 
+// one chunk as the producer hands it to the consumers: runs a..b of walk u
+// (walk-local; tb = the walk's first run), its window origin and shape
 struct __align__(16) ChunkDesc {
   int u, a, b;
   int x0w, y0w, z0w;
   int tx0, ty0, tz0;
   int beam, flags, ex;
-  int nyb, var, tb, pad;
+  int axis, var, tb, pad;
 };
 
 // ------------------------------------------------------------- PTX glue --
@@ -196,13 +198,17 @@ __global__ void range_kernel(const RangeBeam* __restrict__ rbs, ConeDirs D) {
       }
     }
     if (mlo <= mhi) {
-      out = (uint32_t)mlo | ((uint32_t)mhi << 16);
-      // chunks holding the first and last tap
+      // runs holding the first and last tap (whole runs are applied: their
+      // other taps read zero TERMA)
+      const int rb = D.run_base[u];
+      const int rlo = (D.tap_run[base + mlo] >> 3) - rb, rhi = (D.tap_run[base + mhi] >> 3) - rb;
+      out = (uint32_t)rlo | ((uint32_t)rhi << 16);
+      // chunks holding them
       const int* cs = D.chunk_start + D.chunk_base[u];
       const int nc = D.n_chunks[u];
       auto ckey = [&](int c) { return (float)cs[c]; };
-      const int c_first = upper_bound(nc, (float)mlo, ckey) - 1;
-      const int c_last = upper_bound(nc, (float)mhi, ckey) - 1;
+      const int c_first = upper_bound(nc, (float)rlo, ckey) - 1;
+      const int c_last = upper_bound(nc, (float)rhi, ckey) - 1;
       R.cranges[(long long)tile * D.n_dirs + u] = (uint32_t)c_first | ((uint32_t)c_last << 16);
     }
   }
@@ -212,7 +218,7 @@ __global__ void range_kernel(const RangeBeam* __restrict__ rbs, ConeDirs D) {
 // --------------------------------------------------------- gather pass --
 __device__ __forceinline__ void producer(const ConeBeam* __restrict__ beams, int n_beams, const ConeDirs& D,
                                          int total_units, int* unit_counter, unsigned long long* updates,
-                                         int* flags, float* win, int4* slot_taps, ChunkDesc* desc,
+                                         int* flags, float* win, int4* slot_runs, ChunkDesc* desc,
                                          uint64_t* full, uint64_t* empty) {
   const int lane = threadIdx.x & 31;
   const int n_groups = (D.n_dirs + D.group - 1) / D.group;
@@ -225,16 +231,17 @@ __device__ __forceinline__ void producer(const ConeBeam* __restrict__ beams, int
     const uint32_t ph = (uint32_t)(k / N_SLOTS) & 1u;
     if (!mbar_wait(&empty[s], ph ^ 1u)) return false;
     const bool done = (d.flags & DESC_DONE) != 0;
-    const uint32_t tap_bytes = done ? 0u : (uint32_t)(d.b - d.a + 1) * (uint32_t)sizeof(int4);
+    const uint32_t run_bytes = done ? 0u : (uint32_t)(d.b - d.a + 1) * (uint32_t)(RUN_REC_INT4 * sizeof(int4));
     const uint32_t win_bytes = done ? 0u : (uint32_t)(var_p(d.var) * var_rows(d.var) * d.ex * 4);
     if (lane == 0) {
       desc[s] = d;
-      mbar_arrive_expect_tx(&full[s], win_bytes + tap_bytes);
+      mbar_arrive_expect_tx(&full[s], win_bytes + run_bytes);
       if (!done) {
-        // the whole window in one TMA box, the chunk's taps in one bulk copy
+        // the whole window in one TMA box, the chunk's run records in one bulk copy
         tma_load_3d(win + (size_t)s * WIN_FLOATS, &beams[d.beam].tmap[tmap_index(d.var, d.ex)], &full[s], d.z0w,
                     d.y0w, d.x0w);
-        bulk_load(slot_taps + (size_t)s * MAX_CHUNK_TAPS, D.taps + d.tb + d.a, tap_bytes, &full[s]);
+        bulk_load(slot_runs + (size_t)s * MAX_CHUNK_RUNS * RUN_REC_INT4, D.runs + (size_t)(d.tb + d.a) * RUN_REC_INT4,
+                  run_bytes, &full[s]);
       }
     }
     __syncwarp();
@@ -261,61 +268,84 @@ __device__ __forceinline__ void producer(const ConeBeam* __restrict__ beams, int
     const int u_end = min(u0 + D.group, D.n_dirs);
     unsigned long long work = 0;
     for (int ub = u0; ub < u_end && ok; ub += 32) {
+      // lanes fetch, for their walks in parallel, the run and chunk ranges,
+      // the first chunk's record (most ranges lie in one chunk) and the tap
+      // count, so the serial loop below rarely waits on global memory
       uint32_t r = RANGE_EMPTY, cr = 0;
-      int cb = 0, tb = 0;
+      int cb = 0, tb = 0, ax = 0;
+      int4 f0 = make_int4(0, 0, 0, 0), f1 = make_int4(0, 0, 0, 0);
+      unsigned taps = 0;
       if (ub + lane < u_end) {
         const long long ri = (long long)tile * D.n_dirs + ub + lane;
         r = __ldg(B.ranges + ri);
         if (r != RANGE_EMPTY) {
           cr = __ldg(B.cranges + ri);
           cb = __ldg(D.chunk_base + ub + lane);
-          tb = __ldg(D.tap_base + ub + lane);
+          tb = __ldg(D.run_base + ub + lane);
+          ax = __ldg(D.axis + ub + lane);
+          const int cf = cb + (int)(cr & 0xffffu);
+          f0 = __ldg(D.chunk_rec + 2 * cf);
+          f1 = __ldg(D.chunk_rec + 2 * cf + 1);
+          // runs rlo..rhi hold these taps
+          taps = (unsigned)(__ldg(D.run_tap + tb + (int)(r >> 16) + 1) - __ldg(D.run_tap + tb + (int)(r & 0xffffu)));
         }
       }
+      work += __reduce_add_sync(0xffffffffu, taps);
       unsigned act = __ballot_sync(0xffffffffu, r != RANGE_EMPTY);
       while (act && ok) {
         const int j = __ffs(act) - 1;
         act &= act - 1;
         const uint32_t rj = __shfl_sync(0xffffffffu, r, j), crj = __shfl_sync(0xffffffffu, cr, j);
         const int cbj = __shfl_sync(0xffffffffu, cb, j), tbj = __shfl_sync(0xffffffffu, tb, j);
-        const int mlo = (int)(rj & 0xffffu), mhi = (int)(rj >> 16);
+        const int axj = __shfl_sync(0xffffffffu, ax, j);
+        const int rlo = (int)(rj & 0xffffu), rhi = (int)(rj >> 16);
         const int c_first = (int)(crj & 0xffffu), c_last = (int)(crj >> 16);
-        for (int c0 = c_first; c0 <= c_last && ok; c0 += 32) {
-          // lanes fetch up to 32 chunk records at once
+        // one chunk {first run, last run, variant, spans}, {max O} -> descriptor
+        auto add_chunk = [&](int4 r0, int4 r1) {
+          ChunkDesc d;
+          d.u = ub + j;
+          d.a = max(r0.x, rlo);
+          d.b = min(r0.y, rhi);
+          // window of the whole chunk (covers the clipped runs too)
+          d.x0w = tx0 - r1.x;
+          d.y0w = ty0 - r1.y;
+          d.z0w = (tz0 - r1.z) & ~3;
+          d.tx0 = tx0;
+          d.ty0 = ty0;
+          d.tz0 = tz0;
+          d.beam = bi;
+          d.flags = 0;
+          d.ex = TX + (r0.w & 0xffff);
+          d.axis = axj;
+          d.var = r0.z;
+          d.tb = tbj;
+          d.pad = 0;
+          if (have) {
+            // the consumers change their output layout with the run axis:
+            // they flush the sums of the walks before the change
+            if (pend.axis != d.axis) pend.flags |= DESC_LAST;
+            ok = emit(pend);
+          }
+          pend = d;
+          have = true;
+        };
+        add_chunk(make_int4(__shfl_sync(0xffffffffu, f0.x, j), __shfl_sync(0xffffffffu, f0.y, j),
+                            __shfl_sync(0xffffffffu, f0.z, j), __shfl_sync(0xffffffffu, f0.w, j)),
+                  make_int4(__shfl_sync(0xffffffffu, f1.x, j), __shfl_sync(0xffffffffu, f1.y, j),
+                            __shfl_sync(0xffffffffu, f1.z, j), 0));
+        for (int c0 = c_first + 1; c0 <= c_last && ok; c0 += 32) {
+          // lanes fetch up to 32 further chunk records at once
           int4 r0 = make_int4(0, 0, 0, 0), r1 = make_int4(0, 0, 0, 0);
           if (c0 + lane <= c_last) {
             r0 = __ldg(D.chunk_rec + 2 * (cbj + c0 + lane));
             r1 = __ldg(D.chunk_rec + 2 * (cbj + c0 + lane) + 1);
           }
           const int nrec = min(32, c_last - c0 + 1);
-          for (int q = 0; q < nrec && ok; ++q) {
-            const int a0 = __shfl_sync(0xffffffffu, r0.x, q), b0 = __shfl_sync(0xffffffffu, r0.y, q);
-            const int var = __shfl_sync(0xffffffffu, r0.z, q), sxy = __shfl_sync(0xffffffffu, r0.w, q);
-            const int mox = __shfl_sync(0xffffffffu, r1.x, q), moy = __shfl_sync(0xffffffffu, r1.y, q);
-            const int moz = __shfl_sync(0xffffffffu, r1.z, q);
-            ChunkDesc d;
-            d.u = ub + j;
-            d.a = max(a0, mlo);
-            d.b = min(b0, mhi);
-            // window of the whole chunk (covers the clipped taps too)
-            d.x0w = tx0 - mox;
-            d.y0w = ty0 - moy;
-            d.z0w = (tz0 - moz) & ~3;
-            d.tx0 = tx0;
-            d.ty0 = ty0;
-            d.tz0 = tz0;
-            d.beam = bi;
-            d.flags = 0;
-            d.ex = TX + (sxy & 0xffff);
-            d.nyb = 0;
-            d.var = var;
-            d.tb = tbj;
-            d.pad = 0;
-            work += (unsigned long long)(d.b - d.a + 1);
-            if (have) ok = emit(pend);
-            pend = d;
-            have = true;
-          }
+          for (int q = 0; q < nrec && ok; ++q)
+            add_chunk(make_int4(__shfl_sync(0xffffffffu, r0.x, q), __shfl_sync(0xffffffffu, r0.y, q),
+                                __shfl_sync(0xffffffffu, r0.z, q), __shfl_sync(0xffffffffu, r0.w, q)),
+                      make_int4(__shfl_sync(0xffffffffu, r1.x, q), __shfl_sync(0xffffffffu, r1.y, q),
+                                __shfl_sync(0xffffffffu, r1.z, q), 0));
         }
       }
     }
@@ -338,34 +368,56 @@ __device__ __forceinline__ void producer(const ConeBeam* __restrict__ beams, int
   }
 }
 
-// One chunk of taps for one thread: 16 outputs (x = 0..15) of its (y, z)
-// column; window variant V fixes the pitches at compile time.
-template <int V>
-__device__ __forceinline__ void consume_chunk(const float* w, const int4* tp, int n_taps, int base0, float* acc) {
-  constexpr int XS = var_rows(V) * var_p(V);
-  // the chunk's taps sit in shared memory next to its window; the next one
-  // is read an iteration ahead
-  int4 next = tp[0];
-  for (int m = 0; m < n_taps; ++m) {
-    const int4 tap = next;
-    if (m + 1 < n_taps) next = tp[m + 1];
-    const int toff = V == 0 ? tap.x : (V == 1 ? tap.y : tap.z);
-    const float wt = __int_as_float(tap.w);
-    const float* src = w + (base0 - toff);
+// One run of N taps for one thread: the OUT_PER_THREAD - 1 + N window values
+// of its line along the run axis (stride S floats), then OUT_PER_THREAD * N
+// FMAs from registers.
+template <int S, int N>
+__device__ __forceinline__ void apply_run(const float* src, const float (&wt)[RUN_MAX], float* acc) {
+  float line[OUT_PER_THREAD - 1 + N];
 #pragma unroll
-    for (int i = 0; i < OUT_PER_THREAD; ++i) acc[i] = fmaf(wt, src[i * XS], acc[i]);
+  for (int k = 0; k < OUT_PER_THREAD - 1 + N; ++k) line[k] = src[k * S];
+#pragma unroll
+  for (int j = 0; j < N; ++j)
+#pragma unroll
+    for (int i = 0; i < OUT_PER_THREAD; ++i) acc[i] = fmaf(wt[j], line[i + j], acc[i]);
+}
+
+// One chunk of runs for one thread: 16 outputs along run axis AX in window
+// variant V (pitches fixed at compile time).  The records sit in shared
+// memory next to the window; the next run's first half is read a run ahead,
+// the second half (weights 2 and 3) only for runs of more than 2 taps.
+template <int V, int AX>
+__device__ __forceinline__ void consume_chunk(const float* w, const int4* rp, int n_runs, int base0, float* acc) {
+  constexpr int S = AX == 0 ? var_rows(V) * var_p(V) : var_p(V);
+  int4 next = rp[0];
+  for (int r = 0; r < n_runs; ++r) {
+    const int4 h = next;
+    if (r + 1 < n_runs) next = rp[RUN_REC_INT4 * (r + 1)];
+    const float* src = w + (base0 - h.x);
+    float wt[RUN_MAX] = {__int_as_float(h.z), __int_as_float(h.w), 0.0f, 0.0f};
+    if (h.y <= 2) {
+      if (h.y == 1) apply_run<S, 1>(src, wt, acc);
+      else apply_run<S, 2>(src, wt, acc);
+    } else {
+      const int4 t = rp[RUN_REC_INT4 * r + 1];
+      wt[2] = __int_as_float(t.x);
+      wt[3] = __int_as_float(t.y);
+      if (h.y == 3) apply_run<S, 3>(src, wt, acc);
+      else apply_run<S, 4>(src, wt, acc);
+    }
   }
 }
 
 __device__ __forceinline__ void consumer(const ConeBeam* __restrict__ beams, const ConeDirs& D, int* flags,
-                                         const float* win, const int4* slot_taps, const ChunkDesc* desc,
+                                         const float* win, const int4* slot_runs, const ChunkDesc* desc,
                                          uint64_t* full, uint64_t* empty) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rw = warp % (TY / 2);                                // row pair of this warp
-  const int xo = (warp / (TY / 2)) * OUT_PER_THREAD;             // first x of this warp
-  const int zl = lane & 15;                                      // z within the tile
-  const int yl = (rw & 1) + 4 * (rw >> 1) + 2 * (lane >> 4);     // y within the tile
-  float acc[OUT_PER_THREAD];                                     // x = xo .. xo + OUT_PER_THREAD - 1
+  const int wl = warp % (TY / 2);                                  // line pair of this warp
+  const int first = (warp / (TY / 2)) * OUT_PER_THREAD;            // first output along the run axis
+  const int zl = lane & 15;                                        // z within the tile
+  const int row = (wl & 1) + 4 * (wl >> 1) + 2 * (lane >> 4);      // run axis x: this thread's y row
+  const int slice = 2 * wl + (lane >> 4);                          // run axis y: this thread's x slice
+  float acc[OUT_PER_THREAD];                                       // outputs first.. along the run axis
 #pragma unroll
   for (int i = 0; i < OUT_PER_THREAD; ++i) acc[i] = 0.0f;
   for (int k = 0;; ++k) {
@@ -377,24 +429,33 @@ __device__ __forceinline__ void consumer(const ConeBeam* __restrict__ beams, con
     const ChunkDesc d = desc[s];
     if (d.flags & DESC_DONE) break;
     const float* w = win + (size_t)s * WIN_FLOATS;
-    const int4* tp = slot_taps + (size_t)s * MAX_CHUNK_TAPS;
-    const int nt = d.b - d.a + 1;
+    const int4* rp = slot_runs + (size_t)s * MAX_CHUNK_RUNS * RUN_REC_INT4;
+    const int nr = d.b - d.a + 1;
     const int rows = var_rows(d.var), P = var_p(d.var);
-    const int base0 = ((d.tx0 + xo - d.x0w) * rows + (d.ty0 + yl - d.y0w)) * P + (d.tz0 + zl - d.z0w);
-    if (d.var == 0) consume_chunk<0>(w, tp, nt, base0, acc);
-    else if (d.var == 1) consume_chunk<1>(w, tp, nt, base0, acc);
-    else consume_chunk<2>(w, tp, nt, base0, acc);
+    const int xl = d.axis == 0 ? first : slice, yl = d.axis == 0 ? row : first;
+    const int base0 = ((d.tx0 + xl - d.x0w) * rows + (d.ty0 + yl - d.y0w)) * P + (d.tz0 + zl - d.z0w);
+    if (d.axis == 0) {
+      if (d.var == 0) consume_chunk<0, 0>(w, rp, nr, base0, acc);
+      else if (d.var == 1) consume_chunk<1, 0>(w, rp, nr, base0, acc);
+      else consume_chunk<2, 0>(w, rp, nr, base0, acc);
+    } else {
+      if (d.var == 0) consume_chunk<0, 1>(w, rp, nr, base0, acc);
+      else if (d.var == 1) consume_chunk<1, 1>(w, rp, nr, base0, acc);
+      else consume_chunk<2, 1>(w, rp, nr, base0, acc);
+    }
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
     if (d.flags & DESC_LAST) {
       const ConeBeam& B = beams[d.beam];
-      const int y = d.ty0 + yl, z = d.tz0 + zl;
-      if (y < B.n[1] && z < B.n[2]) {
-        float* out = B.dose + ((long long)(d.tx0 + xo) * B.n[1] + y) * B.n[2] + z;
-        const long long xs = (long long)B.n[1] * B.n[2];
+      const int x = d.tx0 + xl, y = d.ty0 + yl, z = d.tz0 + zl;
+      const long long xs = (long long)B.n[1] * B.n[2];
+      const long long step = d.axis == 0 ? xs : (long long)B.n[2];
+      const int lim = d.axis == 0 ? B.n[0] - x : B.n[1] - y;        // outputs inside the grid
+      if (x < B.n[0] && y < B.n[1] && z < B.n[2]) {
+        float* out = B.dose + ((long long)x * B.n[1] + y) * B.n[2] + z;
 #pragma unroll
         for (int i = 0; i < OUT_PER_THREAD; ++i)
-          if (d.tx0 + xo + i < B.n[0]) atomicAdd(out + i * xs, acc[i]);
+          if (i < lim) atomicAdd(out + i * step, acc[i]);
       }
 #pragma unroll
       for (int i = 0; i < OUT_PER_THREAD; ++i) acc[i] = 0.0f;
@@ -410,8 +471,8 @@ __global__ void __launch_bounds__(CONE_THREADS, 1)
   const uint32_t base = smem_u32(smem_raw);
   unsigned char* sm = smem_raw + ((1024u - (base & 1023u)) & 1023u);
   float* win = reinterpret_cast<float*>(sm);
-  int4* slot_taps = reinterpret_cast<int4*>(sm + (size_t)N_SLOTS * WIN_FLOATS * 4);
-  ChunkDesc* desc = reinterpret_cast<ChunkDesc*>(slot_taps + N_SLOTS * MAX_CHUNK_TAPS);
+  int4* slot_runs = reinterpret_cast<int4*>(sm + (size_t)N_SLOTS * WIN_FLOATS * 4);
+  ChunkDesc* desc = reinterpret_cast<ChunkDesc*>(slot_runs + N_SLOTS * MAX_CHUNK_RUNS * RUN_REC_INT4);
   uint64_t* full = reinterpret_cast<uint64_t*>(desc + N_SLOTS);
   uint64_t* empty = full + N_SLOTS;
   if (threadIdx.x == 0) {
@@ -423,13 +484,13 @@ __global__ void __launch_bounds__(CONE_THREADS, 1)
   }
   __syncthreads();
   if ((threadIdx.x >> 5) == CONE_CONSUMER_WARPS)
-    producer(beams, n_beams, D, total_units, unit_counter, updates, flags, win, slot_taps, desc, full, empty);
+    producer(beams, n_beams, D, total_units, unit_counter, updates, flags, win, slot_runs, desc, full, empty);
   else
-    consumer(beams, D, flags, win, slot_taps, desc, full, empty);
+    consumer(beams, D, flags, win, slot_runs, desc, full, empty);
 }
 
 size_t cone_smem_bytes() {
-  return 1024 + (size_t)N_SLOTS * WIN_FLOATS * 4 + (size_t)N_SLOTS * MAX_CHUNK_TAPS * sizeof(int4) +
+  return 1024 + (size_t)N_SLOTS * WIN_FLOATS * 4 + (size_t)N_SLOTS * MAX_CHUNK_RUNS * RUN_REC_INT4 * sizeof(int4) +
          N_SLOTS * sizeof(ChunkDesc) + 2 * N_SLOTS * sizeof(uint64_t);
 }
 

@@ -99,12 +99,14 @@ __global__ void stencil_kernel(const float* __restrict__ theta, int n_theta, con
 }
 
 // New spectrum, same walks: tap weights w = mult * f32(K[row][ki] - K[row][prev])
-// recomputed from the stored t values exactly as stencil_kernel forms them.
+// recomputed from the stored t values exactly as stencil_kernel forms them,
+// written to the tap table and to the tap's slot in its run record.
 // One thread per unique walk.
 __global__ void reweight_kernel(const double* __restrict__ K, int n_r, int n_walks, const int* __restrict__ tap_base,
                                 const int* __restrict__ tap_len, const float* __restrict__ tvals,
                                 const int* __restrict__ walk_row, const int* __restrict__ walk_mult,
-                                int4* __restrict__ taps) {
+                                int4* __restrict__ taps, const int* __restrict__ tap_run, int4* __restrict__ runs) {
+  int* run_words = reinterpret_cast<int*>(runs);
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= n_walks) return;
   const double* Kj = K + (size_t)walk_row[u] * n_r;
@@ -115,14 +117,17 @@ __global__ void reweight_kernel(const double* __restrict__ K, int n_r, int n_wal
     const int ki = kernel_index(tvals[b + m]);
     const double dk = prev < 0 ? Kj[ki] : dsub(Kj[ki], Kj[prev]);
     prev = ki;
-    taps[b + m].w = __float_as_int(__fmul_rn(d2f(dk), mult));
+    const int wbits = __float_as_int(__fmul_rn(d2f(dk), mult));
+    taps[b + m].w = wbits;
+    run_words[tap_run[b + m]] = wbits;
   }
 }
 
 void launch_reweight(const double* K, int n_r, int n_walks, const int* tap_base, const int* tap_len,
-                     const float* tvals, const int* walk_row, const int* walk_mult, int4* taps, cudaStream_t st) {
+                     const float* tvals, const int* walk_row, const int* walk_mult, int4* taps, const int* tap_run,
+                     int4* runs, cudaStream_t st) {
   reweight_kernel<<<(n_walks + 127) / 128, 128, 0, st>>>(K, n_r, n_walks, tap_base, tap_len, tvals, walk_row,
-                                                         walk_mult, taps);
+                                                         walk_mult, taps, tap_run, runs);
 }
 
 void launch_stencil(const float* theta, int n_theta, const float* phi, int n_phi, const double* K, int n_r,
