@@ -7,14 +7,18 @@ g/cc), 5 x 5 cm^2 jaw field, gantry uniform in [0, 360), seeded synthetic
 inputs.  Every beam runs the whole path: blocking -> radiological depth ->
 fluence -> TERMA -> collapsed-cone dose (float32 dose and accumulation).
 
-  value       beams/s with inputs resident in HBM (batched, one persistent
-              cone launch per step), L2 flushed (256 MiB write) between steps
+  value       beams/s with inputs resident in HBM (one batched call per
+              step), L2 flushed (256 MiB write) between steps
   e2e         beams/s through the C ABI with pinned host buffers: density and
               block-map H2D plus dose D2H inside the timed region
-  roofline    cone-gather kernel: algorithmic HBM bytes (TERMA read + dose
-              write per beam) per launch over its CUDA-event time, against
-              the measured HBM peak; "onchip" gives the same kernel's
-              voxel-direction updates/s against its shared-memory ceiling
+  roofline    the cone stage of the schedule in use, from the library's stage
+              events on the launching stream, against the measured HBM peak:
+              spectral (default) = the five FFT passes, achieved = the bytes
+              those passes must move (TERMA pair in, A and B intermediates
+              written and read, dose pair out, S^ once per launch) over their
+              time; gather = algorithmic 8 N bytes per beam over the gather
+              launch, with "onchip" its updates/s against the shared-memory
+              lane ceiling
   cpu_baseline / --impl reference
               the CPU oracle (C++ FP64 restatement of the reference path,
               OpenMP over every host core) on whole beams of the workload
@@ -323,6 +327,30 @@ def batched_extras(args, dev):
             "kernels_per_batch": 2 * args.batch_beams + 3, "graph_launches_per_batch": 1}
 
 
+def spectral_period(n):
+    """FFT period of one axis: the power of two >= 2 n - 1 (at least 16)."""
+    m = 16
+    while m < 2 * n - 1:
+        m *= 2
+    return m
+
+
+def spectral_launches(beams, max_pairs=8):
+    return ((beams + 1) // 2 + max_pairs - 1) // max_pairs
+
+
+def spectral_bytes(size, beams, max_pairs=8):
+    """HBM bytes the five FFT passes must move for `beams` beams of one grid:
+    per pair of beams the two TERMA volumes in and two doses out (16 N), the
+    intermediates A [nx][ny][Mz] and B [nx][My][Mz] (complex float32) each
+    written and read twice, and S^ [Mx][My][Mz] read once per launch."""
+    nx, ny, nz = (int(k) for k in size)
+    Mx, My, Mz = (spectral_period(k) for k in (nx, ny, nz))
+    pairs = (beams + 1) // 2
+    a, b = nx * ny * Mz * 8, nx * My * Mz * 8
+    return pairs * (16 * nx * ny * nz + 4 * a + 4 * b) + spectral_launches(beams, max_pairs) * Mx * My * Mz * 8
+
+
 def config(args, beams_per_step=None):
     return {"workload": f"heterogeneous slab phantom {args.grid}^3 @ {args.spacing:g} cm, "
                         f"{args.field:g}x{args.field:g} cm2 field, gantry U[0,360), 6 MV, 12x48 cones",
@@ -398,10 +426,16 @@ def run_ours(args):
     job_s = max_over_ranks(local_s, dev)
     value = world * args.steps * B / job_s
 
-    # ---- cone kernel roofline (CUDA events around the gather launch, same stream)
+    # ---- cone stage roofline (the library's stage events, same stream)
     cone_ms = statistics.mean(x["ms_cone"] for x in stats)
     updates = statistics.mean(x["updates"] for x in stats)
-    alg_bytes = B * 2 * 4 * N                     # TERMA read + dose write per beam
+    method = "spectral" if int(eng.get_tuning().get("cone_method", 0)) == 0 else "gather"
+    if method == "spectral":
+        alg_bytes = spectral_bytes(ph.size, B)
+        launches_per_step = 1 + 2 * B + 5 * spectral_launches(B)
+    else:
+        alg_bytes = B * 2 * 4 * N                 # TERMA read + dose write per beam
+        launches_per_step = 2 * B + 3
     peaks = {}
     pk_path = os.path.join(HERE, "MEASURED_PEAKS.json")
     if os.path.exists(pk_path):
@@ -411,18 +445,21 @@ def run_ours(args):
     # DRAM bytes of one cone launch: the ncu capture's bytes per beam (it reads
     # each beam's TERMA once) times the beams of this launch
     traffic = None
-    tr_path = os.path.join(HERE, "profiles", "cone_gather_128cube_dram.json")
+    tr_path = os.path.join(HERE, "profiles", f"{'spectral' if method == 'spectral' else 'cone_gather'}"
+                                             f"_128cube_dram.json")
     if os.path.exists(tr_path) and args.grid == 128:
         with open(tr_path) as f:
             tr = json.load(f)
         if tr.get("dram_bytes_per_beam"):
             traffic = tr["dram_bytes_per_beam"] * B
-    props = torch.cuda.get_device_properties(dev)
-    sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
-    lds_ceiling = props.multi_processor_count * 32 * sm_mhz * 1e6     # one 4-byte LDS lane per update
-    onchip = {"metric": "voxel-direction updates/s", "achieved": updates / (cone_ms * 1e-3),
-              "peak": lds_ceiling, "frac": updates / (cone_ms * 1e-3) / lds_ceiling,
-              "peak_basis": "SMs x 32 shared-memory lanes/clk x median SM clock"}
+    onchip = None
+    if method == "gather":
+        props = torch.cuda.get_device_properties(dev)
+        sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+        lds_ceiling = props.multi_processor_count * 32 * sm_mhz * 1e6     # one 4-byte LDS lane per update
+        onchip = {"metric": "voxel-direction updates/s", "achieved": updates / (cone_ms * 1e-3),
+                  "peak": lds_ceiling, "frac": updates / (cone_ms * 1e-3) / lds_ceiling,
+                  "peak_basis": "SMs x 32 shared-memory lanes/clk x median SM clock"}
 
     # ---- e2e through the C ABI with pinned host buffers
     e2e = None
@@ -505,7 +542,9 @@ def run_ours(args):
             "config": config(args),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic,
-                         "kernel": "cone_gather_kernel",
+                         "kernel": ("spectral cone stage (spec_z_forward, spec_y, spec_x, spec_y, "
+                                    "spec_z_inverse)" if method == "spectral" else "cone_gather_kernel"),
+                         "algorithmic_bytes_per_step": alg_bytes,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"},
             "onchip": onchip,
             "cone_ms_per_step": cone_ms,
@@ -514,7 +553,8 @@ def run_ours(args):
             "updates_per_step": updates,
             "e2e": e2e,
             "clocks": clk,
-            "gpu_launches": args.steps * (2 * B + 3),
+            "cone_method": method,
+            "gpu_launches": args.steps * launches_per_step,
             "schedule": schedule,
         }
         line.update(extras)

@@ -76,7 +76,11 @@ class Beamlets(ctypes.Structure):
 
 
 class Tuning(ctypes.Structure):
-    _fields_ = [("dir_group", ctypes.c_int), ("unit_order", ctypes.c_int), ("terma_ctas_per_sm", ctypes.c_int)]
+    _fields_ = [("dir_group", ctypes.c_int), ("unit_order", ctypes.c_int), ("terma_ctas_per_sm", ctypes.c_int),
+                ("cone_method", ctypes.c_int)]
+
+
+CONE_SPECTRAL, CONE_GATHER = 0, 1     # ch_tuning.cone_method
 
 
 class Stats(ctypes.Structure):

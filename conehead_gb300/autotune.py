@@ -9,7 +9,9 @@ cached in a JSON file keyed by the device and a workload signature, so a
 later call with a similar batch is free.
 
 Knobs (see include/conehead_gb300.h):
-  dir_group          unique directions per cone work unit (16, 32, 64)
+  cone_method        0 = spectral (FFT convolution with the tap stencil),
+                     1 = stencil gather
+  dir_group          unique directions per gather work unit (16, 32, 64)
   unit_order         0 = a tile's direction groups run back to back,
                      1 = a direction group's tiles do
   terma_ctas_per_sm  CTAs per SM of the TERMA pass (4, 8, 16)
@@ -20,14 +22,15 @@ import statistics
 
 import numpy as np
 
-DEFAULT = {"dir_group": 16, "unit_order": 0, "terma_ctas_per_sm": 8}
+DEFAULT = {"dir_group": 16, "unit_order": 0, "terma_ctas_per_sm": 8, "cone_method": 0}
 # Units of more than 64 directions also run, but every thread then sums more
 # taps in one float32 register before its add to the dose: measured against
 # the float32-mirrored oracle at 64^3 the error grows from 5e-7 of Dmax (16
 # or 32 directions) and 9e-7 (64) to 1.6e-6 (128) and 9e-6 (1024).  The tuner
 # stays at 64 or below, where the precision is unchanged.
-CANDIDATES = [{"dir_group": g, "unit_order": o, "terma_ctas_per_sm": t}
-              for g in (16, 32, 64) for o in (0, 1) for t in (4, 8, 16)]
+CANDIDATES = ([{"dir_group": 16, "unit_order": 0, "terma_ctas_per_sm": t, "cone_method": 0} for t in (4, 8, 16)] +
+              [{"dir_group": g, "unit_order": o, "terma_ctas_per_sm": t, "cone_method": 1}
+               for g in (16, 32, 64) for o in (0, 1) for t in (4, 8, 16)])
 
 
 def cache_path():
@@ -99,11 +102,12 @@ def autotune(engine, jobs, candidates=None, iters=2, force=False, path=None, tim
     key = signature(device_name, jobs)
     table = _load(path)
     if not force and key in table:
-        best = table[key]["tuning"]
+        best = {**DEFAULT, **table[key]["tuning"]}
         engine.set_tuning(**best)
         return {"tuning": best, "ms": table[key]["ms"], "table": table[key].get("table", []), "cached": True}
     results = []
     for cand in candidates or CANDIDATES:
+        cand = {**DEFAULT, **cand}          # every knob named, unnamed ones at their defaults
         engine.set_tuning(**cand)
         results.append((cand, timer(engine, jobs)))
     best, ms = min(results, key=lambda r: r[1])

@@ -18,7 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libconehead_gb300.so")
-SOURCES = ["prologue.cu", "stencil.cu", "cone.cu", "block.cu", "adjoint.cu", "capi.cu"]
+SOURCES = ["prologue.cu", "stencil.cu", "cone.cu", "spectral.cu", "block.cu", "adjoint.cu", "capi.cu"]
 HEADERS = ["ch_internal.cuh", os.path.join("..", "..", "include", "conehead_gb300.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",

@@ -112,10 +112,19 @@ struct FrameStencils {
   }
 };
 
+// S^ of one grid shape and stencil set (spectral cone stage)
+struct SpecEntry {
+  const StencilSet* set = nullptr;
+  int n[3] = {0, 0, 0};
+  DevBuf shat;               // float2 [Mx][My][Mz]
+  uint64_t last_use = 0;
+  ~SpecEntry() { shat.release(); }
+};
+
 struct ch_plan {
   int device = 0;
   int n_sm = 0;
-  ch_tuning tuning{DIR_GROUP, 0, 8};
+  ch_tuning tuning{DIR_GROUP, 0, 8, CH_CONE_SPECTRAL};
   int live_batches = 0;      // captured batches reading this plan's stencils
   int reweights = 0;         // spectrum switches served by reweighting the stencils
   std::vector<std::unique_ptr<FrameStencils>> frames;   // beam-frame cone stencils by orientation
@@ -126,8 +135,10 @@ struct ch_plan {
   std::vector<float> h_theta, h_phi;   // the direction tables the stencils were built from
   StencilSet st;
   StencilSet st_adj;         // the same walks mirrored (offsets and directions negated): the transposed cone
+  std::vector<std::unique_ptr<SpecEntry>> spec;   // S^ by grid shape and stencil set
+  DevBuf spec_tw;            // FFT twiddles of every period
   // scratch
-  DevBuf T, aabb, counters, ranges, cranges, cone_beams, range_beams, list_v;
+  DevBuf T, aabb, counters, ranges, cranges, cone_beams, range_beams, list_v, spec_work;
   DevBuf adj_in, adj_out, adj_w;   // cone-operator input (padded), output, beamlet gradient (float64)
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaStream_t last_stream = nullptr;
@@ -145,8 +156,9 @@ struct ch_plan {
   ~ch_plan() {
     for (int i = 0; i < 2; ++i)
       if (rec_pending[i] && ev_rec[i]) cudaEventSynchronize(ev_rec[i]);
+    spec.clear();
     for (DevBuf* b : {&K, &theta, &phi, &T, &aabb, &counters, &ranges, &cranges, &cone_beams, &range_beams, &list_v,
-                      &adj_in, &adj_out, &adj_w})
+                      &spec_work, &spec_tw, &adj_in, &adj_out, &adj_w})
       b->release();
     for (StencilSet* S : {&st, &st_adj})
       for (DevBuf* b : S->bufs()) b->release();
@@ -168,8 +180,17 @@ ch_status assemble_stencils(ch_plan* P, StencilSet& S, int sign, int n_raw, int 
                             const std::vector<float>& h_dir_in, const float* spacing, const int* cap,
                             cudaStream_t s);
 
+// drop the S^ built from stencil set S (it is being rebuilt or freed)
+void spec_forget(ch_plan* P, const StencilSet* S) {
+  P->spec.erase(std::remove_if(P->spec.begin(), P->spec.end(),
+                               [S](const std::unique_ptr<SpecEntry>& e) { return e->set == S; }),
+                P->spec.end());
+}
+
 ch_status build_stencils(ch_plan* P, const float* spacing, const int* cap, cudaStream_t s,
                          const ConeFrame& frame, StencilSet& S, StencilSet& S_adj) {
+  spec_forget(P, &S);
+  spec_forget(P, &S_adj);
   const int n_raw = P->n_theta * P->n_phi;
   const int max_len = cap[0] + cap[1] + cap[2] + 2;
   DevBuf off, tv, dk, len;
@@ -440,6 +461,8 @@ ch_status frame_stencils(ch_plan* P, const float* spacing, const int* dims, cons
                                 [](const std::unique_ptr<FrameStencils>& a, const std::unique_ptr<FrameStencils>& b) {
                                   return a->last_use < b->last_use;
                                 });
+    spec_forget(P, &(*lru)->fwd);
+    spec_forget(P, &(*lru)->adj);
     P->frames.erase(lru);
   }
   std::unique_ptr<FrameStencils> f(new FrameStencils());
@@ -475,6 +498,114 @@ ConeDirs cone_dirs(const StencilSet& S, const ch_tuning& t) {
   D.chunk_rec = S.chunk_rec.as<int4>();
   D.dirs = S.dirs.as<float>();
   return D;
+}
+
+// ---------------------------------------------------------- spectral S^ --
+SpecGrid spec_grid(const ch_plan* P, const int* n, const int* M, int zp, int conj, const float2* shat) {
+  SpecGrid g{};
+  for (int k = 0; k < 3; ++k) {
+    g.n[k] = n[k];
+    g.M[k] = M[k];
+    g.logM[k] = __builtin_ctz((unsigned)M[k]);
+    g.tw[k] = P->spec_tw.as<float2>() + spec_twiddle_offset(M[k]);
+  }
+  g.zp = zp;
+  g.conj = conj;
+  g.shat = shat;
+  return g;
+}
+
+// S^ of grid shape n for stencil set S: the current tap weights summed per
+// offset o with |o_k| <= n_k - 1 (float64 sums in offset order, times
+// 1/(Mx My Mz)), placed at o mod M, then three forward FFT passes.  Cached
+// per (set, shape), least recently used out past kSpecEntries while no
+// captured batch holds one.
+constexpr size_t kSpecEntries = 8;
+ch_status spec_shat(ch_plan* P, const StencilSet& S, const int* n, cudaStream_t s, const float2** out) {
+  P->use_clock += 1;
+  for (auto& e : P->spec)
+    if (e->set == &S && e->n[0] == n[0] && e->n[1] == n[1] && e->n[2] == n[2]) {
+      e->last_use = P->use_clock;
+      *out = e->shat.as<float2>();
+      return CH_OK;
+    }
+  if (!P->spec_tw.p) {
+    const std::vector<float2> tw = spec_twiddles();
+    CH_CUDA(P->spec_tw.ensure(tw.size() * sizeof(float2)));
+    CH_CUDA(cudaMemcpy(P->spec_tw.p, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice));
+  }
+  if (P->spec.size() >= kSpecEntries && P->live_batches == 0) {
+    auto lru = std::min_element(P->spec.begin(), P->spec.end(),
+                                [](const std::unique_ptr<SpecEntry>& a, const std::unique_ptr<SpecEntry>& b) {
+                                  return a->last_use < b->last_use;
+                                });
+    P->spec.erase(lru);
+  }
+  const int M[3] = {spec_period(n[0]), spec_period(n[1]), spec_period(n[2])};
+  const size_t vol = (size_t)M[0] * M[1] * M[2];
+  std::vector<int4> taps(S.total_taps);
+  std::vector<short4> offs(S.total_taps);
+  CH_CUDA(cudaMemcpyAsync(taps.data(), S.taps.p, taps.size() * sizeof(int4), cudaMemcpyDeviceToHost, s));
+  CH_CUDA(cudaMemcpyAsync(offs.data(), S.offs.p, offs.size() * sizeof(short4), cudaMemcpyDeviceToHost, s));
+  CH_CUDA(cudaStreamSynchronize(s));
+  std::vector<std::pair<long long, float>> ent;
+  ent.reserve(taps.size());
+  for (size_t t = 0; t < taps.size(); ++t) {
+    const short4 o = offs[t];
+    if (std::abs((int)o.x) > n[0] - 1 || std::abs((int)o.y) > n[1] - 1 || std::abs((int)o.z) > n[2] - 1) continue;
+    const long long i = (((long long)(o.x + M[0]) % M[0]) * M[1] + (o.y + M[1]) % M[1]) * M[2] + (o.z + M[2]) % M[2];
+    float w;
+    std::memcpy(&w, &taps[t].w, 4);
+    ent.emplace_back(i, w);
+  }
+  std::sort(ent.begin(), ent.end(),
+            [](const std::pair<long long, float>& a, const std::pair<long long, float>& b) { return a.first < b.first; });
+  std::vector<long long> idx;
+  std::vector<float> val;
+  const double scale = 1.0 / (double)vol;
+  for (size_t k = 0; k < ent.size();) {
+    double sum = 0.0;
+    size_t e = k;
+    for (; e < ent.size() && ent[e].first == ent[k].first; ++e) sum += (double)ent[e].second;
+    idx.push_back(ent[k].first);
+    val.push_back((float)(sum * scale));
+    k = e;
+  }
+  std::unique_ptr<SpecEntry> E(new SpecEntry());
+  E->set = &S;
+  for (int k = 0; k < 3; ++k) E->n[k] = n[k];
+  DevBuf d_idx, d_val, s_real, work;
+  auto cleanup = [&]() {
+    d_idx.release();
+    d_val.release();
+    s_real.release();
+    work.release();
+  };
+  cudaError_t e = E->shat.ensure(vol * sizeof(float2));
+  if (e == cudaSuccess) e = s_real.ensure(vol * sizeof(float));
+  if (e == cudaSuccess) e = work.ensure(vol * sizeof(float2));
+  if (e == cudaSuccess) e = d_idx.ensure(std::max<size_t>(idx.size(), 1) * sizeof(long long));
+  if (e == cudaSuccess) e = d_val.ensure(std::max<size_t>(val.size(), 1) * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_idx.p, idx.data(), idx.size() * sizeof(long long), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_val.p, val.data(), val.size() * sizeof(float), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s_real.p, 0, vol * sizeof(float), s);
+  if (e != cudaSuccess) {
+    cleanup();
+    return fail(CH_ERR_DEVICE, std::string("spectral stencil: ") + cudaGetErrorString(e));
+  }
+  SpecLaunch L{};
+  L.g = spec_grid(P, M, M, M[2], 0, nullptr);
+  L.n_pairs = 1;
+  L.p[0] = SpecPair{s_real.as<float>(), nullptr, work.as<float2>(), E->shat.as<float2>(), nullptr, nullptr};
+  launch_spec_build(L, d_idx.as<long long>(), d_val.as<float>(), (int)idx.size(), s_real.as<float>(), s);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cleanup();
+  if (e != cudaSuccess) return fail(CH_ERR_DEVICE, std::string("spectral stencil: ") + cudaGetErrorString(e));
+  E->last_use = P->use_clock;
+  *out = E->shat.as<float2>();
+  P->spec.push_back(std::move(E));
+  return CH_OK;
 }
 
 // --------------------------------------------------------- validation --
@@ -698,13 +829,92 @@ ch_status stage_records(ch_plan* P, const ConeBeam* cb, const RangeBeam* rb, int
   return CH_OK;
 }
 
-// Scratch arena sizes of one batch, in the order T, aabb, counters, ranges,
-// cranges, cone_beams, range_beams, list_v (the buffers run() grows).
-struct ScratchNeed {
-  size_t bytes[8];
+// ------------------------------------------------- spectral cone layout --
+// Beams of one grid shape are paired in call order; a launch takes up to
+// SPEC_MAX_PAIRS pairs of one shape, and the launches of a batch run one
+// after another in one work arena (A and B of each pair of the launch).
+struct SpecPlanPair {
+  int j1, j2;                // beams (j2 = -1: the first alone)
+  size_t a_off, b_off;       // float2 offsets in the work arena
+};
+struct SpecPlanLaunch {
+  int n[3], M[3];
+  const float2* shat = nullptr;
+  std::vector<SpecPlanPair> pairs;
+};
+struct SpecLayout {
+  std::vector<SpecPlanLaunch> launches;
+  size_t arena = 0;          // float2
 };
 
-ScratchNeed scratch_need(int n, const ch_grid* grids, int U) {
+constexpr long long kSpecMaxVolume = 1ll << 28;   // largest Mx My Mz (S^ of 2 GiB)
+
+bool spec_fits(const int* n) {
+  long long v = 1;
+  for (int k = 0; k < 3; ++k) {
+    if (2 * n[k] - 1 > SPEC_MAX_PERIOD) return false;
+    v *= spec_period(n[k]);
+  }
+  return v <= kSpecMaxVolume;
+}
+
+SpecLayout spec_layout(int n, const ch_grid* grids) {
+  SpecLayout L;
+  std::vector<char> done(n, 0);
+  for (int i = 0; i < n; ++i) {
+    if (done[i]) continue;
+    std::vector<int> group;
+    for (int j = i; j < n; ++j)
+      if (!done[j] && grids[j].n[0] == grids[i].n[0] && grids[j].n[1] == grids[i].n[1] &&
+          grids[j].n[2] == grids[i].n[2]) {
+        group.push_back(j);
+        done[j] = 1;
+      }
+    const int* d = grids[i].n;
+    const int M[3] = {spec_period(d[0]), spec_period(d[1]), spec_period(d[2])};
+    const size_t a_sz = (size_t)d[0] * d[1] * M[2], b_sz = (size_t)d[0] * M[1] * M[2];
+    for (size_t p = 0; p < group.size(); p += 2 * SPEC_MAX_PAIRS) {
+      SpecPlanLaunch l;
+      for (int k = 0; k < 3; ++k) {
+        l.n[k] = d[k];
+        l.M[k] = M[k];
+      }
+      size_t off = 0;
+      const size_t end = std::min(group.size(), p + 2 * SPEC_MAX_PAIRS);
+      for (size_t q = p; q < end; q += 2) {
+        SpecPlanPair pr;
+        pr.j1 = group[q];
+        pr.j2 = q + 1 < end ? group[q + 1] : -1;
+        pr.a_off = off;
+        off += (a_sz + 31) / 32 * 32;
+        pr.b_off = off;
+        off += (b_sz + 31) / 32 * 32;
+        l.pairs.push_back(pr);
+      }
+      L.arena = std::max(L.arena, off);
+      L.launches.push_back(std::move(l));
+    }
+  }
+  return L;
+}
+
+bool spec_batch(const ch_plan* P, int n, const ch_grid* grids) {
+  if (P->tuning.cone_method != CH_CONE_SPECTRAL) return false;
+  for (int i = 0; i < n; ++i)
+    if (!spec_fits(grids[i].n)) return false;
+  return true;
+}
+
+// Scratch arena sizes of one batch, in the order T, aabb, counters, ranges,
+// cranges, cone_beams, range_beams, list_v, spectral work (the buffers run()
+// grows); the gather's tables are empty for a spectral batch.
+constexpr int N_SCRATCH = 9;
+struct ScratchNeed {
+  size_t bytes[N_SCRATCH];
+};
+
+ScratchNeed scratch_need(int n, const ch_grid* grids, int U, bool spectral = false) {
+  if (spectral) U = 0;
   size_t t_total = 0, r_total = 0, max_vox = 1;
   for (int i = 0; i < n; ++i) {
     const size_t zp = (size_t)round_up(grids[i].n[2], 4);
@@ -724,12 +934,13 @@ ScratchNeed scratch_need(int n, const ch_grid* grids, int U) {
   r.bytes[5] = (size_t)n * sizeof(ConeBeam);
   r.bytes[6] = (size_t)n * sizeof(RangeBeam);
   r.bytes[7] = max_vox * sizeof(int);
+  r.bytes[8] = spectral ? spec_layout(n, grids).arena * sizeof(float2) : 0;
   return r;
 }
 
 const DevBuf* scratch_bufs(const ch_plan* P, int k) {
-  const DevBuf* b[8] = {&P->T, &P->aabb, &P->counters, &P->ranges, &P->cranges, &P->cone_beams, &P->range_beams,
-                        &P->list_v};
+  const DevBuf* b[N_SCRATCH] = {&P->T,          &P->aabb,        &P->counters, &P->ranges,   &P->cranges,
+                                &P->cone_beams, &P->range_beams, &P->list_v,   &P->spec_work};
   return b[k];
 }
 
@@ -740,6 +951,8 @@ struct BatchPlan {
   int U = 0;
   int total_units = 0;
   int max_tiles = 0;
+  bool spectral = false;             // cone stage by FFT convolution (else the gather)
+  SpecLayout spec;
 };
 
 // Scratch a batch runs in (the plan's arena, or a captured batch's own).
@@ -752,6 +965,7 @@ struct Scratch {
   ConeBeam* cone_beams;
   RangeBeam* range_beams;
   int* list_v;
+  float2* spec;           // spectral work arena
 };
 
 ch_status plan_batch(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, const int* swap_xy,
@@ -787,6 +1001,14 @@ ch_status plan_batch(ch_plan* P, int n, const ch_grid* grids, const float* const
     B.set = &P->st;
   }
   B.U = B.set->n_dirs;
+  B.spectral = spec_batch(P, n, grids);
+  if (B.spectral) {
+    B.spec = spec_layout(n, grids);
+    for (SpecPlanLaunch& l : B.spec.launches) {
+      ch_status st = spec_shat(P, *B.set, l.n, s, &l.shat);
+      if (st != CH_OK) return st;
+    }
+  }
   const int n_groups = (B.U + P->tuning.dir_group - 1) / P->tuning.dir_group;
   size_t t_total = 0, r_total = 0;
   B.total_units = 0;
@@ -904,6 +1126,28 @@ ch_status enqueue_batch(ch_plan* P, const BatchPlan& B, const Scratch& S, const 
     CH_CUDA(cudaGetLastError());
   }
   if (ev) CH_CUDA(cudaEventRecord(ev[1], s));
+  if (B.spectral) {
+    // FFT convolution, launch after launch in the work arena; every dose
+    // voxel is written
+    if (ev) CH_CUDA(cudaEventRecord(ev[2], s));
+    for (const SpecPlanLaunch& l : B.spec.launches) {
+      SpecLaunch L{};
+      const BeamJob& J0 = B.jobs[l.pairs[0].j1];
+      L.g = spec_grid(P, l.n, l.M, J0.g.zp, 0, l.shat);
+      L.n_pairs = (int)l.pairs.size();
+      for (int q = 0; q < L.n_pairs; ++q) {
+        const SpecPlanPair& pr = l.pairs[q];
+        const BeamJob& J1 = B.jobs[pr.j1];
+        const BeamJob* J2 = pr.j2 >= 0 ? &B.jobs[pr.j2] : nullptr;
+        L.p[q] = SpecPair{S.T + J1.t_off, J2 ? S.T + J2->t_off : nullptr, S.spec + pr.a_off, S.spec + pr.b_off,
+                          J1.dose, J2 ? J2->dose : nullptr};
+      }
+      launch_spec_pairs(L, s);
+      CH_CUDA(cudaGetLastError());
+    }
+    if (ev) CH_CUDA(cudaEventRecord(ev[3], s));
+    return CH_OK;
+  }
   for (int i = 0; i < n; ++i)
     CH_CUDA(cudaMemsetAsync(B.jobs[i].dose, 0, (size_t)B.jobs[i].g.n[0] * B.jobs[i].g.n[1] * B.jobs[i].g.n[2] * 4,
                             s));
@@ -924,18 +1168,11 @@ ch_status run_group(ch_plan* P, int n, const ch_grid* grids, const float* const*
   BatchPlan B;
   ch_status st = plan_batch(P, n, grids, rho, swap_xy, beams, settings, dose, s, B, set);
   if (st != CH_OK) return st;
-  const ScratchNeed need = scratch_need(n, grids, B.U);
-  CH_CUDA(P->T.ensure(need.bytes[0]));
-  CH_CUDA(P->aabb.ensure(need.bytes[1]));
-  CH_CUDA(P->counters.ensure(need.bytes[2]));
-  CH_CUDA(P->ranges.ensure(need.bytes[3]));
-  CH_CUDA(P->cranges.ensure(need.bytes[4]));
-  CH_CUDA(P->cone_beams.ensure(need.bytes[5]));
-  CH_CUDA(P->range_beams.ensure(need.bytes[6]));
-  CH_CUDA(P->list_v.ensure(need.bytes[7]));
+  const ScratchNeed need = scratch_need(n, grids, B.U, B.spectral && !scatter);
+  for (int k = 0; k < N_SCRATCH; ++k) CH_CUDA(const_cast<DevBuf*>(scratch_bufs(P, k))->ensure(need.bytes[k]));
   const Scratch S{P->T.as<float>(),          P->aabb.as<int>(),           P->counters.as<int>(),
                   P->ranges.as<uint32_t>(),  P->cranges.as<uint32_t>(),   P->cone_beams.as<ConeBeam>(),
-                  P->range_beams.as<RangeBeam>(), P->list_v.as<int>()};
+                  P->range_beams.as<RangeBeam>(), P->list_v.as<int>(),    P->spec_work.as<float2>()};
   for (auto& e : P->ev)
     if (!e) CH_CUDA(cudaEventCreate(&e));
   P->stats = ch_stats{};
@@ -972,12 +1209,14 @@ ch_status run_group(ch_plan* P, int n, const ch_grid* grids, const float* const*
     CH_CUDA(cudaEventRecord(P->ev[3], s));
     return CH_OK;
   }
-  std::vector<ConeBeam> cb;
-  std::vector<RangeBeam> rb;
-  if ((st = make_records(B, S, cb, rb)) != CH_OK) return st;
-  if ((st = stage_records(P, cb.data(), rb.data(), n, s)) != CH_OK) return st;
+  if (!B.spectral) {
+    std::vector<ConeBeam> cb;
+    std::vector<RangeBeam> rb;
+    if ((st = make_records(B, S, cb, rb)) != CH_OK) return st;
+    if ((st = stage_records(P, cb.data(), rb.data(), n, s)) != CH_OK) return st;
+  }
   if ((st = enqueue_batch(P, B, S, inter, P->ev, s)) != CH_OK) return st;
-  P->stats.n_units = B.total_units;
+  P->stats.n_units = B.spectral ? 0 : B.total_units;
   return CH_OK;
 }
 
@@ -1119,6 +1358,7 @@ ch_status ch_plan_set_kernel(ch_plan* P, const ch_kernel* k) {
     P->st_adj.valid = false;
   }
   P->frames.clear();          // beam-frame stencils are rebuilt on demand
+  P->spec.clear();            // S^ follows the tap weights
   return CH_OK;
 }
 
@@ -1456,13 +1696,14 @@ struct ch_batch {
   ch_plan* P = nullptr;
   int n = 0;
   int total_units = 0;
-  DevBuf T, aabb, counters, ranges, cranges, cone_beams, range_beams, list_v;
+  DevBuf T, aabb, counters, ranges, cranges, cone_beams, range_beams, list_v, spec_work;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   ~ch_batch() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
-    for (DevBuf* b : {&T, &aabb, &counters, &ranges, &cranges, &cone_beams, &range_beams, &list_v}) b->release();
+    for (DevBuf* b : {&T, &aabb, &counters, &ranges, &cranges, &cone_beams, &range_beams, &list_v, &spec_work})
+      b->release();
   }
 };
 
@@ -1481,20 +1722,22 @@ ch_status ch_batch_create(ch_plan* P, int n, const ch_grid* grids, const float* 
   bt->P = P;
   bt->n = n;
   bt->total_units = B.total_units;
-  const ScratchNeed need = scratch_need(n, grids, B.U);
-  DevBuf* bufs[8] = {&bt->T, &bt->aabb, &bt->counters, &bt->ranges, &bt->cranges, &bt->cone_beams,
-                     &bt->range_beams, &bt->list_v};
-  for (int k = 0; k < 8; ++k) CH_CUDA(bufs[k]->ensure(need.bytes[k]));
+  const ScratchNeed need = scratch_need(n, grids, B.U, B.spectral);
+  DevBuf* bufs[N_SCRATCH] = {&bt->T,          &bt->aabb,        &bt->counters, &bt->ranges,   &bt->cranges,
+                             &bt->cone_beams, &bt->range_beams, &bt->list_v,   &bt->spec_work};
+  for (int k = 0; k < N_SCRATCH; ++k) CH_CUDA(bufs[k]->ensure(need.bytes[k]));
   const Scratch S{bt->T.as<float>(),          bt->aabb.as<int>(),          bt->counters.as<int>(),
                   bt->ranges.as<uint32_t>(),  bt->cranges.as<uint32_t>(),  bt->cone_beams.as<ConeBeam>(),
-                  bt->range_beams.as<RangeBeam>(), bt->list_v.as<int>()};
-  std::vector<ConeBeam> cb;
-  std::vector<RangeBeam> rb;
-  if ((st = make_records(B, S, cb, rb)) != CH_OK) return st;
-  // the records are fixed for the batch's life: upload them once, outside the graph
+                  bt->range_beams.as<RangeBeam>(), bt->list_v.as<int>(),   bt->spec_work.as<float2>()};
   CH_CUDA(cudaStreamSynchronize(s));
-  CH_CUDA(cudaMemcpy(bt->cone_beams.p, cb.data(), n * sizeof(ConeBeam), cudaMemcpyHostToDevice));
-  CH_CUDA(cudaMemcpy(bt->range_beams.p, rb.data(), n * sizeof(RangeBeam), cudaMemcpyHostToDevice));
+  if (!B.spectral) {
+    std::vector<ConeBeam> cb;
+    std::vector<RangeBeam> rb;
+    if ((st = make_records(B, S, cb, rb)) != CH_OK) return st;
+    // the records are fixed for the batch's life: upload them once, outside the graph
+    CH_CUDA(cudaMemcpy(bt->cone_beams.p, cb.data(), n * sizeof(ConeBeam), cudaMemcpyHostToDevice));
+    CH_CUDA(cudaMemcpy(bt->range_beams.p, rb.data(), n * sizeof(RangeBeam), cudaMemcpyHostToDevice));
+  }
   // capture the device work on a private stream
   cudaStream_t cs;
   CH_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
@@ -1606,6 +1849,8 @@ ch_status ch_plan_set_tuning(ch_plan* P, const ch_tuning* t) {
   if (t->unit_order != 0 && t->unit_order != 1) return fail(CH_ERR_INVALID_ARG, "unit_order must be 0 or 1");
   if (t->terma_ctas_per_sm < 1 || t->terma_ctas_per_sm > 32)
     return fail(CH_ERR_INVALID_ARG, "terma_ctas_per_sm out of range (1..32)");
+  if (t->cone_method != CH_CONE_SPECTRAL && t->cone_method != CH_CONE_GATHER)
+    return fail(CH_ERR_INVALID_ARG, "cone_method must be CH_CONE_SPECTRAL or CH_CONE_GATHER");
   P->tuning = *t;
   return CH_OK;
 }
@@ -1622,17 +1867,22 @@ ch_status ch_plan_prepare(ch_plan* P, const ch_grid* grid, void* stream) {
   ch_status st = check_grid(grid);
   if (st != CH_OK) return st;
   CH_CUDA(cudaSetDevice(P->device));
-  return ensure_stencils(P, grid->spacing, grid->n, (cudaStream_t)stream);
+  st = ensure_stencils(P, grid->spacing, grid->n, (cudaStream_t)stream);
+  if (st != CH_OK || !spec_batch(P, 1, grid)) return st;
+  const float2* shat = nullptr;
+  return spec_shat(P, P->st, grid->n, (cudaStream_t)stream, &shat);
 }
 
 ch_status ch_plan_memory(ch_plan* P, size_t* tables, size_t* scratch) {
   if (!P) return fail(CH_ERR_INVALID_ARG, "plan is NULL");
   size_t b = P->K.bytes + P->theta.bytes + P->phi.bytes;
   for (const StencilSet* S : {&P->st, &P->st_adj}) b += S->bytes();
+  for (const auto& e : P->spec) b += e->shat.bytes;
+  b += P->spec_tw.bytes;
   for (const auto& f : P->frames)
     for (const StencilSet* S : {&f->fwd, &f->adj}) b += S->bytes();
   size_t a = P->adj_in.bytes + P->adj_out.bytes + P->adj_w.bytes;
-  for (int k = 0; k < 8; ++k) a += scratch_bufs(P, k)->bytes;
+  for (int k = 0; k < N_SCRATCH; ++k) a += scratch_bufs(P, k)->bytes;
   if (tables) *tables = b;
   if (scratch) *scratch = a;
   return CH_OK;
@@ -1645,9 +1895,9 @@ ch_status ch_batch_scratch_bytes(ch_plan* P, int n, const ch_grid* grids, size_t
     if (st != CH_OK) return st;
   }
   const int U = P->st.valid ? P->st.n_dirs : P->n_theta * P->n_phi > 0 ? P->n_theta * P->n_phi : 576;
-  const ScratchNeed need = scratch_need(n, grids, U);
+  const ScratchNeed need = scratch_need(n, grids, U, spec_batch(P, n, grids));
   size_t g = 0, t = 0;
-  for (int k = 0; k < 8; ++k) {
+  for (int k = 0; k < N_SCRATCH; ++k) {
     const size_t cur = scratch_bufs(P, k)->bytes;
     t += need.bytes[k];
     if (need.bytes[k] > cur) g += need.bytes[k] - cur;
@@ -1662,7 +1912,7 @@ ch_status ch_plan_trim(ch_plan* P) {
   CH_CUDA(cudaSetDevice(P->device));
   // cudaFree waits for the device, so no call of this plan is still reading the arena
   for (DevBuf* b : {&P->T, &P->aabb, &P->counters, &P->ranges, &P->cranges, &P->cone_beams, &P->range_beams,
-                    &P->list_v, &P->adj_in, &P->adj_out, &P->adj_w})
+                    &P->list_v, &P->spec_work, &P->adj_in, &P->adj_out, &P->adj_w})
     b->release();
   P->stats_pending = false;
   return CH_OK;

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <vector>
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -222,6 +223,44 @@ struct Inter {
   double* blocked;
   float *d_eff, *oad, *fluence, *f_soften, *f_horn, *terma;
 };
+
+// ---------------------------------------------------- spectral cone stage --
+// The cone stage as one circular convolution per grid shape (spectral.cu):
+// periods M_k = the power of two >= 2 n_k - 1 (at least SPEC_MIN_PERIOD),
+// pairs of beams per complex transform.
+constexpr int SPEC_THREADS = 256;
+constexpr int SPEC_ELEMS = 4096;          // complex values per CTA: 4096 / M lines of period M
+constexpr int SPEC_MIN_PERIOD = 16, SPEC_MAX_PERIOD = 4096;
+constexpr int SPEC_MAX_PAIRS = 8;         // beam pairs per launch (their work buffers coexist)
+struct SpecPair {
+  const float* t1;   // TERMA of the first beam [nx][ny][zp]
+  const float* t2;   // of the second (NULL: none)
+  float2* a;         // [nx][ny][Mz]
+  float2* b;         // [nx][My][Mz]
+  float* d1;         // dose of the first beam [nx][ny][nz]
+  float* d2;         // of the second (NULL: none)
+};
+struct SpecGrid {
+  int n[3], M[3], logM[3];
+  int zp;                  // z pitch of the TERMA volumes
+  int conj;                // multiply by conj(S^): the transposed cone
+  const float2* tw[3];     // twiddles exp(-2 pi i k / M_axis)
+  const float2* shat;      // S^ [Mx][My][Mz], 1/(Mx My Mz) folded in
+};
+struct SpecLaunch {
+  SpecGrid g;
+  int n_pairs;
+  SpecPair p[SPEC_MAX_PAIRS];
+};
+int spec_period(int n);
+std::vector<float2> spec_twiddles();      // every period SPEC_MIN_PERIOD .. SPEC_MAX_PERIOD, back to back
+size_t spec_twiddle_offset(int M);
+void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st);
+// S^ of one grid shape: scatter the stencil values into the real volume
+// s_real (zeroed, [Mx][My][Mz] = L.p[0].t1), then three forward passes
+// (L.g.n = M, L.p[0].a = work, L.p[0].b = S^)
+void launch_spec_build(const SpecLaunch& L, const long long* idx, const float* val, int n_val, float* s_real,
+                       cudaStream_t st);
 
 // ------------------------------------------------------------ launchers --
 void upload_unit_partials();

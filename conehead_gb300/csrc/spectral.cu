@@ -1,0 +1,293 @@
+// Collapsed-cone stage as a spectral convolution (replaces the per-voxel
+// scatter of conehead/conehead.py:385-488 by the same linear operator).
+//
+// Every walk from a voxel centre visits the same offsets O_u[m] with the same
+// weights w_u[m], so the cone stage is one linear convolution with a fixed
+// stencil:
+//     dose(v) = sum_s T(s) S(v - s),   S(o) = sum_u sum_m w_u[m] [O_u[m] = o].
+// Walks stop where they leave the grid, i.e. only |o_k| <= n_k - 1 connects
+// two voxels of the grid, so a circular convolution of period
+// M_k >= 2 n_k - 1 on each axis equals the linear one on the grid:
+//     dose = IFFT( FFT(T) . S^ ),   S^ = FFT(S) / (Mx My Mz),
+// with S^ computed once per grid shape and kernel.  Two beams share one
+// complex transform: TERMA of one is the real part, of the other the
+// imaginary part; S is real, so their doses come back as the two parts.
+//
+// Each of the five passes over a pair of beams is a batch of 1-D FFTs of
+// power-of-two length M along one axis.  A CTA holds 4096 complex values
+// (L = 4096 / M lines) in shared memory, element (i, line c) at
+// i * L + (c ^ (i mod L)) so that both line-major and index-major sweeps are
+// free of bank conflicts, and runs radix-4 Stockham stages (one radix-2 stage
+// when log2 M is odd) with twiddles from a host-built table.  The passes skip
+// the zero padding:
+//   z forward  TERMA pair [nx][ny][nz] (pitch zp)  -> A [nx][ny][Mz]
+//   y forward  A (y < ny)                          -> B [nx][My][Mz]
+//   x          B (x < nx): forward, times S^, inverse, x < nx kept (in place)
+//   y inverse  B                                   -> A (y < ny)
+//   z inverse  A                                   -> dose pair [nx][ny][nz]
+// Every global sweep is coalesced: lines along z are read and written along
+// z, lines along y and x are taken in blocks of L consecutive kz.
+
+#include <cmath>
+#include <vector>
+
+#include "ch_internal.cuh"
+
+namespace ch {
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ int swz(int i, int c, int L) { return i * L + (c ^ (i & (L - 1))); }
+
+// In-place FFT of L lines of length M held in sm (layout above); INV uses
+// the conjugate twiddles (no 1/M scale).  tw[k] = exp(-2 pi i k / M).
+template <bool INV>
+__device__ void fft_block(float2* sm, int M, int logM, int L, int logL, const float2* __restrict__ tw) {
+  const int tid = threadIdx.x;
+  int Ns = 1, logNs = 0;
+  while (Ns < M) {
+    if (logM - logNs >= 2) {
+      // radix 4: butterfly j of line c reads j + r M/4, writes (j - k) 4 + k + r Ns
+      const int MR = M >> 2, nb = L * MR, step = M >> (logNs + 2);
+      float2 v[SPEC_ELEMS / 4 / SPEC_THREADS][4];
+#pragma unroll
+      for (int q = 0; q < SPEC_ELEMS / 4 / SPEC_THREADS; ++q) {
+        const int b = tid + q * SPEC_THREADS;
+        if (b < nb) {
+          const int c = b & (L - 1), j = b >> logL;
+#pragma unroll
+          for (int r = 0; r < 4; ++r) v[q][r] = sm[swz(j + r * MR, c, L)];
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < SPEC_ELEMS / 4 / SPEC_THREADS; ++q) {
+        const int b = tid + q * SPEC_THREADS;
+        if (b < nb) {
+          const int c = b & (L - 1), j = b >> logL, k = j & (Ns - 1);
+#pragma unroll
+          for (int r = 1; r < 4; ++r) {
+            float2 w = __ldg(tw + r * k * step);
+            if (INV) w.y = -w.y;
+            v[q][r] = cmul(v[q][r], w);
+          }
+          const float2 a0 = v[q][0], a1 = v[q][1], a2 = v[q][2], a3 = v[q][3];
+          const float2 s02 = make_float2(a0.x + a2.x, a0.y + a2.y), d02 = make_float2(a0.x - a2.x, a0.y - a2.y);
+          const float2 s13 = make_float2(a1.x + a3.x, a1.y + a3.y), d13 = make_float2(a1.x - a3.x, a1.y - a3.y);
+          // forward: X1 = d02 - i d13, X3 = d02 + i d13 (inverse: the other way round)
+          const float2 mi = INV ? make_float2(-d13.y, d13.x) : make_float2(d13.y, -d13.x);   // -+i d13
+          const int o = ((j - k) << 2) + k;
+          sm[swz(o, c, L)] = make_float2(s02.x + s13.x, s02.y + s13.y);
+          sm[swz(o + Ns, c, L)] = make_float2(d02.x + mi.x, d02.y + mi.y);
+          sm[swz(o + 2 * Ns, c, L)] = make_float2(s02.x - s13.x, s02.y - s13.y);
+          sm[swz(o + 3 * Ns, c, L)] = make_float2(d02.x - mi.x, d02.y - mi.y);
+        }
+      }
+      __syncthreads();
+      Ns <<= 2;
+      logNs += 2;
+    } else {
+      // radix 2 (the last stage when log2 M is odd)
+      const int MR = M >> 1, nb = L * MR, step = M >> (logNs + 1);
+      float2 v[SPEC_ELEMS / 2 / SPEC_THREADS][2];
+#pragma unroll
+      for (int q = 0; q < SPEC_ELEMS / 2 / SPEC_THREADS; ++q) {
+        const int b = tid + q * SPEC_THREADS;
+        if (b < nb) {
+          const int c = b & (L - 1), j = b >> logL;
+          v[q][0] = sm[swz(j, c, L)];
+          v[q][1] = sm[swz(j + MR, c, L)];
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < SPEC_ELEMS / 2 / SPEC_THREADS; ++q) {
+        const int b = tid + q * SPEC_THREADS;
+        if (b < nb) {
+          const int c = b & (L - 1), j = b >> logL, k = j & (Ns - 1);
+          float2 w = __ldg(tw + k * step);
+          if (INV) w.y = -w.y;
+          const float2 a0 = v[q][0], a1 = cmul(v[q][1], w);
+          const int o = ((j - k) << 1) + k;
+          sm[swz(o, c, L)] = make_float2(a0.x + a1.x, a0.y + a1.y);
+          sm[swz(o + Ns, c, L)] = make_float2(a0.x - a1.x, a0.y - a1.y);
+        }
+      }
+      __syncthreads();
+      Ns <<= 1;
+      logNs += 1;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- passes --
+// z forward: lines (x, y), TERMA pair in, A out.  One CTA per L lines and pair.
+__global__ void __launch_bounds__(SPEC_THREADS) spec_z_forward_kernel(SpecLaunch P) {
+  __shared__ float2 sm[SPEC_ELEMS];
+  const SpecPair& pr = P.p[blockIdx.y];
+  const int Mz = P.g.M[2], logMz = P.g.logM[2];
+  const int logL = 12 - logMz, L = 1 << logL;
+  const int nl = P.g.n[0] * P.g.n[1], nz = P.g.n[2];
+  const int l0 = blockIdx.x * L;
+  for (int e = threadIdx.x; e < SPEC_ELEMS; e += SPEC_THREADS) {
+    const int i = e & (Mz - 1), c = e >> logMz, l = l0 + c;
+    float2 v = make_float2(0.0f, 0.0f);
+    if (l < nl && i < nz) {
+      const size_t o = (size_t)l * P.g.zp + i;
+      v.x = pr.t1[o];
+      if (pr.t2) v.y = pr.t2[o];
+    }
+    sm[swz(i, c, L)] = v;
+  }
+  __syncthreads();
+  fft_block<false>(sm, Mz, logMz, L, logL, P.g.tw[2]);
+  for (int e = threadIdx.x; e < SPEC_ELEMS; e += SPEC_THREADS) {
+    const int i = e & (Mz - 1), c = e >> logMz, l = l0 + c;
+    if (l < nl) pr.a[(size_t)l * Mz + i] = sm[swz(i, c, L)];
+  }
+}
+
+// y forward (A -> B) or inverse (B -> A): lines (x, kz) in blocks of L kz.
+template <bool INV>
+__global__ void __launch_bounds__(SPEC_THREADS) spec_y_kernel(SpecLaunch P) {
+  __shared__ float2 sm[SPEC_ELEMS];
+  const SpecPair& pr = P.p[blockIdx.y];
+  const int My = P.g.M[1], logMy = P.g.logM[1], Mz = P.g.M[2], logMz = P.g.logM[2];
+  const int logL = min(12 - logMy, logMz), L = 1 << logL;
+  const int nkb = Mz >> logL;
+  const int x = blockIdx.x / nkb, kz0 = (blockIdx.x - x * nkb) << logL;
+  const int ny = P.g.n[1];
+  const int n_in = INV ? My : ny, n_out = INV ? ny : My;
+  const float2* src = INV ? pr.b + (size_t)x * My * Mz : pr.a + (size_t)x * ny * Mz;
+  float2* dst = INV ? pr.a + (size_t)x * ny * Mz : pr.b + (size_t)x * My * Mz;
+  src += kz0;
+  dst += kz0;
+  for (int e = threadIdx.x; e < (L << logMy); e += SPEC_THREADS) {
+    const int c = e & (L - 1), i = e >> logL;
+    sm[swz(i, c, L)] = i < n_in ? src[(size_t)i * Mz + c] : make_float2(0.0f, 0.0f);
+  }
+  __syncthreads();
+  fft_block<INV>(sm, My, logMy, L, logL, P.g.tw[1]);
+  for (int e = threadIdx.x; e < n_out * L; e += SPEC_THREADS) {
+    const int c = e & (L - 1), i = e >> logL;
+    dst[(size_t)i * Mz + c] = sm[swz(i, c, L)];
+  }
+}
+
+// x pass on B, lines (ky, kz) in blocks of L kz; consecutive CTAs take the
+// same lines of consecutive pairs, so each block of S^ is read from L2.
+// CONV: forward, times S^ (or its conjugate), inverse, x < nx kept;
+// otherwise forward only over the full period (building S^).
+template <bool CONV>
+__global__ void __launch_bounds__(SPEC_THREADS) spec_x_kernel(SpecLaunch P) {
+  __shared__ float2 sm[SPEC_ELEMS];
+  const int pair = blockIdx.x % P.n_pairs, blk = blockIdx.x / P.n_pairs;
+  const SpecPair& pr = P.p[pair];
+  const int Mx = P.g.M[0], logMx = P.g.logM[0], My = P.g.M[1], Mz = P.g.M[2], logMz = P.g.logM[2];
+  const int logL = min(12 - logMx, logMz), L = 1 << logL;
+  const int nkb = Mz >> logL;
+  const int ky = blk / nkb, kz0 = (blk - ky * nkb) << logL;
+  const size_t xs = (size_t)My * Mz, off = (size_t)ky * Mz + kz0;
+  float2* b = pr.b + off;
+  const int nx = CONV ? P.g.n[0] : Mx;
+  for (int e = threadIdx.x; e < (L << logMx); e += SPEC_THREADS) {
+    const int c = e & (L - 1), i = e >> logL;
+    sm[swz(i, c, L)] = i < nx ? b[(size_t)i * xs + c] : make_float2(0.0f, 0.0f);
+  }
+  __syncthreads();
+  fft_block<false>(sm, Mx, logMx, L, logL, P.g.tw[0]);
+  if (CONV) {
+    const float2* sh = P.g.shat + off;
+    for (int e = threadIdx.x; e < (L << logMx); e += SPEC_THREADS) {
+      const int c = e & (L - 1), i = e >> logL;
+      float2 s = __ldg(sh + (size_t)i * xs + c);
+      if (P.g.conj) s.y = -s.y;
+      const int k = swz(i, c, L);
+      sm[k] = cmul(sm[k], s);
+    }
+    __syncthreads();
+    fft_block<true>(sm, Mx, logMx, L, logL, P.g.tw[0]);
+  }
+  for (int e = threadIdx.x; e < nx * L; e += SPEC_THREADS) {
+    const int c = e & (L - 1), i = e >> logL;
+    b[(size_t)i * xs + c] = sm[swz(i, c, L)];
+  }
+}
+
+// z inverse: lines (x, y), A in, dose pair out (real part, imaginary part).
+__global__ void __launch_bounds__(SPEC_THREADS) spec_z_inverse_kernel(SpecLaunch P) {
+  __shared__ float2 sm[SPEC_ELEMS];
+  const SpecPair& pr = P.p[blockIdx.y];
+  const int Mz = P.g.M[2], logMz = P.g.logM[2];
+  const int logL = 12 - logMz, L = 1 << logL;
+  const int nl = P.g.n[0] * P.g.n[1], nz = P.g.n[2];
+  const int l0 = blockIdx.x * L;
+  for (int e = threadIdx.x; e < SPEC_ELEMS; e += SPEC_THREADS) {
+    const int i = e & (Mz - 1), c = e >> logMz, l = l0 + c;
+    sm[swz(i, c, L)] = l < nl ? pr.a[(size_t)l * Mz + i] : make_float2(0.0f, 0.0f);
+  }
+  __syncthreads();
+  fft_block<true>(sm, Mz, logMz, L, logL, P.g.tw[2]);
+  for (int e = threadIdx.x; e < SPEC_ELEMS; e += SPEC_THREADS) {
+    const int i = e & (Mz - 1), c = e >> logMz, l = l0 + c;
+    if (l < nl && i < nz) {
+      const float2 v = sm[swz(i, c, L)];
+      pr.d1[(size_t)l * nz + i] = v.x;
+      if (pr.d2) pr.d2[(size_t)l * nz + i] = v.y;
+    }
+  }
+}
+
+__global__ void spec_scatter_kernel(const long long* __restrict__ idx, const float* __restrict__ val, int n,
+                                    float* __restrict__ S) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) S[idx[k]] = val[k];
+}
+
+// ---------------------------------------------------------------- host --
+int spec_period(int n) {
+  int m = SPEC_MIN_PERIOD;
+  while (m < 2 * n - 1) m <<= 1;
+  return m;
+}
+
+std::vector<float2> spec_twiddles() {
+  std::vector<float2> t;
+  for (int M = SPEC_MIN_PERIOD; M <= SPEC_MAX_PERIOD; M <<= 1)
+    for (int k = 0; k < M; ++k) {
+      const double a = -2.0 * 3.14159265358979323846 * (double)k / (double)M;
+      t.push_back(make_float2((float)std::cos(a), (float)std::sin(a)));
+    }
+  return t;
+}
+
+size_t spec_twiddle_offset(int M) { return (size_t)M - SPEC_MIN_PERIOD; }
+
+void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
+  const SpecGrid& g = L.g;
+  const int nl = g.n[0] * g.n[1];
+  const int Lz = SPEC_ELEMS / g.M[2];
+  const int Ly = std::min(SPEC_ELEMS / g.M[1], g.M[2]);
+  const int Lx = std::min(SPEC_ELEMS / g.M[0], g.M[2]);
+  spec_z_forward_kernel<<<dim3((nl + Lz - 1) / Lz, L.n_pairs), SPEC_THREADS, 0, st>>>(L);
+  spec_y_kernel<false><<<dim3(g.n[0] * (g.M[2] / Ly), L.n_pairs), SPEC_THREADS, 0, st>>>(L);
+  spec_x_kernel<true><<<g.M[1] * (g.M[2] / Lx) * L.n_pairs, SPEC_THREADS, 0, st>>>(L);
+  spec_y_kernel<true><<<dim3(g.n[0] * (g.M[2] / Ly), L.n_pairs), SPEC_THREADS, 0, st>>>(L);
+  spec_z_inverse_kernel<<<dim3((nl + Lz - 1) / Lz, L.n_pairs), SPEC_THREADS, 0, st>>>(L);
+}
+
+void launch_spec_build(const SpecLaunch& L, const long long* idx, const float* val, int n_val, float* s_real,
+                       cudaStream_t st) {
+  const SpecGrid& g = L.g;
+  const int nl = g.n[0] * g.n[1];
+  const int Lz = SPEC_ELEMS / g.M[2];
+  const int Ly = std::min(SPEC_ELEMS / g.M[1], g.M[2]);
+  const int Lx = std::min(SPEC_ELEMS / g.M[0], g.M[2]);
+  if (n_val > 0) spec_scatter_kernel<<<(n_val + 255) / 256, 256, 0, st>>>(idx, val, n_val, s_real);
+  spec_z_forward_kernel<<<dim3((nl + Lz - 1) / Lz, 1), SPEC_THREADS, 0, st>>>(L);
+  spec_y_kernel<false><<<dim3(g.n[0] * (g.M[2] / Ly), 1), SPEC_THREADS, 0, st>>>(L);
+  spec_x_kernel<false><<<g.M[1] * (g.M[2] / Lx), SPEC_THREADS, 0, st>>>(L);
+}
+
+}  // namespace ch

@@ -205,8 +205,9 @@ class DoseEngine:
         N.check(self.L.ch_plan_sync(self.plan, self.stream()), "ch_plan_sync")
 
     # ---------------------------------------------------------- schedule --
-    def set_tuning(self, dir_group=16, unit_order=0, terma_ctas_per_sm=8):
-        t = N.Tuning(int(dir_group), int(unit_order), int(terma_ctas_per_sm))
+    def set_tuning(self, dir_group=16, unit_order=0, terma_ctas_per_sm=8, cone_method=N.CONE_SPECTRAL):
+        """Schedule knobs (``ch_tuning``); cone_method 0 = spectral, 1 = gather."""
+        t = N.Tuning(int(dir_group), int(unit_order), int(terma_ctas_per_sm), int(cone_method))
         N.check(self.L.ch_plan_set_tuning(self.plan, ctypes.byref(t)), "ch_plan_set_tuning")
 
     def get_tuning(self):

@@ -265,14 +265,18 @@ class GpuExecutor:
         return name
 
     def prepare(self, settings, spacing, max_size):
-        """Kernel tables and stencils for the largest grid, in every slot."""
+        """Kernel tables and stencils for the largest grid, and the stencil
+        spectrum of every registered phantom's grid, in every slot."""
         from . import _native as N
         import ctypes
-        g = N.grid_struct(max_size, (0.0, 0.0, 0.0), spacing)
+        shapes = [tuple(int(k) for k in max_size)]
+        shapes += [tuple(int(k) for k in ph.size) for ph, _ in self.phantoms.values()]
         for eng, st in zip(self.engines, self.streams):
             with self.torch.cuda.stream(st):
                 eng.set_kernel(settings["energy_weights"])
-                N.check(eng.L.ch_plan_prepare(eng.plan, ctypes.byref(g), eng.stream()), "ch_plan_prepare")
+                for shape in dict.fromkeys(shapes):
+                    g = N.grid_struct(shape, (0.0, 0.0, 0.0), spacing)
+                    N.check(eng.L.ch_plan_prepare(eng.plan, ctypes.byref(g), eng.stream()), "ch_plan_prepare")
         self.torch.cuda.synchronize(self.device)
 
     # ------------------------------------------------------- accounting --

@@ -285,16 +285,26 @@ ch_status ch_dda_trace(const ch_grid* grid, int n_rays, const int* starts_dev,
 ch_status ch_cone_directions(ch_plan* plan, float* out_dev, void* stream);
 
 /* Schedule of the cone and TERMA passes (results do not depend on it, up
- * to the float order of the dose sums).  dir_group: unique directions per
- * cone work unit, 1..1024 (default 16; at least the number of unique
- * directions makes one unit per tile); unit_order: 0 = a tile's direction
- * groups are consecutive units (default), 1 = a direction group's tiles are;
+ * to the float rounding of the dose sums).
+ * cone_method: how the collapsed-cone stage (conehead/conehead.py:385-488)
+ *   is evaluated.  CH_CONE_SPECTRAL (default): the stage is one linear
+ *   convolution with the tap stencil of all cone walks, applied through
+ *   forward and inverse 3-D FFTs of period >= 2n - 1 per axis (grids whose
+ *   periods exceed the limit fall back to the gather).  CH_CONE_GATHER: the
+ *   tap stencil is walked tile by tile (shared-memory windows, no atomics but
+ *   one add per output and work unit).  Both give the reference's dose.
+ * dir_group: unique directions per gather work unit, 1..1024 (default 16);
+ * unit_order: 0 = a tile's direction groups are consecutive gather units
+ * (default), 1 = a direction group's tiles are;
  * terma_ctas_per_sm: CTAs per SM of the TERMA pass, 1..32 (default 8).
  * Picked per workload by conehead_gb300.autotune. */
+#define CH_CONE_SPECTRAL 0
+#define CH_CONE_GATHER 1
 typedef struct {
   int dir_group;
   int unit_order;
   int terma_ctas_per_sm;
+  int cone_method;
 } ch_tuning;
 
 ch_status ch_plan_set_tuning(ch_plan* plan, const ch_tuning* tuning);
@@ -303,8 +313,8 @@ ch_status ch_plan_get_tuning(ch_plan* plan, ch_tuning* tuning);
 /* A batch captured once into a CUDA graph and replayed with one launch.
  * ch_batch_create validates the beams like ch_dose_batch, builds every
  * launch record into device memory the batch owns (with its own scratch),
- * and captures the device work -- every beam's prologue, the tap ranges and
- * the one persistent cone launch -- into a graph.  Each ch_batch_launch
+ * and captures the device work -- every beam's prologue and the cone stage
+ * (FFT passes, or tap ranges and the persistent gather) -- into a graph.  Each ch_batch_launch
  * recomputes all doses from the current contents of the density and
  * block-map buffers (which may change in place between launches; the
  * geometry, settings, grids and schedule are fixed at capture).
@@ -322,10 +332,11 @@ void ch_batch_destroy(ch_batch* batch);
 
 /* Build the plan's direction stencils for this grid's voxel spacing and
  * size ahead of the first dose call (otherwise the first call that brings
- * a new spacing or a larger grid builds them).  Serving code prepares each
- * plan for its largest grid once, so no request pays the build.  No
- * counterpart in the reference (it rebuilds everything per call,
- * conehead/conehead.py:541-738). */
+ * a new spacing or a larger grid builds them), and, with the spectral cone
+ * method, the stencil spectrum of exactly this grid shape (one per shape,
+ * counted in ch_plan_memory's tables).  Serving code prepares each plan for
+ * its grids once, so no request pays the build.  No counterpart in the
+ * reference (it rebuilds everything per call, conehead/conehead.py:541-738). */
 ch_status ch_plan_prepare(ch_plan* plan, const ch_grid* grid, void* stream);
 
 /* Device bytes the plan holds: kernel tables and stencils (`tables`), and
