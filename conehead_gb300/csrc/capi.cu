@@ -1303,6 +1303,7 @@ ch_status ch_plan_create(ch_plan** plan, int device) {
   CH_CUDA(cudaGetDeviceProperties(&prop, device));
   if (prop.major < 10) return fail(CH_ERR_DEVICE, "conehead_gb300 needs a Blackwell (sm_10x) GPU");
   CH_CUDA(setup_cone_kernel());
+  CH_CUDA(setup_spec_kernels());
   upload_unit_partials();
   CH_CUDA(cudaGetLastError());
   ch_plan* P = new ch_plan();

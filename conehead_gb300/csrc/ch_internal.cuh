@@ -229,9 +229,11 @@ struct Inter {
 // periods M_k = the power of two >= 2 n_k - 1 (at least SPEC_MIN_PERIOD),
 // pairs of beams per complex transform.
 constexpr int SPEC_THREADS = 256;
+constexpr int SPEC_CTAS_PER_SM = 3;       // register budget of the passes (85 per thread)
 constexpr int SPEC_ELEMS = 4096;          // complex values per CTA: 4096 / M lines of period M
 constexpr int SPEC_MIN_PERIOD = 16, SPEC_MAX_PERIOD = 4096;
 constexpr int SPEC_MAX_PAIRS = 8;         // beam pairs per launch (their work buffers coexist)
+constexpr int SPEC_SMEM = 2 * SPEC_ELEMS * 8;   // two ping-pong buffers of float2 per CTA
 struct SpecPair {
   const float* t1;   // TERMA of the first beam [nx][ny][zp]
   const float* t2;   // of the second (NULL: none)
@@ -255,6 +257,7 @@ struct SpecLaunch {
 int spec_period(int n);
 std::vector<float2> spec_twiddles();      // every period SPEC_MIN_PERIOD .. SPEC_MAX_PERIOD, back to back
 size_t spec_twiddle_offset(int M);
+cudaError_t setup_spec_kernels();        // allow SPEC_SMEM of dynamic shared memory
 void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st);
 // S^ of one grid shape: scatter the stencil values into the real volume
 // s_real (zeroed, [Mx][My][Mz] = L.p[0].t1), then three forward passes

@@ -40,118 +40,171 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
 }
 __device__ __forceinline__ int swz(int i, int c, int L) { return i * L + (c ^ (i & (L - 1))); }
 
-// In-place FFT of L lines of length M held in sm (layout above); INV uses
-// the conjugate twiddles (no 1/M scale).  tw[k] = exp(-2 pi i k / M).
+// 4-point DFT in place (forward: X1 = d02 - i d13; inverse: d02 + i d13)
 template <bool INV>
-__device__ void fft_block(float2* sm, int M, int logM, int L, int logL, const float2* __restrict__ tw) {
+__device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2& a3) {
+  const float2 s02 = make_float2(a0.x + a2.x, a0.y + a2.y), d02 = make_float2(a0.x - a2.x, a0.y - a2.y);
+  const float2 s13 = make_float2(a1.x + a3.x, a1.y + a3.y), d13 = make_float2(a1.x - a3.x, a1.y - a3.y);
+  const float2 mi = INV ? make_float2(-d13.y, d13.x) : make_float2(d13.y, -d13.x);
+  a0 = make_float2(s02.x + s13.x, s02.y + s13.y);
+  a1 = make_float2(d02.x + mi.x, d02.y + mi.y);
+  a2 = make_float2(s02.x - s13.x, s02.y - s13.y);
+  a3 = make_float2(d02.x - mi.x, d02.y - mi.y);
+}
+
+// v times exp(-+i theta) given (cos theta, sin theta)
+template <bool INV>
+__device__ __forceinline__ float2 rot(float2 v, float c, float s) {
+  const float sn = INV ? s : -s;
+  return make_float2(v.x * c - v.y * sn, v.x * sn + v.y * c);
+}
+
+// 16-point DFT in place as 4 x 4: element r = 4a + b, output k = k1 + 4 k2.
+// DFT4 over a for each b, times exp(-+2 pi i b k1 / 16), DFT4 over b for each
+// k1; X[k1 + 4 k2] ends in v[4 k1 + k2].
+template <bool INV>
+__device__ __forceinline__ void dft16(float2 (&v)[16]) {
+  constexpr float C1 = 0.92387953251128674f;   // cos(pi/8)
+  constexpr float S1 = 0.38268343236508977f;   // sin(pi/8)
+  constexpr float R2 = 0.70710678118654752f;   // cos(pi/4)
+#pragma unroll
+  for (int b = 0; b < 4; ++b) dft4<INV>(v[b], v[4 + b], v[8 + b], v[12 + b]);
+  v[5] = rot<INV>(v[5], C1, S1);     // b k1 = 1
+  v[9] = rot<INV>(v[9], R2, R2);     // 2
+  v[13] = rot<INV>(v[13], S1, C1);   // 3
+  v[6] = rot<INV>(v[6], R2, R2);     // 2
+  v[10] = rot<INV>(v[10], 0.0f, 1.0f);   // 4
+  v[14] = rot<INV>(v[14], -R2, R2);  // 6
+  v[7] = rot<INV>(v[7], S1, C1);     // 3
+  v[11] = rot<INV>(v[11], -R2, R2);  // 6
+  v[15] = rot<INV>(v[15], -C1, -S1); // 9
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) dft4<INV>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+}
+
+// FFT of L lines of length M held in src (layout above), ping-ponging with
+// dst; returns the buffer holding the result.  INV uses the conjugate
+// twiddles (no 1/M scale); tw[k] = exp(-2 pi i k / M).  Stockham stages of
+// radix 16 while four or more factors of two remain, then radix 4 and 2 (256
+// points take two stages); a thread holds one butterfly at a time and every
+// stage ends with one barrier.  The caller has synchronised after filling src.
+template <bool INV>
+__device__ float2* fft_block(float2* src, float2* dst, int M, int logM, int L, int logL,
+                             const float2* __restrict__ tw) {
   const int tid = threadIdx.x;
   int Ns = 1, logNs = 0;
   while (Ns < M) {
-    if (logM - logNs >= 2) {
-      // radix 4: butterfly j of line c reads j + r M/4, writes (j - k) 4 + k + r Ns
-      const int MR = M >> 2, nb = L * MR, step = M >> (logNs + 2);
-      float2 v[SPEC_ELEMS / 4 / SPEC_THREADS][4];
+    if (logM - logNs >= 4) {
+      const int MR = M >> 4, nb = L * MR, step = M >> (logNs + 4);
+      for (int bf = tid; bf < nb; bf += SPEC_THREADS) {
+        const int c = bf & (L - 1), j = bf >> logL, k = j & (Ns - 1);
+        float2 v[16];
 #pragma unroll
-      for (int q = 0; q < SPEC_ELEMS / 4 / SPEC_THREADS; ++q) {
-        const int b = tid + q * SPEC_THREADS;
-        if (b < nb) {
-          const int c = b & (L - 1), j = b >> logL;
+        for (int r = 0; r < 16; ++r) v[r] = src[swz(j + r * MR, c, L)];
+        if (k) {
 #pragma unroll
-          for (int r = 0; r < 4; ++r) v[q][r] = sm[swz(j + r * MR, c, L)];
-        }
-      }
-      __syncthreads();
-#pragma unroll
-      for (int q = 0; q < SPEC_ELEMS / 4 / SPEC_THREADS; ++q) {
-        const int b = tid + q * SPEC_THREADS;
-        if (b < nb) {
-          const int c = b & (L - 1), j = b >> logL, k = j & (Ns - 1);
-#pragma unroll
-          for (int r = 1; r < 4; ++r) {
+          for (int r = 1; r < 16; ++r) {
             float2 w = __ldg(tw + r * k * step);
             if (INV) w.y = -w.y;
-            v[q][r] = cmul(v[q][r], w);
+            v[r] = cmul(v[r], w);
           }
-          const float2 a0 = v[q][0], a1 = v[q][1], a2 = v[q][2], a3 = v[q][3];
-          const float2 s02 = make_float2(a0.x + a2.x, a0.y + a2.y), d02 = make_float2(a0.x - a2.x, a0.y - a2.y);
-          const float2 s13 = make_float2(a1.x + a3.x, a1.y + a3.y), d13 = make_float2(a1.x - a3.x, a1.y - a3.y);
-          // forward: X1 = d02 - i d13, X3 = d02 + i d13 (inverse: the other way round)
-          const float2 mi = INV ? make_float2(-d13.y, d13.x) : make_float2(d13.y, -d13.x);   // -+i d13
-          const int o = ((j - k) << 2) + k;
-          sm[swz(o, c, L)] = make_float2(s02.x + s13.x, s02.y + s13.y);
-          sm[swz(o + Ns, c, L)] = make_float2(d02.x + mi.x, d02.y + mi.y);
-          sm[swz(o + 2 * Ns, c, L)] = make_float2(s02.x - s13.x, s02.y - s13.y);
-          sm[swz(o + 3 * Ns, c, L)] = make_float2(d02.x - mi.x, d02.y - mi.y);
         }
+        dft16<INV>(v);
+        const int o = ((j - k) << 4) + k;
+#pragma unroll
+        for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+          for (int k2 = 0; k2 < 4; ++k2) dst[swz(o + (k1 + 4 * k2) * Ns, c, L)] = v[4 * k1 + k2];
       }
-      __syncthreads();
+      Ns <<= 4;
+      logNs += 4;
+    } else if (logM - logNs >= 2) {
+      const int MR = M >> 2, nb = L * MR, step = M >> (logNs + 2);
+      for (int bf = tid; bf < nb; bf += SPEC_THREADS) {
+        const int c = bf & (L - 1), j = bf >> logL, k = j & (Ns - 1);
+        float2 v[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) v[r] = src[swz(j + r * MR, c, L)];
+#pragma unroll
+        for (int r = 1; r < 4; ++r) {
+          float2 w = __ldg(tw + r * k * step);
+          if (INV) w.y = -w.y;
+          v[r] = cmul(v[r], w);
+        }
+        dft4<INV>(v[0], v[1], v[2], v[3]);
+        const int o = ((j - k) << 2) + k;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) dst[swz(o + r * Ns, c, L)] = v[r];
+      }
       Ns <<= 2;
       logNs += 2;
     } else {
-      // radix 2 (the last stage when log2 M is odd)
       const int MR = M >> 1, nb = L * MR, step = M >> (logNs + 1);
-      float2 v[SPEC_ELEMS / 2 / SPEC_THREADS][2];
-#pragma unroll
-      for (int q = 0; q < SPEC_ELEMS / 2 / SPEC_THREADS; ++q) {
-        const int b = tid + q * SPEC_THREADS;
-        if (b < nb) {
-          const int c = b & (L - 1), j = b >> logL;
-          v[q][0] = sm[swz(j, c, L)];
-          v[q][1] = sm[swz(j + MR, c, L)];
-        }
+      for (int bf = tid; bf < nb; bf += SPEC_THREADS) {
+        const int c = bf & (L - 1), j = bf >> logL, k = j & (Ns - 1);
+        float2 w = __ldg(tw + k * step);
+        if (INV) w.y = -w.y;
+        const float2 a0 = src[swz(j, c, L)], a1 = cmul(src[swz(j + MR, c, L)], w);
+        const int o = ((j - k) << 1) + k;
+        dst[swz(o, c, L)] = make_float2(a0.x + a1.x, a0.y + a1.y);
+        dst[swz(o + Ns, c, L)] = make_float2(a0.x - a1.x, a0.y - a1.y);
       }
-      __syncthreads();
-#pragma unroll
-      for (int q = 0; q < SPEC_ELEMS / 2 / SPEC_THREADS; ++q) {
-        const int b = tid + q * SPEC_THREADS;
-        if (b < nb) {
-          const int c = b & (L - 1), j = b >> logL, k = j & (Ns - 1);
-          float2 w = __ldg(tw + k * step);
-          if (INV) w.y = -w.y;
-          const float2 a0 = v[q][0], a1 = cmul(v[q][1], w);
-          const int o = ((j - k) << 1) + k;
-          sm[swz(o, c, L)] = make_float2(a0.x + a1.x, a0.y + a1.y);
-          sm[swz(o + Ns, c, L)] = make_float2(a0.x - a1.x, a0.y - a1.y);
-        }
-      }
-      __syncthreads();
       Ns <<= 1;
       logNs += 1;
     }
+    __syncthreads();
+    float2* t = src;
+    src = dst;
+    dst = t;
   }
+  return src;
 }
 
 // ---------------------------------------------------------------- passes --
 // z forward: lines (x, y), TERMA pair in, A out.  One CTA per L lines and pair.
-__global__ void __launch_bounds__(SPEC_THREADS) spec_z_forward_kernel(SpecLaunch P) {
-  __shared__ float2 sm[SPEC_ELEMS];
+__global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward_kernel(SpecLaunch P) {
+  extern __shared__ float2 spec_sm[];
+  float2* sm = spec_sm;
+  float2* sm2 = spec_sm + SPEC_ELEMS;
   const SpecPair& pr = P.p[blockIdx.y];
   const int Mz = P.g.M[2], logMz = P.g.logM[2];
   const int logL = 12 - logMz, L = 1 << logL;
   const int nl = P.g.n[0] * P.g.n[1], nz = P.g.n[2];
   const int l0 = blockIdx.x * L;
-  for (int e = threadIdx.x; e < SPEC_ELEMS; e += SPEC_THREADS) {
-    const int i = e & (Mz - 1), c = e >> logMz, l = l0 + c;
-    float2 v = make_float2(0.0f, 0.0f);
-    if (l < nl && i < nz) {
-      const size_t o = (size_t)l * P.g.zp + i;
-      v.x = pr.t1[o];
-      if (pr.t2) v.y = pr.t2[o];
+  {
+    // every load of the thread first, then the shared-memory stores
+    float2 v[SPEC_ELEMS / SPEC_THREADS];
+#pragma unroll
+    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
+      const int e = threadIdx.x + q * SPEC_THREADS;
+      const int i = e & (Mz - 1), c = e >> logMz, l = l0 + c;
+      v[q] = make_float2(0.0f, 0.0f);
+      if (l < nl && i < nz) {
+        const size_t o = (size_t)l * P.g.zp + i;
+        v[q].x = __ldg(pr.t1 + o);
+        if (pr.t2) v[q].y = __ldg(pr.t2 + o);
+      }
     }
-    sm[swz(i, c, L)] = v;
+#pragma unroll
+    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
+      const int e = threadIdx.x + q * SPEC_THREADS;
+      sm[swz(e & (Mz - 1), e >> logMz, L)] = v[q];
+    }
   }
   __syncthreads();
-  fft_block<false>(sm, Mz, logMz, L, logL, P.g.tw[2]);
+  const float2* res = fft_block<false>(sm, sm2, Mz, logMz, L, logL, P.g.tw[2]);
   for (int e = threadIdx.x; e < SPEC_ELEMS; e += SPEC_THREADS) {
     const int i = e & (Mz - 1), c = e >> logMz, l = l0 + c;
-    if (l < nl) pr.a[(size_t)l * Mz + i] = sm[swz(i, c, L)];
+    if (l < nl) pr.a[(size_t)l * Mz + i] = res[swz(i, c, L)];
   }
 }
 
 // y forward (A -> B) or inverse (B -> A): lines (x, kz) in blocks of L kz.
 template <bool INV>
-__global__ void __launch_bounds__(SPEC_THREADS) spec_y_kernel(SpecLaunch P) {
-  __shared__ float2 sm[SPEC_ELEMS];
+__global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_y_kernel(SpecLaunch P) {
+  extern __shared__ float2 spec_sm[];
+  float2* sm = spec_sm;
+  float2* sm2 = spec_sm + SPEC_ELEMS;
   const SpecPair& pr = P.p[blockIdx.y];
   const int My = P.g.M[1], logMy = P.g.logM[1], Mz = P.g.M[2], logMz = P.g.logM[2];
   const int logL = min(12 - logMy, logMz), L = 1 << logL;
@@ -163,15 +216,25 @@ __global__ void __launch_bounds__(SPEC_THREADS) spec_y_kernel(SpecLaunch P) {
   float2* dst = INV ? pr.a + (size_t)x * ny * Mz : pr.b + (size_t)x * My * Mz;
   src += kz0;
   dst += kz0;
-  for (int e = threadIdx.x; e < (L << logMy); e += SPEC_THREADS) {
-    const int c = e & (L - 1), i = e >> logL;
-    sm[swz(i, c, L)] = i < n_in ? src[(size_t)i * Mz + c] : make_float2(0.0f, 0.0f);
+  {
+    float2 v[SPEC_ELEMS / SPEC_THREADS];
+#pragma unroll
+    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
+      const int e = threadIdx.x + q * SPEC_THREADS;
+      const int c = e & (L - 1), i = e >> logL;
+      v[q] = (e < (L << logMy) && i < n_in) ? src[(size_t)i * Mz + c] : make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
+      const int e = threadIdx.x + q * SPEC_THREADS;
+      if (e < (L << logMy)) sm[swz(e >> logL, e & (L - 1), L)] = v[q];
+    }
   }
   __syncthreads();
-  fft_block<INV>(sm, My, logMy, L, logL, P.g.tw[1]);
+  const float2* res = fft_block<INV>(sm, sm2, My, logMy, L, logL, P.g.tw[1]);
   for (int e = threadIdx.x; e < n_out * L; e += SPEC_THREADS) {
     const int c = e & (L - 1), i = e >> logL;
-    dst[(size_t)i * Mz + c] = sm[swz(i, c, L)];
+    dst[(size_t)i * Mz + c] = res[swz(i, c, L)];
   }
 }
 
@@ -180,8 +243,10 @@ __global__ void __launch_bounds__(SPEC_THREADS) spec_y_kernel(SpecLaunch P) {
 // CONV: forward, times S^ (or its conjugate), inverse, x < nx kept;
 // otherwise forward only over the full period (building S^).
 template <bool CONV>
-__global__ void __launch_bounds__(SPEC_THREADS) spec_x_kernel(SpecLaunch P) {
-  __shared__ float2 sm[SPEC_ELEMS];
+__global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(SpecLaunch P) {
+  extern __shared__ float2 spec_sm[];
+  float2* sm = spec_sm;
+  float2* sm2 = spec_sm + SPEC_ELEMS;
   const int pair = blockIdx.x % P.n_pairs, blk = blockIdx.x / P.n_pairs;
   const SpecPair& pr = P.p[pair];
   const int Mx = P.g.M[0], logMx = P.g.logM[0], My = P.g.M[1], Mz = P.g.M[2], logMz = P.g.logM[2];
@@ -191,48 +256,79 @@ __global__ void __launch_bounds__(SPEC_THREADS) spec_x_kernel(SpecLaunch P) {
   const size_t xs = (size_t)My * Mz, off = (size_t)ky * Mz + kz0;
   float2* b = pr.b + off;
   const int nx = CONV ? P.g.n[0] : Mx;
-  for (int e = threadIdx.x; e < (L << logMx); e += SPEC_THREADS) {
-    const int c = e & (L - 1), i = e >> logL;
-    sm[swz(i, c, L)] = i < nx ? b[(size_t)i * xs + c] : make_float2(0.0f, 0.0f);
+  {
+    float2 v[SPEC_ELEMS / SPEC_THREADS];
+#pragma unroll
+    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
+      const int e = threadIdx.x + q * SPEC_THREADS;
+      const int c = e & (L - 1), i = e >> logL;
+      v[q] = (e < (L << logMx) && i < nx) ? b[(size_t)i * xs + c] : make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
+      const int e = threadIdx.x + q * SPEC_THREADS;
+      if (e < (L << logMx)) sm[swz(e >> logL, e & (L - 1), L)] = v[q];
+    }
   }
   __syncthreads();
-  fft_block<false>(sm, Mx, logMx, L, logL, P.g.tw[0]);
+  float2* res = fft_block<false>(sm, sm2, Mx, logMx, L, logL, P.g.tw[0]);
   if (CONV) {
     const float2* sh = P.g.shat + off;
-    for (int e = threadIdx.x; e < (L << logMx); e += SPEC_THREADS) {
-      const int c = e & (L - 1), i = e >> logL;
-      float2 s = __ldg(sh + (size_t)i * xs + c);
-      if (P.g.conj) s.y = -s.y;
-      const int k = swz(i, c, L);
-      sm[k] = cmul(sm[k], s);
+    float2 sv[SPEC_ELEMS / SPEC_THREADS];
+#pragma unroll
+    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
+      const int e = threadIdx.x + q * SPEC_THREADS;
+      sv[q] = e < (L << logMx) ? __ldg(sh + (size_t)(e >> logL) * xs + (e & (L - 1))) : make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
+      const int e = threadIdx.x + q * SPEC_THREADS;
+      if (e < (L << logMx)) {
+        float2 s = sv[q];
+        if (P.g.conj) s.y = -s.y;
+        const int k = swz(e >> logL, e & (L - 1), L);
+        res[k] = cmul(res[k], s);
+      }
     }
     __syncthreads();
-    fft_block<true>(sm, Mx, logMx, L, logL, P.g.tw[0]);
+    res = fft_block<true>(res, res == sm ? sm2 : sm, Mx, logMx, L, logL, P.g.tw[0]);
   }
   for (int e = threadIdx.x; e < nx * L; e += SPEC_THREADS) {
     const int c = e & (L - 1), i = e >> logL;
-    b[(size_t)i * xs + c] = sm[swz(i, c, L)];
+    b[(size_t)i * xs + c] = res[swz(i, c, L)];
   }
 }
 
 // z inverse: lines (x, y), A in, dose pair out (real part, imaginary part).
-__global__ void __launch_bounds__(SPEC_THREADS) spec_z_inverse_kernel(SpecLaunch P) {
-  __shared__ float2 sm[SPEC_ELEMS];
+__global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_inverse_kernel(SpecLaunch P) {
+  extern __shared__ float2 spec_sm[];
+  float2* sm = spec_sm;
+  float2* sm2 = spec_sm + SPEC_ELEMS;
   const SpecPair& pr = P.p[blockIdx.y];
   const int Mz = P.g.M[2], logMz = P.g.logM[2];
   const int logL = 12 - logMz, L = 1 << logL;
   const int nl = P.g.n[0] * P.g.n[1], nz = P.g.n[2];
   const int l0 = blockIdx.x * L;
-  for (int e = threadIdx.x; e < SPEC_ELEMS; e += SPEC_THREADS) {
-    const int i = e & (Mz - 1), c = e >> logMz, l = l0 + c;
-    sm[swz(i, c, L)] = l < nl ? pr.a[(size_t)l * Mz + i] : make_float2(0.0f, 0.0f);
+  {
+    float2 v[SPEC_ELEMS / SPEC_THREADS];
+#pragma unroll
+    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
+      const int e = threadIdx.x + q * SPEC_THREADS;
+      const int l = l0 + (e >> logMz);
+      v[q] = l < nl ? pr.a[(size_t)l * Mz + (e & (Mz - 1))] : make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
+      const int e = threadIdx.x + q * SPEC_THREADS;
+      sm[swz(e & (Mz - 1), e >> logMz, L)] = v[q];
+    }
   }
   __syncthreads();
-  fft_block<true>(sm, Mz, logMz, L, logL, P.g.tw[2]);
+  const float2* res = fft_block<true>(sm, sm2, Mz, logMz, L, logL, P.g.tw[2]);
   for (int e = threadIdx.x; e < SPEC_ELEMS; e += SPEC_THREADS) {
     const int i = e & (Mz - 1), c = e >> logMz, l = l0 + c;
     if (l < nl && i < nz) {
-      const float2 v = sm[swz(i, c, L)];
+      const float2 v = res[swz(i, c, L)];
       pr.d1[(size_t)l * nz + i] = v.x;
       if (pr.d2) pr.d2[(size_t)l * nz + i] = v.y;
     }
@@ -264,17 +360,26 @@ std::vector<float2> spec_twiddles() {
 
 size_t spec_twiddle_offset(int M) { return (size_t)M - SPEC_MIN_PERIOD; }
 
+cudaError_t setup_spec_kernels() {
+  cudaError_t e = cudaSuccess;
+  for (const void* f : {(const void*)spec_z_forward_kernel, (const void*)spec_y_kernel<false>,
+                        (const void*)spec_y_kernel<true>, (const void*)spec_x_kernel<false>,
+                        (const void*)spec_x_kernel<true>, (const void*)spec_z_inverse_kernel})
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_SMEM);
+  return e;
+}
+
 void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
   const SpecGrid& g = L.g;
   const int nl = g.n[0] * g.n[1];
   const int Lz = SPEC_ELEMS / g.M[2];
   const int Ly = std::min(SPEC_ELEMS / g.M[1], g.M[2]);
   const int Lx = std::min(SPEC_ELEMS / g.M[0], g.M[2]);
-  spec_z_forward_kernel<<<dim3((nl + Lz - 1) / Lz, L.n_pairs), SPEC_THREADS, 0, st>>>(L);
-  spec_y_kernel<false><<<dim3(g.n[0] * (g.M[2] / Ly), L.n_pairs), SPEC_THREADS, 0, st>>>(L);
-  spec_x_kernel<true><<<g.M[1] * (g.M[2] / Lx) * L.n_pairs, SPEC_THREADS, 0, st>>>(L);
-  spec_y_kernel<true><<<dim3(g.n[0] * (g.M[2] / Ly), L.n_pairs), SPEC_THREADS, 0, st>>>(L);
-  spec_z_inverse_kernel<<<dim3((nl + Lz - 1) / Lz, L.n_pairs), SPEC_THREADS, 0, st>>>(L);
+  spec_z_forward_kernel<<<dim3((nl + Lz - 1) / Lz, L.n_pairs), SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  spec_y_kernel<false><<<dim3(g.n[0] * (g.M[2] / Ly), L.n_pairs), SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  spec_x_kernel<true><<<g.M[1] * (g.M[2] / Lx) * L.n_pairs, SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  spec_y_kernel<true><<<dim3(g.n[0] * (g.M[2] / Ly), L.n_pairs), SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  spec_z_inverse_kernel<<<dim3((nl + Lz - 1) / Lz, L.n_pairs), SPEC_THREADS, SPEC_SMEM, st>>>(L);
 }
 
 void launch_spec_build(const SpecLaunch& L, const long long* idx, const float* val, int n_val, float* s_real,
@@ -285,9 +390,9 @@ void launch_spec_build(const SpecLaunch& L, const long long* idx, const float* v
   const int Ly = std::min(SPEC_ELEMS / g.M[1], g.M[2]);
   const int Lx = std::min(SPEC_ELEMS / g.M[0], g.M[2]);
   if (n_val > 0) spec_scatter_kernel<<<(n_val + 255) / 256, 256, 0, st>>>(idx, val, n_val, s_real);
-  spec_z_forward_kernel<<<dim3((nl + Lz - 1) / Lz, 1), SPEC_THREADS, 0, st>>>(L);
-  spec_y_kernel<false><<<dim3(g.n[0] * (g.M[2] / Ly), 1), SPEC_THREADS, 0, st>>>(L);
-  spec_x_kernel<false><<<g.M[1] * (g.M[2] / Lx), SPEC_THREADS, 0, st>>>(L);
+  spec_z_forward_kernel<<<dim3((nl + Lz - 1) / Lz, 1), SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  spec_y_kernel<false><<<dim3(g.n[0] * (g.M[2] / Ly), 1), SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  spec_x_kernel<false><<<g.M[1] * (g.M[2] / Lx), SPEC_THREADS, SPEC_SMEM, st>>>(L);
 }
 
 }  // namespace ch
