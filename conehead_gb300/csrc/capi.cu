@@ -138,7 +138,7 @@ struct ch_plan {
   std::vector<std::unique_ptr<SpecEntry>> spec;   // S^ by grid shape and stencil set
   DevBuf spec_tw;            // FFT twiddles of every period
   // scratch
-  DevBuf T, aabb, counters, ranges, cranges, cone_beams, range_beams, list_v, spec_work;
+  DevBuf T, aabb, counters, ranges, cranges, cone_beams, range_beams, list_v, spec_work, pro_beams;
   DevBuf adj_in, adj_out, adj_w;   // cone-operator input (padded), output, beamlet gradient (float64)
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaStream_t last_stream = nullptr;
@@ -158,7 +158,7 @@ struct ch_plan {
       if (rec_pending[i] && ev_rec[i]) cudaEventSynchronize(ev_rec[i]);
     spec.clear();
     for (DevBuf* b : {&K, &theta, &phi, &T, &aabb, &counters, &ranges, &cranges, &cone_beams, &range_beams, &list_v,
-                      &spec_work, &spec_tw, &adj_in, &adj_out, &adj_w})
+                      &spec_work, &pro_beams, &spec_tw, &adj_in, &adj_out, &adj_w})
       b->release();
     for (StencilSet* S : {&st, &st_adj})
       for (DevBuf* b : S->bufs()) b->release();
@@ -778,6 +778,7 @@ struct BeamJob {
   float* dose;
   size_t t_off;        // float offset in the T arena
   size_t r_off;        // uint32 offset in the ranges arena
+  size_t l_off;        // int offset of the beam's voxel list
   int ntile[3];
   int n_tiles;
   int n_units;
@@ -805,25 +806,37 @@ ch_status encode_windows(PFN_cuTensorMapEncodeTiled_v12000 enc, ConeBeam& C, flo
 
 // Upload launch records through the plan's double-buffered pinned staging
 // (a true async copy, issued before the kernels that read them).
-ch_status stage_records(ch_plan* P, const ConeBeam* cb, const RangeBeam* rb, int n, cudaStream_t s) {
+// One host array staged to a device buffer.
+struct Seg {
+  void* dst;
+  const void* src;
+  size_t bytes;
+};
+
+// Launch records go through pinned, double-buffered staging so their upload
+// is a true asynchronous copy: the buffer used two calls ago is reused once
+// its upload has been read.
+ch_status stage_records(ch_plan* P, const std::vector<Seg>& segs, cudaStream_t s) {
   const int hb = P->rec_next;
   P->rec_next ^= 1;
   if (P->rec_pending[hb]) CH_CUDA(cudaEventSynchronize(P->ev_rec[hb]));
   P->rec_pending[hb] = false;
-  const size_t cb_bytes = n * sizeof(ConeBeam), rb_bytes = n * sizeof(RangeBeam);
-  if (cb_bytes + rb_bytes > P->h_rec_bytes[hb]) {
+  size_t total = 0;
+  for (const Seg& g : segs) total += (g.bytes + 255) / 256 * 256;
+  if (total > P->h_rec_bytes[hb]) {
     if (P->h_rec[hb]) CH_CUDA(cudaFreeHost(P->h_rec[hb]));
     P->h_rec[hb] = nullptr;
     P->h_rec_bytes[hb] = 0;
-    CH_CUDA(cudaMallocHost(&P->h_rec[hb], cb_bytes + rb_bytes));
-    P->h_rec_bytes[hb] = cb_bytes + rb_bytes;
+    CH_CUDA(cudaMallocHost(&P->h_rec[hb], total));
+    P->h_rec_bytes[hb] = total;
   }
   if (!P->ev_rec[hb]) CH_CUDA(cudaEventCreateWithFlags(&P->ev_rec[hb], cudaEventDisableTiming));
   char* h = static_cast<char*>(P->h_rec[hb]);
-  std::memcpy(h, cb, cb_bytes);
-  std::memcpy(h + cb_bytes, rb, rb_bytes);
-  CH_CUDA(cudaMemcpyAsync(P->cone_beams.p, h, cb_bytes, cudaMemcpyHostToDevice, s));
-  CH_CUDA(cudaMemcpyAsync(P->range_beams.p, h + cb_bytes, rb_bytes, cudaMemcpyHostToDevice, s));
+  for (const Seg& g : segs) {
+    std::memcpy(h, g.src, g.bytes);
+    CH_CUDA(cudaMemcpyAsync(g.dst, h, g.bytes, cudaMemcpyHostToDevice, s));
+    h += (g.bytes + 255) / 256 * 256;
+  }
   CH_CUDA(cudaEventRecord(P->ev_rec[hb], s));
   P->rec_pending[hb] = true;
   return CH_OK;
@@ -906,16 +919,17 @@ bool spec_batch(const ch_plan* P, int n, const ch_grid* grids) {
 }
 
 // Scratch arena sizes of one batch, in the order T, aabb, counters, ranges,
-// cranges, cone_beams, range_beams, list_v, spectral work (the buffers run()
-// grows); the gather's tables are empty for a spectral batch.
-constexpr int N_SCRATCH = 9;
+// cranges, cone_beams, range_beams, list_v (every beam's voxel list),
+// spectral work, prologue records (the buffers run() grows); the gather's
+// tables are empty for a spectral batch.
+constexpr int N_SCRATCH = 10;
 struct ScratchNeed {
   size_t bytes[N_SCRATCH];
 };
 
 ScratchNeed scratch_need(int n, const ch_grid* grids, int U, bool spectral = false) {
   if (spectral) U = 0;
-  size_t t_total = 0, r_total = 0, max_vox = 1;
+  size_t t_total = 0, r_total = 0, l_total = 0;
   for (int i = 0; i < n; ++i) {
     const size_t zp = (size_t)round_up(grids[i].n[2], 4);
     t_total += (size_t)grids[i].n[0] * grids[i].n[1] * zp;
@@ -923,7 +937,7 @@ ScratchNeed scratch_need(int n, const ch_grid* grids, int U, bool spectral = fal
     const size_t tiles = (size_t)((grids[i].n[0] + TX - 1) / TX) * ((grids[i].n[1] + TY - 1) / TY) *
                          ((grids[i].n[2] + TZ - 1) / TZ);
     r_total += tiles * U;
-    max_vox = std::max(max_vox, (size_t)grids[i].n[0] * grids[i].n[1] * grids[i].n[2]);
+    l_total += ((size_t)grids[i].n[0] * grids[i].n[1] * grids[i].n[2] + 63) / 64 * 64;
   }
   ScratchNeed r;
   r.bytes[0] = t_total * sizeof(float);
@@ -933,14 +947,15 @@ ScratchNeed scratch_need(int n, const ch_grid* grids, int U, bool spectral = fal
   r.bytes[4] = r.bytes[3];
   r.bytes[5] = (size_t)n * sizeof(ConeBeam);
   r.bytes[6] = (size_t)n * sizeof(RangeBeam);
-  r.bytes[7] = max_vox * sizeof(int);
+  r.bytes[7] = std::max<size_t>(l_total, 1) * sizeof(int);
   r.bytes[8] = spectral ? spec_layout(n, grids).arena * sizeof(float2) : 0;
+  r.bytes[9] = (size_t)n * sizeof(PrologueBeam);
   return r;
 }
 
 const DevBuf* scratch_bufs(const ch_plan* P, int k) {
-  const DevBuf* b[N_SCRATCH] = {&P->T,          &P->aabb,        &P->counters, &P->ranges,   &P->cranges,
-                                &P->cone_beams, &P->range_beams, &P->list_v,   &P->spec_work};
+  const DevBuf* b[N_SCRATCH] = {&P->T,          &P->aabb,        &P->counters, &P->ranges,    &P->cranges,
+                                &P->cone_beams, &P->range_beams, &P->list_v,   &P->spec_work, &P->pro_beams};
   return b[k];
 }
 
@@ -966,6 +981,7 @@ struct Scratch {
   RangeBeam* range_beams;
   int* list_v;
   float2* spec;           // spectral work arena
+  PrologueBeam* pro;      // batched prologue records
 };
 
 ch_status plan_batch(ch_plan* P, int n, const ch_grid* grids, const float* const* rho, const int* swap_xy,
@@ -1010,7 +1026,7 @@ ch_status plan_batch(ch_plan* P, int n, const ch_grid* grids, const float* const
     }
   }
   const int n_groups = (B.U + P->tuning.dir_group - 1) / P->tuning.dir_group;
-  size_t t_total = 0, r_total = 0;
+  size_t t_total = 0, r_total = 0, l_total = 0;
   B.total_units = 0;
   B.max_tiles = 0;
   for (int i = 0; i < n; ++i) {
@@ -1031,6 +1047,8 @@ ch_status plan_batch(ch_plan* P, int n, const ch_grid* grids, const float* const
     J.t_off = t_total;
     t_total += (size_t)J.g.n[0] * J.g.n[1] * J.g.zp;
     t_total = (t_total + 63) / 64 * 64;
+    J.l_off = l_total;
+    l_total += ((size_t)J.g.n[0] * J.g.n[1] * J.g.n[2] + 63) / 64 * 64;
     J.ntile[0] = (J.g.n[0] + TX - 1) / TX;
     J.ntile[1] = (J.g.n[1] + TY - 1) / TY;
     J.ntile[2] = (J.g.n[2] + TZ - 1) / TZ;
@@ -1087,6 +1105,24 @@ ch_status make_records(const BatchPlan& B, const Scratch& S, std::vector<ConeBea
   return CH_OK;
 }
 
+// Records of the batched prologue, pointing into scratch S.
+std::vector<PrologueBeam> make_prologue_records(const BatchPlan& B, const Scratch& S) {
+  std::vector<PrologueBeam> pb(B.jobs.size());
+  for (size_t i = 0; i < B.jobs.size(); ++i) {
+    const BeamJob& J = B.jobs[i];
+    PrologueBeam& R = pb[i];
+    std::memset(&R, 0, sizeof(R));
+    R.g = J.g;
+    R.b = J.b;
+    R.s = J.s;
+    R.rho = J.rho;
+    R.T = S.T + J.t_off;
+    R.aabb = S.aabb + 8 * i;
+    R.list_v = S.list_v + J.l_off;
+  }
+  return pb;
+}
+
 // Device view of the optional intermediates; all = 1 when a per-voxel output
 // other than blocked/TERMA is wanted (every voxel is then evaluated).
 Inter make_inter(const ch_intermediates* inter, int& all) {
@@ -1116,13 +1152,21 @@ ch_status enqueue_batch(ch_plan* P, const BatchPlan& B, const Scratch& S, const 
   unsigned long long* updates = reinterpret_cast<unsigned long long*>(S.counters + 2);
   if (ev) CH_CUDA(cudaEventRecord(ev[0], s));
   launch_init_scratch(S.aabb, n, S.counters, s);
-  for (int i = 0; i < n; ++i) {
-    const BeamJob& J = B.jobs[i];
-    int all = 0;
-    const Inter in = make_inter(inter, all);
-    // the voxel list is reused beam after beam (stream order)
-    launch_prologue(J.rho, J.g, J.b, J.s, S.T + J.t_off, in, all, S.aabb + 8 * i, S.list_v, P->n_sm, flags, s,
-                    P->tuning.terma_ctas_per_sm);
+  if (inter) {
+    // intermediates wanted: the per-beam prologue writes them
+    for (int i = 0; i < n; ++i) {
+      const BeamJob& J = B.jobs[i];
+      int all = 0;
+      const Inter in = make_inter(inter, all);
+      launch_prologue(J.rho, J.g, J.b, J.s, S.T + J.t_off, in, all, S.aabb + 8 * i, S.list_v + J.l_off, P->n_sm,
+                      flags, s, P->tuning.terma_ctas_per_sm);
+      CH_CUDA(cudaGetLastError());
+    }
+  } else {
+    // every beam's prologue in one cull and one TERMA launch (records staged)
+    long long max_vox = 1;
+    for (const BeamJob& J : B.jobs) max_vox = std::max(max_vox, (long long)J.g.n[0] * J.g.n[1] * J.g.n[2]);
+    launch_prologue_batch(S.pro, n, max_vox, P->n_sm, flags, s, P->tuning.terma_ctas_per_sm);
     CH_CUDA(cudaGetLastError());
   }
   if (ev) CH_CUDA(cudaEventRecord(ev[1], s));
@@ -1172,7 +1216,8 @@ ch_status run_group(ch_plan* P, int n, const ch_grid* grids, const float* const*
   for (int k = 0; k < N_SCRATCH; ++k) CH_CUDA(const_cast<DevBuf*>(scratch_bufs(P, k))->ensure(need.bytes[k]));
   const Scratch S{P->T.as<float>(),          P->aabb.as<int>(),           P->counters.as<int>(),
                   P->ranges.as<uint32_t>(),  P->cranges.as<uint32_t>(),   P->cone_beams.as<ConeBeam>(),
-                  P->range_beams.as<RangeBeam>(), P->list_v.as<int>(),    P->spec_work.as<float2>()};
+                  P->range_beams.as<RangeBeam>(), P->list_v.as<int>(),    P->spec_work.as<float2>(),
+                  P->pro_beams.as<PrologueBeam>()};
   for (auto& e : P->ev)
     if (!e) CH_CUDA(cudaEventCreate(&e));
   P->stats = ch_stats{};
@@ -1188,7 +1233,8 @@ ch_status run_group(ch_plan* P, int n, const ch_grid* grids, const float* const*
       const BeamJob& J = B.jobs[i];
       int all = 0;
       const Inter in = make_inter(inter, all);
-      launch_prologue(J.rho, J.g, J.b, J.s, S.T + J.t_off, in, all, S.aabb + 8 * i, S.list_v, P->n_sm, flags, s,
+      launch_prologue(J.rho, J.g, J.b, J.s, S.T + J.t_off, in, all, S.aabb + 8 * i, S.list_v + J.l_off, P->n_sm,
+                      flags, s,
                       P->tuning.terma_ctas_per_sm);
       CH_CUDA(cudaGetLastError());
     }
@@ -1209,12 +1255,17 @@ ch_status run_group(ch_plan* P, int n, const ch_grid* grids, const float* const*
     CH_CUDA(cudaEventRecord(P->ev[3], s));
     return CH_OK;
   }
+  const std::vector<PrologueBeam> pb = make_prologue_records(B, S);
+  std::vector<Seg> segs;
+  if (!inter) segs.push_back(Seg{S.pro, pb.data(), pb.size() * sizeof(PrologueBeam)});
+  std::vector<ConeBeam> cb;
+  std::vector<RangeBeam> rb;
   if (!B.spectral) {
-    std::vector<ConeBeam> cb;
-    std::vector<RangeBeam> rb;
     if ((st = make_records(B, S, cb, rb)) != CH_OK) return st;
-    if ((st = stage_records(P, cb.data(), rb.data(), n, s)) != CH_OK) return st;
+    segs.push_back(Seg{S.cone_beams, cb.data(), cb.size() * sizeof(ConeBeam)});
+    segs.push_back(Seg{S.range_beams, rb.data(), rb.size() * sizeof(RangeBeam)});
   }
+  if (!segs.empty() && (st = stage_records(P, segs, s)) != CH_OK) return st;
   if ((st = enqueue_batch(P, B, S, inter, P->ev, s)) != CH_OK) return st;
   P->stats.n_units = B.spectral ? 0 : B.total_units;
   return CH_OK;
@@ -1581,7 +1632,8 @@ ch_status cone_operator(ch_plan* P, const ch_grid& grid, const float* in_dense, 
       R.opk0[j] = out_planes->pk0[j];
     }
   }
-  if ((st = stage_records(P, &C, &R, 1, s)) != CH_OK) return st;
+  if ((st = stage_records(P, {Seg{P->cone_beams.p, &C, sizeof(C)}, Seg{P->range_beams.p, &R, sizeof(R)}}, s)) != CH_OK)
+    return st;
   // input into the padded layout the window tensor maps read
   CH_CUDA(cudaMemcpy2DAsync(P->adj_in.p, (size_t)g.zp * sizeof(float), in_dense, (size_t)g.n[2] * sizeof(float),
                             (size_t)g.n[2] * sizeof(float), (size_t)g.n[0] * g.n[1], cudaMemcpyDeviceToDevice, s));
@@ -1697,13 +1749,14 @@ struct ch_batch {
   ch_plan* P = nullptr;
   int n = 0;
   int total_units = 0;
-  DevBuf T, aabb, counters, ranges, cranges, cone_beams, range_beams, list_v, spec_work;
+  DevBuf T, aabb, counters, ranges, cranges, cone_beams, range_beams, list_v, spec_work, pro_beams;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   ~ch_batch() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
-    for (DevBuf* b : {&T, &aabb, &counters, &ranges, &cranges, &cone_beams, &range_beams, &list_v, &spec_work})
+    for (DevBuf* b : {&T, &aabb, &counters, &ranges, &cranges, &cone_beams, &range_beams, &list_v, &spec_work,
+                      &pro_beams})
       b->release();
   }
 };
@@ -1724,13 +1777,19 @@ ch_status ch_batch_create(ch_plan* P, int n, const ch_grid* grids, const float* 
   bt->n = n;
   bt->total_units = B.total_units;
   const ScratchNeed need = scratch_need(n, grids, B.U, B.spectral);
-  DevBuf* bufs[N_SCRATCH] = {&bt->T,          &bt->aabb,        &bt->counters, &bt->ranges,   &bt->cranges,
-                             &bt->cone_beams, &bt->range_beams, &bt->list_v,   &bt->spec_work};
+  DevBuf* bufs[N_SCRATCH] = {&bt->T,          &bt->aabb,        &bt->counters, &bt->ranges,    &bt->cranges,
+                             &bt->cone_beams, &bt->range_beams, &bt->list_v,   &bt->spec_work, &bt->pro_beams};
   for (int k = 0; k < N_SCRATCH; ++k) CH_CUDA(bufs[k]->ensure(need.bytes[k]));
   const Scratch S{bt->T.as<float>(),          bt->aabb.as<int>(),          bt->counters.as<int>(),
                   bt->ranges.as<uint32_t>(),  bt->cranges.as<uint32_t>(),  bt->cone_beams.as<ConeBeam>(),
-                  bt->range_beams.as<RangeBeam>(), bt->list_v.as<int>(),   bt->spec_work.as<float2>()};
+                  bt->range_beams.as<RangeBeam>(), bt->list_v.as<int>(),   bt->spec_work.as<float2>(),
+                  bt->pro_beams.as<PrologueBeam>()};
   CH_CUDA(cudaStreamSynchronize(s));
+  {
+    // the records are fixed for the batch's life: uploaded once, outside the graph
+    const std::vector<PrologueBeam> pb = make_prologue_records(B, S);
+    CH_CUDA(cudaMemcpy(bt->pro_beams.p, pb.data(), pb.size() * sizeof(PrologueBeam), cudaMemcpyHostToDevice));
+  }
   if (!B.spectral) {
     std::vector<ConeBeam> cb;
     std::vector<RangeBeam> rb;
@@ -1913,7 +1972,7 @@ ch_status ch_plan_trim(ch_plan* P) {
   CH_CUDA(cudaSetDevice(P->device));
   // cudaFree waits for the device, so no call of this plan is still reading the arena
   for (DevBuf* b : {&P->T, &P->aabb, &P->counters, &P->ranges, &P->cranges, &P->cone_beams, &P->range_beams,
-                    &P->list_v, &P->spec_work, &P->adj_in, &P->adj_out, &P->adj_w})
+                    &P->list_v, &P->spec_work, &P->pro_beams, &P->adj_in, &P->adj_out, &P->adj_w})
     b->release();
   P->stats_pending = false;
   return CH_OK;

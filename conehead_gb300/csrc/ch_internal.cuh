@@ -265,8 +265,21 @@ void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st);
 void launch_spec_build(const SpecLaunch& L, const long long* idx, const float* val, int n_val, float* s_real,
                        cudaStream_t st);
 
+// One beam of a batched prologue (device record).
+struct PrologueBeam {
+  GridDev g;
+  BeamDev b;
+  SettingsDev s;
+  const float* rho;
+  float* T;          // [nx][ny][zp]
+  int* aabb;         // 8 ints: TERMA box, list count at [6]
+  int* list_v;       // this beam's voxel list (nx ny nz entries)
+};
+
 // ------------------------------------------------------------ launchers --
 void upload_unit_partials();
+void launch_prologue_batch(const PrologueBeam* recs, int n_beams, long long max_voxels, int n_sm, int* flags,
+                           cudaStream_t st, int ctas_per_sm);
 void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const SettingsDev& s, float* T,
                      const Inter& inter, int all_voxels, int* aabb, int* list_v, int n_sm, int* flags,
                      cudaStream_t st, int ctas_per_sm = 8);

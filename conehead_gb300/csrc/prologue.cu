@@ -17,6 +17,7 @@
 // Fluence and TERMA run in float32 (reference: float64 fluence, float32
 // TERMA) and are compared with a tolerance.
 
+#include <algorithm>
 #include <cstdio>
 
 #include "ch_internal.cuh"
@@ -286,12 +287,11 @@ __device__ float radiological_depth(const float* __restrict__ rho, const GridDev
 // Pass 1, every voxel: zero TERMA and keep the voxels the beam may reach
 // (all voxels when intermediates are requested) on a compact list, so the
 // blocking/depth/TERMA pass runs on full warps.
-__global__ void __launch_bounds__(256) cull_kernel(GridDev g, BeamDev b, float* __restrict__ T, Inter inter,
-                                                   int all_voxels, int* __restrict__ list_count,
-                                                   int* __restrict__ list_v) {
+__device__ __forceinline__ void cull_body(const GridDev& g, const BeamDev& b, float* __restrict__ T,
+                                          const Inter& inter, int all_voxels, int* __restrict__ list_count,
+                                          int* __restrict__ list_v, int v) {
   // volumes hold fewer than 2^31 voxels (checked on the host)
   const int N = g.n[0] * g.n[1] * g.n[2];
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = v < N;
   bool keep = false;
   if (live) {
@@ -343,19 +343,45 @@ __global__ void __launch_bounds__(256) cull_kernel(GridDev g, BeamDev b, float* 
   }
 }
 
+__global__ void __launch_bounds__(256) cull_kernel(GridDev g, BeamDev b, float* __restrict__ T, Inter inter,
+                                                   int all_voxels, int* __restrict__ list_count,
+                                                   int* __restrict__ list_v) {
+  cull_body(g, b, T, inter, all_voxels, list_count, list_v, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// this CTA's beam record (blockIdx.y) copied into shared memory
+__device__ __forceinline__ void load_record(const PrologueBeam* __restrict__ recs, PrologueBeam& R) {
+  static_assert(sizeof(PrologueBeam) % 4 == 0 && sizeof(PrologueBeam) <= 4 * 1024, "record copy");
+  const int* src = reinterpret_cast<const int*>(recs + blockIdx.y);
+  int* dst = reinterpret_cast<int*>(&R);
+  for (int i = threadIdx.x; i < (int)(sizeof(PrologueBeam) / 4); i += blockDim.x) dst[i] = __ldg(src + i);
+  __syncthreads();
+}
+
+// every beam of a batch in one launch: blockIdx.y = beam
+__global__ void __launch_bounds__(256) cull_batch_kernel(const PrologueBeam* __restrict__ recs) {
+  __shared__ PrologueBeam R;
+  load_record(recs, R);
+  const int N = R.g.n[0] * R.g.n[1] * R.g.n[2];
+  if ((int)(blockIdx.x * blockDim.x) >= N) return;
+  cull_body(R.g, R.b, R.T, Inter{}, 0, R.aabb + 6, R.list_v, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // Pass 2, listed voxels: blocked fraction, then (where the beam is not
 // fully blocked, or for every voxel when intermediates are requested)
 // radiological depth, oad, fluence, softening/horn and TERMA; TERMA support
 // box for the cone stage.
-__global__ void __launch_bounds__(256) terma_kernel(const float* __restrict__ rho, GridDev g, BeamDev b,
-                                                    SettingsDev s, float* __restrict__ T, Inter inter,
-                                                    int all_voxels, const int* __restrict__ list_count,
-                                                    const int* __restrict__ list_v, int* __restrict__ aabb,
-                                                    int* __restrict__ flags) {
+// The listed voxels of one beam, taken by n_ctas CTAs (this one is cta) in
+// rounds of n_ctas * blockDim.x.
+__device__ __forceinline__ void terma_body(const float* __restrict__ rho, const GridDev& g, const BeamDev& b,
+                                           const SettingsDev& s, float* __restrict__ T, const Inter& inter,
+                                           int all_voxels, const int* __restrict__ list_count,
+                                           const int* __restrict__ list_v, int* __restrict__ aabb,
+                                           int* __restrict__ flags, int cta, int n_ctas) {
   const int count = *list_count;
-  const int rounds = (count + blockDim.x * gridDim.x - 1) / (blockDim.x * gridDim.x);
+  const int rounds = (count + blockDim.x * n_ctas - 1) / (blockDim.x * n_ctas);
   for (int it = 0; it < rounds; ++it) {
-    const int e = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
+    const int e = (it * n_ctas + cta) * blockDim.x + threadIdx.x;
     const bool live = e < count;
     int x = 0, y = 0, z = 0, bad = 0;
     float Tv = 0.0f;
@@ -445,6 +471,21 @@ __global__ void __launch_bounds__(256) terma_kernel(const float* __restrict__ rh
     }
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flags, FLAG_PARALLEL_RAY);
   }
+}
+
+__global__ void __launch_bounds__(256) terma_kernel(const float* __restrict__ rho, GridDev g, BeamDev b,
+                                                    SettingsDev s, float* __restrict__ T, Inter inter,
+                                                    int all_voxels, const int* __restrict__ list_count,
+                                                    const int* __restrict__ list_v, int* __restrict__ aabb,
+                                                    int* __restrict__ flags) {
+  terma_body(rho, g, b, s, T, inter, all_voxels, list_count, list_v, aabb, flags, blockIdx.x, gridDim.x);
+}
+
+__global__ void __launch_bounds__(256) terma_batch_kernel(const PrologueBeam* __restrict__ recs,
+                                                          int* __restrict__ flags) {
+  __shared__ PrologueBeam R;
+  load_record(recs, R);
+  terma_body(R.rho, R.g, R.b, R.s, R.T, Inter{}, 0, R.aabb + 6, R.list_v, R.aabb, flags, blockIdx.x, gridDim.x);
 }
 
 // ----------------------------------------------------- beamlet adjoint --
@@ -579,6 +620,18 @@ void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const
   const int grid = (int)(want < cap ? want : cap);
   terma_kernel<<<grid > 0 ? grid : 1, threads, 0, st>>>(rho, g, b, s, T, inter, all_voxels, list_count, list_v,
                                                         aabb, flags);
+}
+
+// Batched prologue (no intermediates): one cull launch over every beam's grid
+// and one TERMA launch in which each beam's list is shared by the same number
+// of CTAs, so all beams run together and no beam leaves a tail.
+void launch_prologue_batch(const PrologueBeam* recs, int n_beams, long long max_voxels, int n_sm, int* flags,
+                           cudaStream_t st, int ctas_per_sm) {
+  const int threads = 256;
+  cull_batch_kernel<<<dim3((unsigned)((max_voxels + threads - 1) / threads), n_beams), threads, 0, st>>>(recs);
+  const long long per_beam = std::max(1ll, ((long long)n_sm * ctas_per_sm + n_beams - 1) / n_beams);
+  const long long want = (max_voxels + threads - 1) / threads;
+  terma_batch_kernel<<<dim3((unsigned)std::min(per_beam, want), n_beams), threads, 0, st>>>(recs, flags);
 }
 
 __global__ void init_scratch_kernel(int* aabb, int n_beams, int* counters) {
