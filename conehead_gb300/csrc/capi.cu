@@ -1164,9 +1164,12 @@ ch_status enqueue_batch(ch_plan* P, const BatchPlan& B, const Scratch& S, const 
     }
   } else {
     // every beam's prologue in one cull and one TERMA launch (records staged)
-    long long max_vox = 1;
-    for (const BeamJob& J : B.jobs) max_vox = std::max(max_vox, (long long)J.g.n[0] * J.g.n[1] * J.g.n[2]);
-    launch_prologue_batch(S.pro, n, max_vox, P->n_sm, flags, s, P->tuning.terma_ctas_per_sm);
+    long long max_vox = 1, max_lines = 1;
+    for (const BeamJob& J : B.jobs) {
+      max_vox = std::max(max_vox, (long long)J.g.n[0] * J.g.n[1] * J.g.n[2]);
+      max_lines = std::max(max_lines, (long long)J.g.n[0] * J.g.n[1]);
+    }
+    launch_prologue_batch(S.pro, n, max_vox, max_lines, P->n_sm, flags, s, P->tuning.terma_ctas_per_sm);
     CH_CUDA(cudaGetLastError());
   }
   if (ev) CH_CUDA(cudaEventRecord(ev[1], s));

@@ -198,28 +198,27 @@ __device__ __noinline__ double blocked_general(const BeamDev& b, const GridDev& 
 }
 
 // blocked fraction of one voxel; the 3x3x3 jaw case (values 0 and 1 only)
-// is unrolled and sums through the precomputed float64 partial sums
+// counts open samples and sums through the precomputed float64 partial sums
 __device__ double blocked_fraction(const BeamDev& b, const GridDev& g, int S, const float* pos, int& bad) {
   if (S != 3 || b.geom_f32) return blocked_general(b, g, S, pos, bad);
-  float off[3], rel[3][3];
+  float off[3];
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    off[k] = fdiv(g.spacing[k], 3.0f);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) rel[k][i] = off[k] * ((float)i + 0.5f) - g.spacing[k] * 0.5f;
-  }
+  for (int k = 0; k < 3; ++k) off[k] = fdiv(g.spacing[k], 3.0f);
   int n_one = 0;
   bool other = false;
-#pragma unroll
-  for (int ix = 0; ix < 3; ++ix)
-#pragma unroll
-    for (int iy = 0; iy < 3; ++iy)
-#pragma unroll
-      for (int iz = 0; iz < 3; ++iz) {
-        const float v = sample_value(b, g, pos, off, rel[0][ix], rel[1][iy], rel[2][iz], ix, iy, iz, bad);
-        n_one += v == 1.0f ? 1 : 0;
-        other |= v != 0.0f && v != 1.0f;
-      }
+  // a rolled loop: one copy of the sample code keeps the kernel inside the
+  // instruction cache (the float32 offsets only steer the classification,
+  // whose ambiguous samples are recomputed exactly from ix, iy, iz)
+#pragma unroll 1
+  for (int sidx = 0; sidx < 27; ++sidx) {
+    const int ix = sidx / 9, iy = (sidx / 3) % 3, iz = sidx % 3;
+    const float rx = off[0] * ((float)ix + 0.5f) - g.spacing[0] * 0.5f;
+    const float ry = off[1] * ((float)iy + 0.5f) - g.spacing[1] * 0.5f;
+    const float rz = off[2] * ((float)iz + 0.5f) - g.spacing[2] * 0.5f;
+    const float v = sample_value(b, g, pos, off, rx, ry, rz, ix, iy, iz, bad);
+    n_one += v == 1.0f ? 1 : 0;
+    other |= v != 0.0f && v != 1.0f;
+  }
   if (!other) return c_unit_partial[n_one];
   return blocked_general(b, g, 3, pos, bad);
 }
@@ -246,9 +245,10 @@ __device__ float radiological_depth(const float* __restrict__ rho, const GridDev
   const int st1 = g.swap_xy ? n0 * n2 : n2;
   int idx = g.swap_xy ? (y * n0 + x) * n2 + z : (x * n1 + y) * n2 + z;
   const int dx = s0 * st0, dy = s1 * st1, dz = s2;
-  int cx = x, cy = y, cz = z;
-  float deff = 0.0f, tprev = 0.0f;
-  bool first = true, inside = true;
+  // steps each axis may still take before the walk leaves the grid
+  int left0 = s0 > 0 ? n0 - 1 - x : x, left1 = s1 > 0 ? n1 - 1 - y : y, left2 = s2 > 0 ? n2 - 1 - z : z;
+  float deff = 0.0f, tprev = 0.0f;   // the first step adds rho * (t - 0), i.e. rho * t exactly
+  bool inside = true;
   while (inside) {
     int vi[DDA_UNROLL];
     float tv[DDA_UNROLL];
@@ -257,15 +257,20 @@ __device__ float radiological_depth(const float* __restrict__ rho, const GridDev
     for (int q = 0; q < DDA_UNROLL; ++q) {
       if (inside) {
         vi[q] = idx;
-        if (t0 < t1) {
-          if (t0 < t2) { tv[q] = t0; t0 = fadd(t0, d0); cx += s0; idx += dx; }
-          else { tv[q] = t2; t2 = fadd(t2, d2); cz += s2; idx += dz; }
-        } else {
-          if (t1 < t2) { tv[q] = t1; t1 = fadd(t1, d1); cy += s1; idx += dy; }
-          else { tv[q] = t2; t2 = fadd(t2, d2); cz += s2; idx += dz; }
-        }
+        // the reference's choice, without divergent branches
+        const int ax = (t0 < t1) ? ((t0 < t2) ? 0 : 2) : ((t1 < t2) ? 1 : 2);
+        tv[q] = ax == 0 ? t0 : (ax == 1 ? t1 : t2);
+        const float n0t = fadd(t0, d0), n1t = fadd(t1, d1), n2t = fadd(t2, d2);
+        t0 = ax == 0 ? n0t : t0;
+        t1 = ax == 1 ? n1t : t1;
+        t2 = ax == 2 ? n2t : t2;
+        idx += ax == 0 ? dx : (ax == 1 ? dy : dz);
+        const int left = (ax == 0 ? left0 : (ax == 1 ? left1 : left2)) - 1;
+        left0 = ax == 0 ? left : left0;
+        left1 = ax == 1 ? left : left1;
+        left2 = ax == 2 ? left : left2;
         cnt = q + 1;
-        inside = cx >= 0 && cx < n0 && cy >= 0 && cy < n1 && cz >= 0 && cz < n2;
+        inside = left >= 0;
       }
     }
     float r[DDA_UNROLL];
@@ -274,8 +279,7 @@ __device__ float radiological_depth(const float* __restrict__ rho, const GridDev
 #pragma unroll
     for (int q = 0; q < DDA_UNROLL; ++q) {
       if (q < cnt) {
-        deff = first ? fadd(deff, fmul(r[q], tv[q])) : fadd(deff, fmul(r[q], fsub(tv[q], tprev)));
-        first = false;
+        deff = fadd(deff, fmul(r[q], fsub(tv[q], tprev)));
         tprev = tv[q];
       }
     }
@@ -287,66 +291,71 @@ __device__ float radiological_depth(const float* __restrict__ rho, const GridDev
 // Pass 1, every voxel: zero TERMA and keep the voxels the beam may reach
 // (all voxels when intermediates are requested) on a compact list, so the
 // blocking/depth/TERMA pass runs on full warps.
-__device__ __forceinline__ void cull_body(const GridDev& g, const BeamDev& b, float* __restrict__ T,
+// One warp per (x, y) line of the grid, lanes along z: the index arithmetic
+// runs once per line and the zeroing of TERMA is coalesced.
+__device__ __forceinline__ void cull_line(const GridDev& g, const BeamDev& b, float* __restrict__ T,
                                           const Inter& inter, int all_voxels, int* __restrict__ list_count,
-                                          int* __restrict__ list_v, int v) {
+                                          int* __restrict__ list_v, int line) {
   // volumes hold fewer than 2^31 voxels (checked on the host)
-  const int N = g.n[0] * g.n[1] * g.n[2];
-  const bool live = v < N;
-  bool keep = false;
-  if (live) {
-    const int z = v % g.n[2];
-    const int r = v / g.n[2];
-    const int y = r % g.n[1];
-    const int x = r / g.n[1];
-    float pos[3];
-    pos[0] = voxel_centre(g.origin[0], g.spacing[0], x);
-    pos[1] = voxel_centre(g.origin[1], g.spacing[1], y);
-    pos[2] = voxel_centre(g.origin[2], g.spacing[2], z);
-    bool candidate = true;
-    if (b.cull_enable) {
-      const float np_ = b.vyf[0] * pos[0] + b.vyf[1] * pos[1] + b.vyf[2] * pos[2];
-      const float m0p = b.m0f[0] * pos[0] + b.m0f[1] * pos[1] + b.m0f[2] * pos[2];
-      const float m2p = b.m2f[0] * pos[0] + b.m2f[1] * pos[1] + b.m2f[2] * pos[2];
-      const float ndr = b.a_nS - np_;   // n . (S - p) = -depth
-      const float depth = -ndr;
-      if (depth > 0.2f * fabsf(b.a_K)) {
-        const float si = b.a_K / ndr;
-        const float xb = b.a_c0 + si * (b.a_m0S - m0p);
-        const float zb = b.a_c2 + si * (b.a_m2S - m2p);
-        const float lat = fmaxf(fabsf(b.a_m0S - m0p), fabsf(b.a_m2S - m2p)) / depth;
-        const float margin = b.cull_margin_k * fabsf(b.a_K) / depth * (1.0f + lat) + 0.01f;
-        if (xb < b.cx_lo - margin || xb > b.cx_hi + margin || zb < b.cz_lo - margin ||
-            zb > b.cz_hi + margin)
-          candidate = false;
+  if (line >= g.n[0] * g.n[1]) return;   // whole warp
+  const int lane = threadIdx.x & 31;
+  const int x = line / g.n[1], y = line - x * g.n[1];
+  const float px = voxel_centre(g.origin[0], g.spacing[0], x);
+  const float py = voxel_centre(g.origin[1], g.spacing[1], y);
+  for (int z0 = 0; z0 < g.n[2]; z0 += 32) {
+    const int z = z0 + lane;
+    const bool live = z < g.n[2];
+    const int v = line * g.n[2] + z;
+    bool keep = false;
+    if (live) {
+      float pos[3];
+      pos[0] = px;
+      pos[1] = py;
+      pos[2] = voxel_centre(g.origin[2], g.spacing[2], z);
+      bool candidate = true;
+      if (b.cull_enable) {
+        const float np_ = b.vyf[0] * pos[0] + b.vyf[1] * pos[1] + b.vyf[2] * pos[2];
+        const float m0p = b.m0f[0] * pos[0] + b.m0f[1] * pos[1] + b.m0f[2] * pos[2];
+        const float m2p = b.m2f[0] * pos[0] + b.m2f[1] * pos[1] + b.m2f[2] * pos[2];
+        const float ndr = b.a_nS - np_;   // n . (S - p) = -depth
+        const float depth = -ndr;
+        if (depth > 0.2f * fabsf(b.a_K)) {
+          const float si = b.a_K / ndr;
+          const float xb = b.a_c0 + si * (b.a_m0S - m0p);
+          const float zb = b.a_c2 + si * (b.a_m2S - m2p);
+          const float lat = fmaxf(fabsf(b.a_m0S - m0p), fabsf(b.a_m2S - m2p)) / depth;
+          const float margin = b.cull_margin_k * fabsf(b.a_K) / depth * (1.0f + lat) + 0.01f;
+          if (xb < b.cx_lo - margin || xb > b.cx_hi + margin || zb < b.cz_lo - margin ||
+              zb > b.cz_hi + margin)
+            candidate = false;
+        }
+      }
+      keep = candidate || all_voxels;
+      T[((size_t)x * g.n[1] + y) * g.zp + z] = 0.0f;
+      if (!keep) {
+        if (inter.blocked) inter.blocked[v] = 0.0;
+        if (inter.d_eff) inter.d_eff[v] = 0.0f;
+        if (inter.oad) inter.oad[v] = 0.0f;
+        if (inter.fluence) inter.fluence[v] = 0.0f;
+        if (inter.f_soften) inter.f_soften[v] = 1.0f;
+        if (inter.f_horn) inter.f_horn[v] = 1.0f;
+        if (inter.terma) inter.terma[v] = 0.0f;
       }
     }
-    keep = candidate || all_voxels;
-    T[((size_t)x * g.n[1] + y) * g.zp + z] = 0.0f;
-    if (!keep) {
-      if (inter.blocked) inter.blocked[v] = 0.0;
-      if (inter.d_eff) inter.d_eff[v] = 0.0f;
-      if (inter.oad) inter.oad[v] = 0.0f;
-      if (inter.fluence) inter.fluence[v] = 0.0f;
-      if (inter.f_soften) inter.f_soften[v] = 1.0f;
-      if (inter.f_horn) inter.f_horn[v] = 1.0f;
-      if (inter.terma) inter.terma[v] = 0.0f;
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (m) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(list_count, __popc(m));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (keep) list_v[base + __popc(m & ((1u << lane) - 1u))] = v;
     }
-  }
-  const unsigned m = __ballot_sync(0xffffffffu, keep);
-  if (m) {
-    const int lane = threadIdx.x & 31;
-    int base = 0;
-    if (lane == 0) base = atomicAdd(list_count, __popc(m));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (keep) list_v[base + __popc(m & ((1u << lane) - 1u))] = v;
   }
 }
 
 __global__ void __launch_bounds__(256) cull_kernel(GridDev g, BeamDev b, float* __restrict__ T, Inter inter,
                                                    int all_voxels, int* __restrict__ list_count,
                                                    int* __restrict__ list_v) {
-  cull_body(g, b, T, inter, all_voxels, list_count, list_v, blockIdx.x * blockDim.x + threadIdx.x);
+  cull_line(g, b, T, inter, all_voxels, list_count, list_v, (blockIdx.x * blockDim.x + threadIdx.x) >> 5);
 }
 
 // this CTA's beam record (blockIdx.y) copied into shared memory
@@ -362,9 +371,7 @@ __device__ __forceinline__ void load_record(const PrologueBeam* __restrict__ rec
 __global__ void __launch_bounds__(256) cull_batch_kernel(const PrologueBeam* __restrict__ recs) {
   __shared__ PrologueBeam R;
   load_record(recs, R);
-  const int N = R.g.n[0] * R.g.n[1] * R.g.n[2];
-  if ((int)(blockIdx.x * blockDim.x) >= N) return;
-  cull_body(R.g, R.b, R.T, Inter{}, 0, R.aabb + 6, R.list_v, blockIdx.x * blockDim.x + threadIdx.x);
+  cull_line(R.g, R.b, R.T, Inter{}, 0, R.aabb + 6, R.list_v, (blockIdx.x * blockDim.x + threadIdx.x) >> 5);
 }
 
 // Pass 2, listed voxels: blocked fraction, then (where the beam is not
@@ -612,9 +619,9 @@ void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const
                      cudaStream_t st, int ctas_per_sm) {
   const long long N = (long long)g.n[0] * g.n[1] * g.n[2];
   const int threads = 256;
-  const long long blocks = (N + threads - 1) / threads;
+  const long long lines = (long long)g.n[0] * g.n[1];
   int* list_count = aabb + 6;
-  cull_kernel<<<(unsigned)blocks, threads, 0, st>>>(g, b, T, inter, all_voxels, list_count, list_v);
+  cull_kernel<<<(unsigned)((lines + 7) / 8), threads, 0, st>>>(g, b, T, inter, all_voxels, list_count, list_v);
   const long long want = (N + threads - 1) / threads;
   const long long cap = (long long)n_sm * ctas_per_sm;
   const int grid = (int)(want < cap ? want : cap);
@@ -625,10 +632,10 @@ void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const
 // Batched prologue (no intermediates): one cull launch over every beam's grid
 // and one TERMA launch in which each beam's list is shared by the same number
 // of CTAs, so all beams run together and no beam leaves a tail.
-void launch_prologue_batch(const PrologueBeam* recs, int n_beams, long long max_voxels, int n_sm, int* flags,
-                           cudaStream_t st, int ctas_per_sm) {
+void launch_prologue_batch(const PrologueBeam* recs, int n_beams, long long max_voxels, long long max_lines,
+                           int n_sm, int* flags, cudaStream_t st, int ctas_per_sm) {
   const int threads = 256;
-  cull_batch_kernel<<<dim3((unsigned)((max_voxels + threads - 1) / threads), n_beams), threads, 0, st>>>(recs);
+  cull_batch_kernel<<<dim3((unsigned)((max_lines + 7) / 8), n_beams), threads, 0, st>>>(recs);
   const long long per_beam = std::max(1ll, ((long long)n_sm * ctas_per_sm + n_beams - 1) / n_beams);
   const long long want = (max_voxels + threads - 1) / threads;
   terma_batch_kernel<<<dim3((unsigned)std::min(per_beam, want), n_beams), threads, 0, st>>>(recs, flags);
