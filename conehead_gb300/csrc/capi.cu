@@ -1583,6 +1583,25 @@ GridDev grid_dev(const ch_grid& grid, int swap_xy) {
 // counters must have been reset (launch_init_scratch) by the caller.
 ch_status cone_operator(ch_plan* P, const ch_grid& grid, const float* in_dense, float* out, bool transpose,
                         int* box, const int* out_box, cudaStream_t s, const RangeBeam* out_planes = nullptr) {
+  if (spec_batch(P, 1, &grid)) {
+    // spectral: C in = IFFT(FFT(in) S^), C^T in = IFFT(FFT(in) conj(S^)) (S is
+    // real, so the mirrored stencil's spectrum is the conjugate); every
+    // output voxel is computed
+    const float2* shat = nullptr;
+    ch_status st = spec_shat(P, P->st, grid.n, s, &shat);
+    if (st != CH_OK) return st;
+    const SpecLayout L = spec_layout(1, &grid);
+    CH_CUDA(P->spec_work.ensure(L.arena * sizeof(float2)));
+    const SpecPlanLaunch& l = L.launches[0];
+    SpecLaunch SL{};
+    SL.g = spec_grid(P, l.n, l.M, grid.n[2], transpose ? 1 : 0, shat);
+    SL.n_pairs = 1;
+    float2* w = P->spec_work.as<float2>();
+    SL.p[0] = SpecPair{in_dense, nullptr, w + l.pairs[0].a_off, w + l.pairs[0].b_off, out, nullptr};
+    launch_spec_pairs(SL, s);
+    CH_CUDA(cudaGetLastError());
+    return CH_OK;
+  }
   const GridDev g = grid_dev(grid, 0);
   const StencilSet& S = transpose ? P->st_adj : P->st;
   const int U = S.n_dirs;

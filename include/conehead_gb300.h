@@ -251,8 +251,10 @@ ch_status ch_block_from_beamlets(const ch_beamlets* beamlets, const float* weigh
 
 /* The cone stage as an operator on any volume (device, float32 [x][y][z]):
  * out = C in, or out = C^T in with transpose = 1, where C maps TERMA to dose
- * exactly as ch_dose's cone stage does (conehead/conehead.py:385-488).  The
- * transpose gathers along the mirrored walks.  in and out must differ. */
+ * exactly as ch_dose's cone stage does (conehead/conehead.py:385-488), by
+ * the plan's cone method: spectral (the transpose multiplies by the
+ * conjugate stencil spectrum) or gather (the transpose walks the mirrored
+ * walks).  in and out must differ. */
 ch_status ch_cone(ch_plan* plan, const ch_grid* grid, const float* in_dev, float* out_dev, int transpose,
                   void* stream);
 
@@ -260,8 +262,9 @@ ch_status ch_cone(ch_plan* plan, const ch_grid* grid, const float* in_dev, float
  * grad_dose = dL/d(dose) (device, [x][y][z]) for the dose ch_dose computes
  * from this beam (whose block crop is the beamlet grid's), writes
  * grad_weights = dL/dw (device, float32 [rows][cols]) and, if grad_terma is
- * not NULL, dL/d(TERMA) ([x][y][z]; computed where TERMA can be nonzero --
- * inside its box and the beam frustum -- and 0 elsewhere).  Steps: the
+ * not NULL, dL/d(TERMA) ([x][y][z]; exact where TERMA can be nonzero --
+ * inside its box and the beam frustum -- and elsewhere the full C^T value
+ * with the spectral cone method, 0 with the gather).  Steps: the
  * forward prologue, the transposed cone (C^T grad_dose on those voxels), and
  * the transposed blocking: blocked(v) = sum over the S^3 sub-samples of
  * w[beamlet] / S^3 and TERMA = blocked^2 * H(v) (fluence and TERMA each carry

@@ -207,10 +207,12 @@ def test_config_large_field_96(eng, settings, oracle_lib):
 
 
 # ------------------------------------------------------------ paths agree --
-def test_large_ragged_grid_gather_equals_scatter(eng, settings):
+@pytest.mark.parametrize("method", [0, 1], ids=["spectral", "gather"])
+def test_large_ragged_grid_cone_equals_scatter(eng, settings, method):
     """250 x 224 x 163 voxels at 0.2 cm (50 x 45 x 33 cm): walks of up to
-    ~640 taps, ragged tiles on every axis, a field larger than one tile.  The
-    gather must equal the plain per-voxel scatter, whose indexing is the
+    ~640 taps, FFT periods of 512 on every axis (spectral), ragged tiles on
+    every axis (gather), a field larger than one tile.  Both cone methods
+    must equal the plain per-voxel scatter, whose indexing is the
     reference's loop."""
     from conehead_gb300 import GridPhantom
     from conehead_gb300.phantoms import random_beam
@@ -223,29 +225,38 @@ def test_large_ragged_grid_gather_equals_scatter(eng, settings):
     ph = GridPhantom(rho, tuple(-(k - 1) * s / 2 for k in n), (s, s, s))
     src, blk = random_beam(rng, rect=(6.0, 10.0), collimator=True)
     eng.set_kernel(settings["energy_weights"])
-    r = eng.upload_densities(ph.densities)
-    db = eng.block_for(blk)
-    a = eng.run(eng.job(ph, r, src, db, settings)).clone()
-    b = eng.run(eng.job(ph, r, src, db, settings), scatter=True)
-    eng.sync()
+    eng.set_tuning(cone_method=method)
+    try:
+        r = eng.upload_densities(ph.densities)
+        db = eng.block_for(blk)
+        a = eng.run(eng.job(ph, r, src, db, settings)).clone()
+        b = eng.run(eng.job(ph, r, src, db, settings), scatter=True)
+        eng.sync()
+    finally:
+        eng.set_tuning()
     a, b = a.cpu().numpy(), b.cpu().numpy()
     assert b.max() > 0
     err = np.abs(a - b).max() / b.max()
-    print(f"250x224x163 gather vs scatter: {err:.2e} of Dmax")
+    print(f"250x224x163 {('spectral', 'gather')[method]} vs scatter: {err:.2e} of Dmax")
     assert err <= 2e-5
 
 
-def test_gather_equals_scatter(eng, settings):
+@pytest.mark.parametrize("method", [0, 1], ids=["spectral", "gather"])
+def test_cone_equals_scatter(eng, settings, method):
     from conehead_gb300.phantoms import random_beam, slab_phantom
     rng = np.random.default_rng(3)
     ph = slab_phantom(64, 0.25, seed=3)
     src, blk = random_beam(rng, field=6.0)
     eng.set_kernel(settings["energy_weights"])
-    rho = eng.upload_densities(ph.densities)
-    db = eng.upload_block(blk.block_values)
-    a = eng.run(eng.job(ph, rho, src, db, settings)).clone()
-    b = eng.run(eng.job(ph, rho, src, db, settings), scatter=True)
-    eng.sync()
+    eng.set_tuning(cone_method=method)
+    try:
+        rho = eng.upload_densities(ph.densities)
+        db = eng.upload_block(blk.block_values)
+        a = eng.run(eng.job(ph, rho, src, db, settings)).clone()
+        b = eng.run(eng.job(ph, rho, src, db, settings), scatter=True)
+        eng.sync()
+    finally:
+        eng.set_tuning()
     a, b = a.cpu().numpy(), b.cpu().numpy()
     assert np.abs(a - b).max() <= 2e-5 * b.max()
 
