@@ -2,7 +2,7 @@
 
 The schedule knobs do not change results (beyond the float order of the
 dose sums), only speed, and the best setting depends on the workload:
-grid sizes, field sizes and how many beams share one persistent cone launch.
+grid sizes, field sizes and how many beams share one cone launch.
 ``autotune`` times every candidate on a representative batch (CUDA events
 on the engine's stream, after a warm-up) and keeps the fastest; results are
 cached in a JSON file keyed by the device and a workload signature, so a

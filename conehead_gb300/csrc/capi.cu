@@ -786,7 +786,7 @@ struct BeamJob {
   ch_beam beam;
 };
 
-// The 39 TMA tensor maps of one padded [x][y][zp] volume: one per window
+// The TMA tensor maps of one padded [x][y][zp] volume: one per window
 // shape and x extent (boxes P z x rows y x ex x, zero fill outside).
 ch_status encode_windows(PFN_cuTensorMapEncodeTiled_v12000 enc, ConeBeam& C, float* vol, const GridDev& g) {
   cuuint64_t gdim[3] = {(cuuint64_t)g.n[2], (cuuint64_t)g.n[1], (cuuint64_t)g.n[0]};
@@ -1062,7 +1062,7 @@ ch_status plan_batch(ch_plan* P, int n, const ch_grid* grids, const float* const
   return CH_OK;
 }
 
-// Launch records of every beam (39 tensor maps over its TERMA volume, tap
+// Launch records of every beam (tensor maps over its TERMA volume, tap
 // ranges, beam frustum planes) pointing into scratch S.
 ch_status make_records(const BatchPlan& B, const Scratch& S, std::vector<ConeBeam>& cb, std::vector<RangeBeam>& rb) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();

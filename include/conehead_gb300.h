@@ -161,7 +161,8 @@ ch_status ch_dose_ex(ch_plan* plan, const ch_grid* grid, const float* rho_dev, i
                      const ch_intermediates* inter, void* stream);
 
 /* Many beams (each with its own grid/density/settings) in one pass: every
- * beam's prologue, then one persistent cone launch over all beams' work. */
+ * beam's prologue in one launch pair, then the cone stage over all beams
+ * (one FFT launch group per grid shape, or one persistent gather). */
 ch_status ch_dose_batch(ch_plan* plan, int n_beams, const ch_grid* grids,
                         const float* const* rho_dev, const int* swap_xy,
                         const ch_beam* beams, const ch_settings* settings,
