@@ -82,76 +82,105 @@ __device__ __forceinline__ void dft16(float2 (&v)[16]) {
   for (int k1 = 0; k1 < 4; ++k1) dft4<INV>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
 }
 
-// FFT of L lines of length M held in src (layout above), ping-ponging with
-// dst; returns the buffer holding the result.  INV uses the conjugate
-// twiddles (no 1/M scale); tw[k] = exp(-2 pi i k / M).  Stockham stages of
-// radix 16 while four or more factors of two remain, then radix 4 and 2 (256
-// points take two stages); a thread holds one butterfly at a time and every
-// stage ends with one barrier.  The caller has synchronised after filling src.
+// One Stockham stage from src to dst (element (i, line c) layout above) on L
+// lines of period M; Ns = 2^logNs is the sub-transform size done so far and
+// tw[k] = exp(-2 pi i k / M).  A thread takes one butterfly at a time.
 template <bool INV>
-__device__ float2* fft_block(float2* src, float2* dst, int M, int logM, int L, int logL,
-                             const float2* __restrict__ tw) {
-  const int tid = threadIdx.x;
-  int Ns = 1, logNs = 0;
-  while (Ns < M) {
-    if (logM - logNs >= 4) {
-      const int MR = M >> 4, nb = L * MR, step = M >> (logNs + 4);
-      for (int bf = tid; bf < nb; bf += SPEC_THREADS) {
-        const int c = bf & (L - 1), j = bf >> logL, k = j & (Ns - 1);
-        float2 v[16];
+__device__ __forceinline__ void stage16(const float2* src, float2* dst, int M, int L, int logL, int logNs,
+                                        const float2* __restrict__ tw) {
+  const int Ns = 1 << logNs, MR = M >> 4, nb = L * MR, step = M >> (logNs + 4);
+  for (int bf = threadIdx.x; bf < nb; bf += SPEC_THREADS) {
+    const int c = bf & (L - 1), j = bf >> logL, k = j & (Ns - 1);
+    float2 v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = src[swz(j + r * MR, c, L)];
-        if (k) {
+    for (int r = 0; r < 16; ++r) v[r] = src[swz(j + r * MR, c, L)];
+    if (k) {
 #pragma unroll
-          for (int r = 1; r < 16; ++r) {
-            float2 w = __ldg(tw + r * k * step);
-            if (INV) w.y = -w.y;
-            v[r] = cmul(v[r], w);
-          }
-        }
-        dft16<INV>(v);
-        const int o = ((j - k) << 4) + k;
-#pragma unroll
-        for (int k1 = 0; k1 < 4; ++k1)
-#pragma unroll
-          for (int k2 = 0; k2 < 4; ++k2) dst[swz(o + (k1 + 4 * k2) * Ns, c, L)] = v[4 * k1 + k2];
-      }
-      Ns <<= 4;
-      logNs += 4;
-    } else if (logM - logNs >= 2) {
-      const int MR = M >> 2, nb = L * MR, step = M >> (logNs + 2);
-      for (int bf = tid; bf < nb; bf += SPEC_THREADS) {
-        const int c = bf & (L - 1), j = bf >> logL, k = j & (Ns - 1);
-        float2 v[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) v[r] = src[swz(j + r * MR, c, L)];
-#pragma unroll
-        for (int r = 1; r < 4; ++r) {
-          float2 w = __ldg(tw + r * k * step);
-          if (INV) w.y = -w.y;
-          v[r] = cmul(v[r], w);
-        }
-        dft4<INV>(v[0], v[1], v[2], v[3]);
-        const int o = ((j - k) << 2) + k;
-#pragma unroll
-        for (int r = 0; r < 4; ++r) dst[swz(o + r * Ns, c, L)] = v[r];
-      }
-      Ns <<= 2;
-      logNs += 2;
-    } else {
-      const int MR = M >> 1, nb = L * MR, step = M >> (logNs + 1);
-      for (int bf = tid; bf < nb; bf += SPEC_THREADS) {
-        const int c = bf & (L - 1), j = bf >> logL, k = j & (Ns - 1);
-        float2 w = __ldg(tw + k * step);
+      for (int r = 1; r < 16; ++r) {
+        float2 w = __ldg(tw + r * k * step);
         if (INV) w.y = -w.y;
-        const float2 a0 = src[swz(j, c, L)], a1 = cmul(src[swz(j + MR, c, L)], w);
-        const int o = ((j - k) << 1) + k;
-        dst[swz(o, c, L)] = make_float2(a0.x + a1.x, a0.y + a1.y);
-        dst[swz(o + Ns, c, L)] = make_float2(a0.x - a1.x, a0.y - a1.y);
+        v[r] = cmul(v[r], w);
       }
-      Ns <<= 1;
-      logNs += 1;
     }
+    dft16<INV>(v);
+    const int o = ((j - k) << 4) + k;
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+      for (int k2 = 0; k2 < 4; ++k2) dst[swz(o + (k1 + 4 * k2) * Ns, c, L)] = v[4 * k1 + k2];
+  }
+}
+
+template <bool INV>
+__device__ __forceinline__ void stage4(const float2* src, float2* dst, int M, int L, int logL, int logNs,
+                                       const float2* __restrict__ tw) {
+  const int Ns = 1 << logNs, MR = M >> 2, nb = L * MR, step = M >> (logNs + 2);
+  for (int bf = threadIdx.x; bf < nb; bf += SPEC_THREADS) {
+    const int c = bf & (L - 1), j = bf >> logL, k = j & (Ns - 1);
+    float2 v[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) v[r] = src[swz(j + r * MR, c, L)];
+#pragma unroll
+    for (int r = 1; r < 4; ++r) {
+      float2 w = __ldg(tw + r * k * step);
+      if (INV) w.y = -w.y;
+      v[r] = cmul(v[r], w);
+    }
+    dft4<INV>(v[0], v[1], v[2], v[3]);
+    const int o = ((j - k) << 2) + k;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) dst[swz(o + r * Ns, c, L)] = v[r];
+  }
+}
+
+template <bool INV>
+__device__ __forceinline__ void stage2(const float2* src, float2* dst, int M, int L, int logL, int logNs,
+                                       const float2* __restrict__ tw) {
+  const int Ns = 1 << logNs, MR = M >> 1, nb = L * MR, step = M >> (logNs + 1);
+  for (int bf = threadIdx.x; bf < nb; bf += SPEC_THREADS) {
+    const int c = bf & (L - 1), j = bf >> logL, k = j & (Ns - 1);
+    float2 w = __ldg(tw + k * step);
+    if (INV) w.y = -w.y;
+    const float2 a0 = src[swz(j, c, L)], a1 = cmul(src[swz(j + MR, c, L)], w);
+    const int o = ((j - k) << 1) + k;
+    dst[swz(o, c, L)] = make_float2(a0.x + a1.x, a0.y + a1.y);
+    dst[swz(o + Ns, c, L)] = make_float2(a0.x - a1.x, a0.y - a1.y);
+  }
+}
+
+// FFT of the L lines of period M held in src, ping-ponging with dst; returns
+// the buffer holding the result.  INV uses the conjugate twiddles (no 1/M
+// scale).  Stockham stages of radix 16 while four or more factors of two
+// remain, then radix 4 and 2 (256 points take two stages); every stage ends
+// with one barrier.  The caller has synchronised after filling src.
+// LM, LL >= 0 fix log2 M and log2 L at compile time (the stages unroll and
+// the shared-memory addresses fold); -1 takes them at run time.
+template <bool INV, int LM, int LL>
+__device__ __forceinline__ float2* fft_block(float2* src, float2* dst, int logM_rt, int logL_rt,
+                                             const float2* __restrict__ tw) {
+  const int logM = LM >= 0 ? LM : logM_rt, logL = LL >= 0 ? LL : logL_rt;
+  const int M = 1 << logM, L = 1 << logL;
+  int logNs = 0;
+#pragma unroll
+  for (int st = 0; st < (LM >= 0 ? LM / 4 : 3); ++st) {
+    if (LM < 0 && logM - logNs < 4) break;
+    stage16<INV>(src, dst, M, L, logL, logNs, tw);
+    __syncthreads();
+    float2* t = src;
+    src = dst;
+    dst = t;
+    logNs += 4;
+  }
+  if (logM - logNs >= 2) {
+    stage4<INV>(src, dst, M, L, logL, logNs, tw);
+    __syncthreads();
+    float2* t = src;
+    src = dst;
+    dst = t;
+    logNs += 2;
+  }
+  if (logM - logNs >= 1) {
+    stage2<INV>(src, dst, M, L, logL, logNs, tw);
     __syncthreads();
     float2* t = src;
     src = dst;
@@ -161,13 +190,17 @@ __device__ float2* fft_block(float2* src, float2* dst, int M, int logM, int L, i
 }
 
 // ---------------------------------------------------------------- passes --
+// Every pass is a template on LM = log2 of its period and LL = log2 of its
+// lines per CTA: >= 0 fixes them at compile time, -1 reads them from the
+// launch.
 // z forward: lines (x, y), TERMA pair in, A out.  One CTA per L lines and pair.
+template <int LM>
 __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward_kernel(SpecLaunch P) {
   extern __shared__ float2 spec_sm[];
   float2* sm = spec_sm;
   float2* sm2 = spec_sm + SPEC_ELEMS;
   const SpecPair& pr = P.p[blockIdx.y];
-  const int Mz = P.g.M[2], logMz = P.g.logM[2];
+  const int logMz = LM >= 0 ? LM : P.g.logM[2], Mz = 1 << logMz;
   const int logL = 12 - logMz, L = 1 << logL;
   const int nl = P.g.n[0] * P.g.n[1], nz = P.g.n[2];
   const int l0 = blockIdx.x * L;
@@ -192,7 +225,7 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward
     }
   }
   __syncthreads();
-  const float2* res = fft_block<false>(sm, sm2, Mz, logMz, L, logL, P.g.tw[2]);
+  const float2* res = fft_block<false, LM, (LM >= 0 ? 12 - LM : -1)>(sm, sm2, logMz, logL, P.g.tw[2]);
   for (int e = threadIdx.x; e < SPEC_ELEMS; e += SPEC_THREADS) {
     const int i = e & (Mz - 1), c = e >> logMz, l = l0 + c;
     if (l < nl) pr.a[(size_t)l * Mz + i] = res[swz(i, c, L)];
@@ -200,14 +233,14 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward
 }
 
 // y forward (A -> B) or inverse (B -> A): lines (x, kz) in blocks of L kz.
-template <bool INV>
+template <bool INV, int LM, int LL>
 __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_y_kernel(SpecLaunch P) {
   extern __shared__ float2 spec_sm[];
   float2* sm = spec_sm;
   float2* sm2 = spec_sm + SPEC_ELEMS;
   const SpecPair& pr = P.p[blockIdx.y];
-  const int My = P.g.M[1], logMy = P.g.logM[1], Mz = P.g.M[2], logMz = P.g.logM[2];
-  const int logL = min(12 - logMy, logMz), L = 1 << logL;
+  const int logMy = LM >= 0 ? LM : P.g.logM[1], My = 1 << logMy, Mz = P.g.M[2], logMz = P.g.logM[2];
+  const int logL = LL >= 0 ? LL : min(12 - logMy, logMz), L = 1 << logL;
   const int nkb = Mz >> logL;
   const int x = blockIdx.x / nkb, kz0 = (blockIdx.x - x * nkb) << logL;
   const int ny = P.g.n[1];
@@ -231,7 +264,7 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_y_kernel(
     }
   }
   __syncthreads();
-  const float2* res = fft_block<INV>(sm, sm2, My, logMy, L, logL, P.g.tw[1]);
+  const float2* res = fft_block<INV, LM, LL>(sm, sm2, logMy, logL, P.g.tw[1]);
   for (int e = threadIdx.x; e < n_out * L; e += SPEC_THREADS) {
     const int c = e & (L - 1), i = e >> logL;
     dst[(size_t)i * Mz + c] = res[swz(i, c, L)];
@@ -242,15 +275,16 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_y_kernel(
 // same lines of consecutive pairs, so each block of S^ is read from L2.
 // CONV: forward, times S^ (or its conjugate), inverse, x < nx kept;
 // otherwise forward only over the full period (building S^).
-template <bool CONV>
+template <bool CONV, int LM, int LL>
 __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(SpecLaunch P) {
   extern __shared__ float2 spec_sm[];
   float2* sm = spec_sm;
   float2* sm2 = spec_sm + SPEC_ELEMS;
   const int pair = blockIdx.x % P.n_pairs, blk = blockIdx.x / P.n_pairs;
   const SpecPair& pr = P.p[pair];
-  const int Mx = P.g.M[0], logMx = P.g.logM[0], My = P.g.M[1], Mz = P.g.M[2], logMz = P.g.logM[2];
-  const int logL = min(12 - logMx, logMz), L = 1 << logL;
+  const int logMx = LM >= 0 ? LM : P.g.logM[0], Mx = 1 << logMx, My = P.g.M[1], Mz = P.g.M[2];
+  const int logMz = P.g.logM[2];
+  const int logL = LL >= 0 ? LL : min(12 - logMx, logMz), L = 1 << logL;
   const int nkb = Mz >> logL;
   const int ky = blk / nkb, kz0 = (blk - ky * nkb) << logL;
   const size_t xs = (size_t)My * Mz, off = (size_t)ky * Mz + kz0;
@@ -271,7 +305,7 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(
     }
   }
   __syncthreads();
-  float2* res = fft_block<false>(sm, sm2, Mx, logMx, L, logL, P.g.tw[0]);
+  float2* res = fft_block<false, LM, LL>(sm, sm2, logMx, logL, P.g.tw[0]);
   if (CONV) {
     const float2* sh = P.g.shat + off;
     float2 sv[SPEC_ELEMS / SPEC_THREADS];
@@ -291,7 +325,7 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(
       }
     }
     __syncthreads();
-    res = fft_block<true>(res, res == sm ? sm2 : sm, Mx, logMx, L, logL, P.g.tw[0]);
+    res = fft_block<true, LM, LL>(res, res == sm ? sm2 : sm, logMx, logL, P.g.tw[0]);
   }
   for (int e = threadIdx.x; e < nx * L; e += SPEC_THREADS) {
     const int c = e & (L - 1), i = e >> logL;
@@ -300,12 +334,13 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(
 }
 
 // z inverse: lines (x, y), A in, dose pair out (real part, imaginary part).
+template <int LM>
 __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_inverse_kernel(SpecLaunch P) {
   extern __shared__ float2 spec_sm[];
   float2* sm = spec_sm;
   float2* sm2 = spec_sm + SPEC_ELEMS;
   const SpecPair& pr = P.p[blockIdx.y];
-  const int Mz = P.g.M[2], logMz = P.g.logM[2];
+  const int logMz = LM >= 0 ? LM : P.g.logM[2], Mz = 1 << logMz;
   const int logL = 12 - logMz, L = 1 << logL;
   const int nl = P.g.n[0] * P.g.n[1], nz = P.g.n[2];
   const int l0 = blockIdx.x * L;
@@ -324,7 +359,7 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_inverse
     }
   }
   __syncthreads();
-  const float2* res = fft_block<true>(sm, sm2, Mz, logMz, L, logL, P.g.tw[2]);
+  const float2* res = fft_block<true, LM, (LM >= 0 ? 12 - LM : -1)>(sm, sm2, logMz, logL, P.g.tw[2]);
   for (int e = threadIdx.x; e < SPEC_ELEMS; e += SPEC_THREADS) {
     const int i = e & (Mz - 1), c = e >> logMz, l = l0 + c;
     if (l < nl && i < nz) {
@@ -360,26 +395,68 @@ std::vector<float2> spec_twiddles() {
 
 size_t spec_twiddle_offset(int M) { return (size_t)M - SPEC_MIN_PERIOD; }
 
-cudaError_t setup_spec_kernels() {
+// Compile-time periods for the common shapes (grids of 17 to 256 voxels per
+// axis): a pass is specialised when its lines per CTA are 4096 / M.
+#define SPEC_FOR_PERIODS(X) X(6, 6) X(7, 5) X(8, 4) X(9, 3)
+
+template <int LM, int LL>
+cudaError_t set_smem() {
   cudaError_t e = cudaSuccess;
-  for (const void* f : {(const void*)spec_z_forward_kernel, (const void*)spec_y_kernel<false>,
-                        (const void*)spec_y_kernel<true>, (const void*)spec_x_kernel<false>,
-                        (const void*)spec_x_kernel<true>, (const void*)spec_z_inverse_kernel})
+  for (const void* f : {(const void*)spec_z_forward_kernel<LM>, (const void*)spec_y_kernel<false, LM, LL>,
+                        (const void*)spec_y_kernel<true, LM, LL>, (const void*)spec_x_kernel<false, LM, LL>,
+                        (const void*)spec_x_kernel<true, LM, LL>, (const void*)spec_z_inverse_kernel<LM>})
     if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_SMEM);
   return e;
 }
 
+cudaError_t setup_spec_kernels() {
+  cudaError_t e = set_smem<-1, -1>();
+#define SPEC_SET(lm, ll) \
+  if (e == cudaSuccess) e = set_smem<lm, ll>();
+  SPEC_FOR_PERIODS(SPEC_SET)
+#undef SPEC_SET
+  return e;
+}
+
+// Each pass is launched specialised when (log2 M, log2 L) is one of
+// SPEC_FOR_PERIODS, generic otherwise.
 void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
   const SpecGrid& g = L.g;
   const int nl = g.n[0] * g.n[1];
   const int Lz = SPEC_ELEMS / g.M[2];
   const int Ly = std::min(SPEC_ELEMS / g.M[1], g.M[2]);
   const int Lx = std::min(SPEC_ELEMS / g.M[0], g.M[2]);
-  spec_z_forward_kernel<<<dim3((nl + Lz - 1) / Lz, L.n_pairs), SPEC_THREADS, SPEC_SMEM, st>>>(L);
-  spec_y_kernel<false><<<dim3(g.n[0] * (g.M[2] / Ly), L.n_pairs), SPEC_THREADS, SPEC_SMEM, st>>>(L);
-  spec_x_kernel<true><<<g.M[1] * (g.M[2] / Lx) * L.n_pairs, SPEC_THREADS, SPEC_SMEM, st>>>(L);
-  spec_y_kernel<true><<<dim3(g.n[0] * (g.M[2] / Ly), L.n_pairs), SPEC_THREADS, SPEC_SMEM, st>>>(L);
-  spec_z_inverse_kernel<<<dim3((nl + Lz - 1) / Lz, L.n_pairs), SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  const dim3 gz((nl + Lz - 1) / Lz, L.n_pairs), gy(g.n[0] * (g.M[2] / Ly), L.n_pairs);
+  const unsigned gx = g.M[1] * (g.M[2] / Lx) * L.n_pairs;
+  const int lz = g.logM[2], ly = g.logM[1], lx = g.logM[0];
+  const bool sy = (SPEC_ELEMS / g.M[1]) == Ly, sx = (SPEC_ELEMS / g.M[0]) == Lx;
+  bool z_done = false, y_done = false, x_done = false;
+#define SPEC_Z(lm, ll) \
+  if (!z_done && lz == lm) { spec_z_forward_kernel<lm><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L); z_done = true; }
+#define SPEC_Y(lm, ll) \
+  if (!y_done && sy && ly == lm) { spec_y_kernel<false, lm, ll><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L); y_done = true; }
+#define SPEC_X(lm, ll) \
+  if (!x_done && sx && lx == lm) { spec_x_kernel<true, lm, ll><<<gx, SPEC_THREADS, SPEC_SMEM, st>>>(L); x_done = true; }
+  SPEC_FOR_PERIODS(SPEC_Z)
+  if (!z_done) spec_z_forward_kernel<-1><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  SPEC_FOR_PERIODS(SPEC_Y)
+  if (!y_done) spec_y_kernel<false, -1, -1><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  SPEC_FOR_PERIODS(SPEC_X)
+  if (!x_done) spec_x_kernel<true, -1, -1><<<gx, SPEC_THREADS, SPEC_SMEM, st>>>(L);
+#undef SPEC_Z
+#undef SPEC_Y
+#undef SPEC_X
+  y_done = z_done = false;
+#define SPEC_YI(lm, ll) \
+  if (!y_done && sy && ly == lm) { spec_y_kernel<true, lm, ll><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L); y_done = true; }
+#define SPEC_ZI(lm, ll) \
+  if (!z_done && lz == lm) { spec_z_inverse_kernel<lm><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L); z_done = true; }
+  SPEC_FOR_PERIODS(SPEC_YI)
+  if (!y_done) spec_y_kernel<true, -1, -1><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  SPEC_FOR_PERIODS(SPEC_ZI)
+  if (!z_done) spec_z_inverse_kernel<-1><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
+#undef SPEC_YI
+#undef SPEC_ZI
 }
 
 void launch_spec_build(const SpecLaunch& L, const long long* idx, const float* val, int n_val, float* s_real,
@@ -390,9 +467,9 @@ void launch_spec_build(const SpecLaunch& L, const long long* idx, const float* v
   const int Ly = std::min(SPEC_ELEMS / g.M[1], g.M[2]);
   const int Lx = std::min(SPEC_ELEMS / g.M[0], g.M[2]);
   if (n_val > 0) spec_scatter_kernel<<<(n_val + 255) / 256, 256, 0, st>>>(idx, val, n_val, s_real);
-  spec_z_forward_kernel<<<dim3((nl + Lz - 1) / Lz, 1), SPEC_THREADS, SPEC_SMEM, st>>>(L);
-  spec_y_kernel<false><<<dim3(g.n[0] * (g.M[2] / Ly), 1), SPEC_THREADS, SPEC_SMEM, st>>>(L);
-  spec_x_kernel<false><<<g.M[1] * (g.M[2] / Lx), SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  spec_z_forward_kernel<-1><<<dim3((nl + Lz - 1) / Lz, 1), SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  spec_y_kernel<false, -1, -1><<<dim3(g.n[0] * (g.M[2] / Ly), 1), SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  spec_x_kernel<false, -1, -1><<<g.M[1] * (g.M[2] / Lx), SPEC_THREADS, SPEC_SMEM, st>>>(L);
 }
 
 }  // namespace ch
