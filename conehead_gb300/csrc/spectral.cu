@@ -82,16 +82,59 @@ __device__ __forceinline__ void dft16(float2 (&v)[16]) {
   for (int k1 = 0; k1 < 4; ++k1) dft4<INV>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
 }
 
+// dft16 with v[8..15] = 0 (the upper half of a zero-padded input): the first
+// DFT4s see two inputs
+template <bool INV>
+__device__ __forceinline__ void dft16_half_in(float2 (&v)[16]) {
+  constexpr float C1 = 0.92387953251128674f;
+  constexpr float S1 = 0.38268343236508977f;
+  constexpr float R2 = 0.70710678118654752f;
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    const float2 a0 = v[b], a1 = v[4 + b];
+    const float2 mi = INV ? make_float2(-a1.y, a1.x) : make_float2(a1.y, -a1.x);   // -+i a1
+    v[b] = make_float2(a0.x + a1.x, a0.y + a1.y);
+    v[4 + b] = make_float2(a0.x + mi.x, a0.y + mi.y);
+    v[8 + b] = make_float2(a0.x - a1.x, a0.y - a1.y);
+    v[12 + b] = make_float2(a0.x - mi.x, a0.y - mi.y);
+  }
+  v[5] = rot<INV>(v[5], C1, S1);
+  v[9] = rot<INV>(v[9], R2, R2);
+  v[13] = rot<INV>(v[13], S1, C1);
+  v[6] = rot<INV>(v[6], R2, R2);
+  v[10] = rot<INV>(v[10], 0.0f, 1.0f);
+  v[14] = rot<INV>(v[14], -R2, R2);
+  v[7] = rot<INV>(v[7], S1, C1);
+  v[11] = rot<INV>(v[11], -R2, R2);
+  v[15] = rot<INV>(v[15], -C1, -S1);
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) dft4<INV>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+}
+
 // One Stockham stage from src to dst (element (i, line c) layout above) on L
 // lines of period M; Ns = 2^logNs is the sub-transform size done so far and
 // tw[k] = exp(-2 pi i k / M).  A thread takes one butterfly at a time.
+// hin: the first stage of a transform whose input's upper half is zero (it
+// reads only r < 8); hout: the last stage of one whose output's upper half
+// is not wanted (it writes only the lower half).
 template <bool INV>
 __device__ __forceinline__ void stage16(const float2* src, float2* dst, int M, int L, int logL, int logNs,
-                                        const float2* __restrict__ tw) {
+                                        const float2* __restrict__ tw, bool hin, bool hout) {
   const int Ns = 1 << logNs, MR = M >> 4, nb = L * MR, step = M >> (logNs + 4);
   for (int bf = threadIdx.x; bf < nb; bf += SPEC_THREADS) {
     const int c = bf & (L - 1), j = bf >> logL, k = j & (Ns - 1);
     float2 v[16];
+    if (hin) {
+#pragma unroll
+      for (int r = 0; r < 8; ++r) v[r] = src[swz(j + r * MR, c, L)];
+      dft16_half_in<INV>(v);     // first stage: k = 0, no twiddles
+      const int o = j << 4;
+#pragma unroll
+      for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+        for (int k2 = 0; k2 < 4; ++k2) dst[swz(o + (k1 + 4 * k2) * Ns, c, L)] = v[4 * k1 + k2];
+      continue;
+    }
 #pragma unroll
     for (int r = 0; r < 16; ++r) v[r] = src[swz(j + r * MR, c, L)];
     if (k) {
@@ -104,16 +147,24 @@ __device__ __forceinline__ void stage16(const float2* src, float2* dst, int M, i
     }
     dft16<INV>(v);
     const int o = ((j - k) << 4) + k;
+    if (hout) {
+      // outputs o + q Ns with q = k1 + 4 k2 < 8 are the lower half
 #pragma unroll
-    for (int k1 = 0; k1 < 4; ++k1)
+      for (int k1 = 0; k1 < 4; ++k1)
 #pragma unroll
-      for (int k2 = 0; k2 < 4; ++k2) dst[swz(o + (k1 + 4 * k2) * Ns, c, L)] = v[4 * k1 + k2];
+        for (int k2 = 0; k2 < 2; ++k2) dst[swz(o + (k1 + 4 * k2) * Ns, c, L)] = v[4 * k1 + k2];
+    } else {
+#pragma unroll
+      for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+        for (int k2 = 0; k2 < 4; ++k2) dst[swz(o + (k1 + 4 * k2) * Ns, c, L)] = v[4 * k1 + k2];
+    }
   }
 }
 
 template <bool INV>
 __device__ __forceinline__ void stage4(const float2* src, float2* dst, int M, int L, int logL, int logNs,
-                                       const float2* __restrict__ tw) {
+                                       const float2* __restrict__ tw, bool hout) {
   const int Ns = 1 << logNs, MR = M >> 2, nb = L * MR, step = M >> (logNs + 2);
   for (int bf = threadIdx.x; bf < nb; bf += SPEC_THREADS) {
     const int c = bf & (L - 1), j = bf >> logL, k = j & (Ns - 1);
@@ -128,14 +179,19 @@ __device__ __forceinline__ void stage4(const float2* src, float2* dst, int M, in
     }
     dft4<INV>(v[0], v[1], v[2], v[3]);
     const int o = ((j - k) << 2) + k;
+    if (hout) {
+      dst[swz(o, c, L)] = v[0];
+      dst[swz(o + Ns, c, L)] = v[1];
+    } else {
 #pragma unroll
-    for (int r = 0; r < 4; ++r) dst[swz(o + r * Ns, c, L)] = v[r];
+      for (int r = 0; r < 4; ++r) dst[swz(o + r * Ns, c, L)] = v[r];
+    }
   }
 }
 
 template <bool INV>
 __device__ __forceinline__ void stage2(const float2* src, float2* dst, int M, int L, int logL, int logNs,
-                                       const float2* __restrict__ tw) {
+                                       const float2* __restrict__ tw, bool hout) {
   const int Ns = 1 << logNs, MR = M >> 1, nb = L * MR, step = M >> (logNs + 1);
   for (int bf = threadIdx.x; bf < nb; bf += SPEC_THREADS) {
     const int c = bf & (L - 1), j = bf >> logL, k = j & (Ns - 1);
@@ -144,7 +200,7 @@ __device__ __forceinline__ void stage2(const float2* src, float2* dst, int M, in
     const float2 a0 = src[swz(j, c, L)], a1 = cmul(src[swz(j + MR, c, L)], w);
     const int o = ((j - k) << 1) + k;
     dst[swz(o, c, L)] = make_float2(a0.x + a1.x, a0.y + a1.y);
-    dst[swz(o + Ns, c, L)] = make_float2(a0.x - a1.x, a0.y - a1.y);
+    if (!hout) dst[swz(o + Ns, c, L)] = make_float2(a0.x - a1.x, a0.y - a1.y);
   }
 }
 
@@ -154,17 +210,19 @@ __device__ __forceinline__ void stage2(const float2* src, float2* dst, int M, in
 // remain, then radix 4 and 2 (256 points take two stages); every stage ends
 // with one barrier.  The caller has synchronised after filling src.
 // LM, LL >= 0 fix log2 M and log2 L at compile time (the stages unroll and
-// the shared-memory addresses fold); -1 takes them at run time.
+// the shared-memory addresses fold); -1 takes them at run time.  half_in:
+// the input's upper half is zero; half_out: only the output's lower half is
+// wanted (the upper half of the result buffer is then left stale).
 template <bool INV, int LM, int LL>
 __device__ __forceinline__ float2* fft_block(float2* src, float2* dst, int logM_rt, int logL_rt,
-                                             const float2* __restrict__ tw) {
+                                             const float2* __restrict__ tw, bool half_in, bool half_out) {
   const int logM = LM >= 0 ? LM : logM_rt, logL = LL >= 0 ? LL : logL_rt;
   const int M = 1 << logM, L = 1 << logL;
   int logNs = 0;
 #pragma unroll
   for (int st = 0; st < (LM >= 0 ? LM / 4 : 3); ++st) {
     if (LM < 0 && logM - logNs < 4) break;
-    stage16<INV>(src, dst, M, L, logL, logNs, tw);
+    stage16<INV>(src, dst, M, L, logL, logNs, tw, half_in && logNs == 0, half_out && logNs + 4 == logM);
     __syncthreads();
     float2* t = src;
     src = dst;
@@ -172,7 +230,7 @@ __device__ __forceinline__ float2* fft_block(float2* src, float2* dst, int logM_
     logNs += 4;
   }
   if (logM - logNs >= 2) {
-    stage4<INV>(src, dst, M, L, logL, logNs, tw);
+    stage4<INV>(src, dst, M, L, logL, logNs, tw, half_out && logNs + 2 == logM);
     __syncthreads();
     float2* t = src;
     src = dst;
@@ -180,7 +238,7 @@ __device__ __forceinline__ float2* fft_block(float2* src, float2* dst, int logM_
     logNs += 2;
   }
   if (logM - logNs >= 1) {
-    stage2<INV>(src, dst, M, L, logL, logNs, tw);
+    stage2<INV>(src, dst, M, L, logL, logNs, tw, half_out);
     __syncthreads();
     float2* t = src;
     src = dst;
@@ -225,7 +283,8 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward
     }
   }
   __syncthreads();
-  const float2* res = fft_block<false, LM, (LM >= 0 ? 12 - LM : -1)>(sm, sm2, logMz, logL, P.g.tw[2]);
+  const float2* res =
+      fft_block<false, LM, (LM >= 0 ? 12 - LM : -1)>(sm, sm2, logMz, logL, P.g.tw[2], 2 * nz <= Mz, false);
   for (int e = threadIdx.x; e < SPEC_ELEMS; e += SPEC_THREADS) {
     const int i = e & (Mz - 1), c = e >> logMz, l = l0 + c;
     if (l < nl) pr.a[(size_t)l * Mz + i] = res[swz(i, c, L)];
@@ -264,7 +323,8 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_y_kernel(
     }
   }
   __syncthreads();
-  const float2* res = fft_block<INV, LM, LL>(sm, sm2, logMy, logL, P.g.tw[1]);
+  const float2* res = fft_block<INV, LM, LL>(sm, sm2, logMy, logL, P.g.tw[1], !INV && 2 * ny <= My,
+                                             INV && 2 * ny <= My);
   for (int e = threadIdx.x; e < n_out * L; e += SPEC_THREADS) {
     const int c = e & (L - 1), i = e >> logL;
     dst[(size_t)i * Mz + c] = res[swz(i, c, L)];
@@ -305,7 +365,7 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(
     }
   }
   __syncthreads();
-  float2* res = fft_block<false, LM, LL>(sm, sm2, logMx, logL, P.g.tw[0]);
+  float2* res = fft_block<false, LM, LL>(sm, sm2, logMx, logL, P.g.tw[0], 2 * nx <= Mx, false);
   if (CONV) {
     const float2* sh = P.g.shat + off;
     float2 sv[SPEC_ELEMS / SPEC_THREADS];
@@ -325,7 +385,7 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(
       }
     }
     __syncthreads();
-    res = fft_block<true, LM, LL>(res, res == sm ? sm2 : sm, logMx, logL, P.g.tw[0]);
+    res = fft_block<true, LM, LL>(res, res == sm ? sm2 : sm, logMx, logL, P.g.tw[0], false, 2 * nx <= Mx);
   }
   for (int e = threadIdx.x; e < nx * L; e += SPEC_THREADS) {
     const int c = e & (L - 1), i = e >> logL;
@@ -359,7 +419,8 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_inverse
     }
   }
   __syncthreads();
-  const float2* res = fft_block<true, LM, (LM >= 0 ? 12 - LM : -1)>(sm, sm2, logMz, logL, P.g.tw[2]);
+  const float2* res =
+      fft_block<true, LM, (LM >= 0 ? 12 - LM : -1)>(sm, sm2, logMz, logL, P.g.tw[2], false, 2 * nz <= Mz);
   for (int e = threadIdx.x; e < SPEC_ELEMS; e += SPEC_THREADS) {
     const int i = e & (Mz - 1), c = e >> logMz, l = l0 + c;
     if (l < nl && i < nz) {
