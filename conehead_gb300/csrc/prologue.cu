@@ -204,6 +204,44 @@ __device__ double blocked_fraction(const BeamDev& b, const GridDev& g, int S, co
   float off[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) off[k] = fdiv(g.spacing[k], 3.0f);
+  if (b.uniform) {
+    // Fast test for a voxel wholly inside a jaw opening.  The samples lie in
+    // the box of the extreme ones (offsets -s/3 and +s/3 per axis).  On the
+    // source's side of the plane the projection through the source maps
+    // segments to segments, so every sample's cell lies in the cell box of
+    // the 8 corner projections, widened by the same float32 error bound as a
+    // single sample.  The open cells of a uniform crop form a rectangle (the
+    // -1 wrap at index -2000 excluded), so when both extreme cells of the box
+    // are open every sample is open: blocked is the reference's sum of 27
+    // ones.  Otherwise the samples are classified one by one.
+    float umin = 3.0e38f, umax = -3.0e38f, wmin = 3.0e38f, wmax = -3.0e38f;
+    bool ok = true;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const float rx = off[0] * ((c & 1) ? 2.5f : 0.5f) - g.spacing[0] * 0.5f;
+      const float ry = off[1] * ((c & 2) ? 2.5f : 0.5f) - g.spacing[1] * 0.5f;
+      const float rz = off[2] * ((c & 4) ? 2.5f : 0.5f) - g.spacing[2] * 0.5f;
+      const float p0 = pos[0] + rx, p1 = pos[1] + ry, p2 = pos[2] + rz;
+      const float np_ = b.vyf[0] * p0 + b.vyf[1] * p1 + b.vyf[2] * p2;
+      const float m0p = b.m0f[0] * p0 + b.m0f[1] * p1 + b.m0f[2] * p2;
+      const float m2p = b.m2f[0] * p0 + b.m2f[1] * p1 + b.m2f[2] * p2;
+      const float ndr = b.a_nS - np_;
+      ok = ok && fabsf(ndr) > 0.2f * fabsf(b.a_K);
+      const float si = __fdividef(b.a_K, ndr);
+      const float ux = (b.a_c0 + si * (b.a_m0S - m0p)) * 100.0f;
+      const float uz = (b.a_c2 + si * (b.a_m2S - m2p)) * 100.0f;
+      umin = fminf(umin, ux);
+      umax = fmaxf(umax, ux);
+      wmin = fminf(wmin, uz);
+      wmax = fmaxf(wmax, uz);
+    }
+    if (ok) {
+      const int i0 = floor_cell(umin - SAMPLE_DELTA), i1 = floor_cell(umax + SAMPLE_DELTA);
+      const int k0 = floor_cell(wmin - SAMPLE_DELTA), k1 = floor_cell(wmax + SAMPLE_DELTA);
+      if (i0 > -2000 && k0 > -2000 && cell_value(b, i0, k0) == 1.0f && cell_value(b, i1, k1) == 1.0f)
+        return c_unit_partial[27];
+    }
+  }
   int n_one = 0;
   bool other = false;
   // a rolled loop: one copy of the sample code keeps the kernel inside the
