@@ -358,11 +358,14 @@ __device__ __forceinline__ void cull_line(const GridDev& g, const BeamDev& b, fl
         const float ndr = b.a_nS - np_;   // n . (S - p) = -depth
         const float depth = -ndr;
         if (depth > 0.2f * fabsf(b.a_K)) {
-          const float si = b.a_K / ndr;
+          // one fast reciprocal: its ~2 ulp error is far inside the 0.01 cm
+          // margin, so the candidate set stays a superset of the beam
+          const float inv_depth = __fdividef(1.0f, depth);
+          const float si = -b.a_K * inv_depth;
           const float xb = b.a_c0 + si * (b.a_m0S - m0p);
           const float zb = b.a_c2 + si * (b.a_m2S - m2p);
-          const float lat = fmaxf(fabsf(b.a_m0S - m0p), fabsf(b.a_m2S - m2p)) / depth;
-          const float margin = b.cull_margin_k * fabsf(b.a_K) / depth * (1.0f + lat) + 0.01f;
+          const float lat = fmaxf(fabsf(b.a_m0S - m0p), fabsf(b.a_m2S - m2p)) * inv_depth;
+          const float margin = b.cull_margin_k * fabsf(b.a_K) * inv_depth * (1.0f + lat) + 0.01f;
           if (xb < b.cx_lo - margin || xb > b.cx_hi + margin || zb < b.cz_lo - margin ||
               zb > b.cz_hi + margin)
             candidate = false;
