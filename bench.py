@@ -328,11 +328,9 @@ def batched_extras(args, dev):
 
 
 def spectral_period(n):
-    """FFT period of one axis: the power of two >= 2 n - 1 (at least 16)."""
-    m = 16
-    while m < 2 * n - 1:
-        m *= 2
-    return m
+    """FFT period of one axis: the smallest 2^a or 3 * 2^a (a >= 4) >= 2 n - 1."""
+    periods = sorted({16 << a for a in range(9)} | {48 << a for a in range(7)})
+    return next(m for m in periods if m >= 2 * n - 1)
 
 
 def spectral_launches(beams, max_pairs=8):

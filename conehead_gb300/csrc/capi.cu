@@ -506,7 +506,7 @@ SpecGrid spec_grid(const ch_plan* P, const int* n, const int* M, int zp, int con
   for (int k = 0; k < 3; ++k) {
     g.n[k] = n[k];
     g.M[k] = M[k];
-    g.logM[k] = __builtin_ctz((unsigned)M[k]);
+    g.logL[k] = k == 2 ? spec_lines_log2(M[2]) : spec_pass_lines_log2(M[k], M[2]);
     g.tw[k] = P->spec_tw.as<float2>() + spec_twiddle_offset(M[k]);
   }
   g.zp = zp;
@@ -865,8 +865,9 @@ constexpr long long kSpecMaxVolume = 1ll << 28;   // largest Mx My Mz (S^ of 2 G
 bool spec_fits(const int* n) {
   long long v = 1;
   for (int k = 0; k < 3; ++k) {
-    if (2 * n[k] - 1 > SPEC_MAX_PERIOD) return false;
-    v *= spec_period(n[k]);
+    const int m = spec_period(n[k]);
+    if (m == 0) return false;
+    v *= m;
   }
   return v <= kSpecMaxVolume;
 }

@@ -226,8 +226,8 @@ struct Inter {
 
 // ---------------------------------------------------- spectral cone stage --
 // The cone stage as one circular convolution per grid shape (spectral.cu):
-// periods M_k = the power of two >= 2 n_k - 1 (at least SPEC_MIN_PERIOD),
-// pairs of beams per complex transform.
+// periods M_k = the smallest 2^a or 3 * 2^a >= 2 n_k - 1 (at least
+// SPEC_MIN_PERIOD), pairs of beams per complex transform.
 constexpr int SPEC_THREADS = 256;
 constexpr int SPEC_CTAS_PER_SM = 3;       // register budget of the passes (85 per thread)
 constexpr int SPEC_ELEMS = 4096;          // complex values per CTA: 4096 / M lines of period M
@@ -243,7 +243,8 @@ struct SpecPair {
   float* d2;         // of the second (NULL: none)
 };
 struct SpecGrid {
-  int n[3], M[3], logM[3];
+  int n[3], M[3];
+  int logL[3];             // log2 of the lines per CTA of the pass along x, y, z
   int zp;                  // z pitch of the TERMA volumes
   int conj;                // multiply by conj(S^): the transposed cone
   const float2* tw[3];     // twiddles exp(-2 pi i k / M_axis)
@@ -254,8 +255,10 @@ struct SpecLaunch {
   int n_pairs;
   SpecPair p[SPEC_MAX_PAIRS];
 };
-int spec_period(int n);
-std::vector<float2> spec_twiddles();      // every period SPEC_MIN_PERIOD .. SPEC_MAX_PERIOD, back to back
+int spec_period(int n);                  // 0 when no period up to SPEC_MAX_PERIOD holds 2n - 1
+int spec_lines_log2(int M);
+int spec_pass_lines_log2(int M, int Mz);
+std::vector<float2> spec_twiddles();      // every period (ascending), back to back
 size_t spec_twiddle_offset(int M);
 cudaError_t setup_spec_kernels();        // allow SPEC_SMEM of dynamic shared memory
 void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st);

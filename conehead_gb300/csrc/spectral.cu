@@ -14,12 +14,12 @@
 // imaginary part; S is real, so their doses come back as the two parts.
 //
 // Each of the five passes over a pair of beams is a batch of 1-D FFTs of
-// power-of-two length M along one axis.  A CTA holds 4096 complex values
-// (L = 4096 / M lines) in shared memory, element (i, line c) at
+// period M = 2^a or 3 * 2^a (the smallest >= 2n - 1, at least 16) along one
+// axis.  A CTA holds up to 4096 complex values (L lines, L the largest power
+// of two with L M <= 4096) in shared memory, element (i, line c) at
 // i * L + (c ^ (i mod L)) so that both line-major and index-major sweeps are
-// free of bank conflicts, and runs radix-4 Stockham stages (one radix-2 stage
-// when log2 M is odd) with twiddles from a host-built table.  The passes skip
-// the zero padding:
+// free of bank conflicts, and runs Stockham stages of radix 16, 3, 4 and 2
+// with twiddles from a host-built table.  The passes skip the zero padding:
 //   z forward  TERMA pair [nx][ny][nz] (pitch zp)  -> A [nx][ny][Mz]
 //   y forward  A (y < ny)                          -> B [nx][My][Mz]
 //   x          B (x < nx): forward, times S^, inverse, x < nx kept (in place)
@@ -28,6 +28,7 @@
 // Every global sweep is coalesced: lines along z are read and written along
 // z, lines along y and x are taken in blocks of L consecutive kz.
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -111,18 +112,33 @@ __device__ __forceinline__ void dft16_half_in(float2 (&v)[16]) {
   for (int k1 = 0; k1 < 4; ++k1) dft4<INV>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
 }
 
+// 3-point DFT in place: X0 = a + s, X1,2 = a - s/2 -+ i (sqrt 3 / 2) d with
+// s = b + c, d = b - c (forward sign -, inverse +)
+template <bool INV>
+__device__ __forceinline__ void dft3(float2& a, float2& b, float2& c) {
+  constexpr float H = 0.86602540378443865f;   // sqrt(3) / 2
+  const float2 s = make_float2(b.x + c.x, b.y + c.y), d = make_float2(b.x - c.x, b.y - c.y);
+  const float2 t = make_float2(a.x - 0.5f * s.x, a.y - 0.5f * s.y);
+  const float2 u = INV ? make_float2(-H * d.y, H * d.x) : make_float2(H * d.y, -H * d.x);
+  a = make_float2(a.x + s.x, a.y + s.y);
+  b = make_float2(t.x + u.x, t.y + u.y);
+  c = make_float2(t.x - u.x, t.y - u.y);
+}
+
 // One Stockham stage from src to dst (element (i, line c) layout above) on L
-// lines of period M; Ns = 2^logNs is the sub-transform size done so far and
-// tw[k] = exp(-2 pi i k / M).  A thread takes one butterfly at a time.
+// lines of period M; Ns is the product of the radices done so far, tw[k] =
+// exp(-2 pi i k / M).  Butterfly j of a line reads j + r M/R, multiplies by
+// tw[r k M/(Ns R)] with k = j mod Ns, and writes (j - k) R + k + r Ns.  A
+// thread takes one butterfly at a time.
 // hin: the first stage of a transform whose input's upper half is zero (it
 // reads only r < 8); hout: the last stage of one whose output's upper half
 // is not wanted (it writes only the lower half).
 template <bool INV>
-__device__ __forceinline__ void stage16(const float2* src, float2* dst, int M, int L, int logL, int logNs,
+__device__ __forceinline__ void stage16(const float2* src, float2* dst, int M, int L, int logL, int Ns,
                                         const float2* __restrict__ tw, bool hin, bool hout) {
-  const int Ns = 1 << logNs, MR = M >> 4, nb = L * MR, step = M >> (logNs + 4);
+  const int MR = M / 16, nb = L * MR, step = M / (Ns * 16);
   for (int bf = threadIdx.x; bf < nb; bf += SPEC_THREADS) {
-    const int c = bf & (L - 1), j = bf >> logL, k = j & (Ns - 1);
+    const int c = bf & (L - 1), j = bf >> logL, k = j % Ns;
     float2 v[16];
     if (hin) {
 #pragma unroll
@@ -146,7 +162,7 @@ __device__ __forceinline__ void stage16(const float2* src, float2* dst, int M, i
       }
     }
     dft16<INV>(v);
-    const int o = ((j - k) << 4) + k;
+    const int o = (j - k) * 16 + k;
     if (hout) {
       // outputs o + q Ns with q = k1 + 4 k2 < 8 are the lower half
 #pragma unroll
@@ -163,11 +179,33 @@ __device__ __forceinline__ void stage16(const float2* src, float2* dst, int M, i
 }
 
 template <bool INV>
-__device__ __forceinline__ void stage4(const float2* src, float2* dst, int M, int L, int logL, int logNs,
-                                       const float2* __restrict__ tw, bool hout) {
-  const int Ns = 1 << logNs, MR = M >> 2, nb = L * MR, step = M >> (logNs + 2);
+__device__ __forceinline__ void stage3(const float2* src, float2* dst, int M, int L, int logL, int Ns,
+                                       const float2* __restrict__ tw) {
+  const int MR = M / 3, nb = L * MR, step = M / (Ns * 3);
   for (int bf = threadIdx.x; bf < nb; bf += SPEC_THREADS) {
-    const int c = bf & (L - 1), j = bf >> logL, k = j & (Ns - 1);
+    const int c = bf & (L - 1), j = bf >> logL, k = j % Ns;
+    float2 v0 = src[swz(j, c, L)], v1 = src[swz(j + MR, c, L)], v2 = src[swz(j + 2 * MR, c, L)];
+    float2 w1 = __ldg(tw + k * step), w2 = __ldg(tw + 2 * k * step);
+    if (INV) {
+      w1.y = -w1.y;
+      w2.y = -w2.y;
+    }
+    v1 = cmul(v1, w1);
+    v2 = cmul(v2, w2);
+    dft3<INV>(v0, v1, v2);
+    const int o = (j - k) * 3 + k;
+    dst[swz(o, c, L)] = v0;
+    dst[swz(o + Ns, c, L)] = v1;
+    dst[swz(o + 2 * Ns, c, L)] = v2;
+  }
+}
+
+template <bool INV>
+__device__ __forceinline__ void stage4(const float2* src, float2* dst, int M, int L, int logL, int Ns,
+                                       const float2* __restrict__ tw, bool hout) {
+  const int MR = M / 4, nb = L * MR, step = M / (Ns * 4);
+  for (int bf = threadIdx.x; bf < nb; bf += SPEC_THREADS) {
+    const int c = bf & (L - 1), j = bf >> logL, k = j % Ns;
     float2 v[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) v[r] = src[swz(j + r * MR, c, L)];
@@ -178,7 +216,7 @@ __device__ __forceinline__ void stage4(const float2* src, float2* dst, int M, in
       v[r] = cmul(v[r], w);
     }
     dft4<INV>(v[0], v[1], v[2], v[3]);
-    const int o = ((j - k) << 2) + k;
+    const int o = (j - k) * 4 + k;
     if (hout) {
       dst[swz(o, c, L)] = v[0];
       dst[swz(o + Ns, c, L)] = v[1];
@@ -190,55 +228,80 @@ __device__ __forceinline__ void stage4(const float2* src, float2* dst, int M, in
 }
 
 template <bool INV>
-__device__ __forceinline__ void stage2(const float2* src, float2* dst, int M, int L, int logL, int logNs,
+__device__ __forceinline__ void stage2(const float2* src, float2* dst, int M, int L, int logL, int Ns,
                                        const float2* __restrict__ tw, bool hout) {
-  const int Ns = 1 << logNs, MR = M >> 1, nb = L * MR, step = M >> (logNs + 1);
+  const int MR = M / 2, nb = L * MR, step = M / (Ns * 2);
   for (int bf = threadIdx.x; bf < nb; bf += SPEC_THREADS) {
-    const int c = bf & (L - 1), j = bf >> logL, k = j & (Ns - 1);
+    const int c = bf & (L - 1), j = bf >> logL, k = j % Ns;
     float2 w = __ldg(tw + k * step);
     if (INV) w.y = -w.y;
     const float2 a0 = src[swz(j, c, L)], a1 = cmul(src[swz(j + MR, c, L)], w);
-    const int o = ((j - k) << 1) + k;
+    const int o = (j - k) * 2 + k;
     dst[swz(o, c, L)] = make_float2(a0.x + a1.x, a0.y + a1.y);
     if (!hout) dst[swz(o + Ns, c, L)] = make_float2(a0.x - a1.x, a0.y - a1.y);
   }
 }
 
-// FFT of the L lines of period M held in src, ping-ponging with dst; returns
-// the buffer holding the result.  INV uses the conjugate twiddles (no 1/M
-// scale).  Stockham stages of radix 16 while four or more factors of two
-// remain, then radix 4 and 2 (256 points take two stages); every stage ends
-// with one barrier.  The caller has synchronised after filling src.
-// LM, LL >= 0 fix log2 M and log2 L at compile time (the stages unroll and
-// the shared-memory addresses fold); -1 takes them at run time.  half_in:
-// the input's upper half is zero; half_out: only the output's lower half is
-// wanted (the upper half of the result buffer is then left stale).
-template <bool INV, int LM, int LL>
-__device__ __forceinline__ float2* fft_block(float2* src, float2* dst, int logM_rt, int logL_rt,
+// factors of two of a period (compile time)
+__host__ __device__ constexpr int twos_of(int m) { return (m & 1) ? 0 : 1 + twos_of(m >> 1); }
+
+// FFT of the L lines of period M (2^a or 3 * 2^a, a >= 4) held in src,
+// ping-ponging with dst; returns the buffer holding the result.  INV uses
+// the conjugate twiddles (no 1/M scale).  Stages: radix 16, then radix 3 for
+// a period with a factor 3, then radix 16 while four or more factors of two
+// remain, then radix 4 and 2 (256 points take two stages, 384 four); every
+// stage ends with one barrier.  The caller has synchronised after filling
+// src.  MP > 0 (and LL >= 0) fix the period (and log2 L) at compile time:
+// the stages unroll and the shared-memory addresses fold; otherwise they are
+// read at run time.  half_in: the input's upper half is zero; half_out: only
+// the output's lower half is wanted (the upper half of the result buffer is
+// then left stale; a period of 48 ends on its radix-3 stage, which writes
+// everything).
+template <bool INV, int MP, int LL>
+__device__ __forceinline__ float2* fft_block(float2* src, float2* dst, int M_rt, int logL_rt,
                                              const float2* __restrict__ tw, bool half_in, bool half_out) {
-  const int logM = LM >= 0 ? LM : logM_rt, logL = LL >= 0 ? LL : logL_rt;
-  const int M = 1 << logM, L = 1 << logL;
-  int logNs = 0;
+  const int M = MP > 0 ? MP : M_rt;
+  const int logL = LL >= 0 ? LL : logL_rt, L = 1 << logL;
+  const int a = MP > 0 ? twos_of(MP) : __ffs(M) - 1;
+  const bool three = (M >> a) == 3;
+  int twos = a - 4, Ns = 16;
+  stage16<INV>(src, dst, M, L, logL, 1, tw, half_in, half_out && M == 16);
+  __syncthreads();
+  {
+    float2* t = src;
+    src = dst;
+    dst = t;
+  }
+  if (three) {
+    stage3<INV>(src, dst, M, L, logL, Ns, tw);
+    __syncthreads();
+    float2* t = src;
+    src = dst;
+    dst = t;
+    Ns *= 3;
+  }
 #pragma unroll
-  for (int st = 0; st < (LM >= 0 ? LM / 4 : 3); ++st) {
-    if (LM < 0 && logM - logNs < 4) break;
-    stage16<INV>(src, dst, M, L, logL, logNs, tw, half_in && logNs == 0, half_out && logNs + 4 == logM);
+  for (int st = 0; st < (MP > 0 ? (twos_of(MP > 0 ? MP : 1) - 4) / 4 : 2); ++st) {
+    if (MP <= 0 && twos < 4) break;
+    stage16<INV>(src, dst, M, L, logL, Ns, tw, false, half_out && twos == 4);
     __syncthreads();
     float2* t = src;
     src = dst;
     dst = t;
-    logNs += 4;
+    Ns *= 16;
+    twos -= 4;
   }
-  if (logM - logNs >= 2) {
-    stage4<INV>(src, dst, M, L, logL, logNs, tw, half_out && logNs + 2 == logM);
+  if (twos >= 2) {
+    stage4<INV>(src, dst, M, L, logL, Ns, tw, half_out && twos == 2);
     __syncthreads();
     float2* t = src;
     src = dst;
     dst = t;
-    logNs += 2;
+    Ns *= 4;
+    twos -= 2;
   }
-  if (logM - logNs >= 1) {
-    stage2<INV>(src, dst, M, L, logL, logNs, tw, half_out);
+  if (twos >= 1) {
+    stage2<INV>(src, dst, M, L, logL, Ns, tw, half_out);
     __syncthreads();
     float2* t = src;
     src = dst;
@@ -248,18 +311,20 @@ __device__ __forceinline__ float2* fft_block(float2* src, float2* dst, int logM_
 }
 
 // ---------------------------------------------------------------- passes --
-// Every pass is a template on LM = log2 of its period and LL = log2 of its
-// lines per CTA: >= 0 fixes them at compile time, -1 reads them from the
-// launch.
+// Every pass is a template on MP, its period, and LL, log2 of its lines per
+// CTA: MP > 0 fixes both at compile time, MP = -1 reads them from the launch
+// (P.g.M and P.g.logL).  Lines per CTA: the largest power of two L with
+// L M <= 4096 for lines along z; lines along y and x are taken in blocks of L
+// consecutive kz, so L also divides Mz.
 // z forward: lines (x, y), TERMA pair in, A out.  One CTA per L lines and pair.
-template <int LM>
+template <int MP, int LL>
 __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward_kernel(SpecLaunch P) {
   extern __shared__ float2 spec_sm[];
   float2* sm = spec_sm;
   float2* sm2 = spec_sm + SPEC_ELEMS;
   const SpecPair& pr = P.p[blockIdx.y];
-  const int logMz = LM >= 0 ? LM : P.g.logM[2], Mz = 1 << logMz;
-  const int logL = 12 - logMz, L = 1 << logL;
+  const int Mz = MP > 0 ? MP : P.g.M[2];
+  const int logL = MP > 0 ? LL : P.g.logL[2], L = 1 << logL;
   const int nl = P.g.n[0] * P.g.n[1], nz = P.g.n[2];
   const int l0 = blockIdx.x * L;
   {
@@ -268,9 +333,9 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward
 #pragma unroll
     for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
       const int e = threadIdx.x + q * SPEC_THREADS;
-      const int i = e & (Mz - 1), c = e >> logMz, l = l0 + c;
+      const int c = e / Mz, i = e - c * Mz, l = l0 + c;
       v[q] = make_float2(0.0f, 0.0f);
-      if (l < nl && i < nz) {
+      if (c < L && l < nl && i < nz) {
         const size_t o = (size_t)l * P.g.zp + i;
         v[q].x = __ldg(pr.t1 + o);
         if (pr.t2) v[q].y = __ldg(pr.t2 + o);
@@ -279,27 +344,27 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward
 #pragma unroll
     for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
       const int e = threadIdx.x + q * SPEC_THREADS;
-      sm[swz(e & (Mz - 1), e >> logMz, L)] = v[q];
+      const int c = e / Mz, i = e - c * Mz;
+      if (c < L) sm[swz(i, c, L)] = v[q];
     }
   }
   __syncthreads();
-  const float2* res =
-      fft_block<false, LM, (LM >= 0 ? 12 - LM : -1)>(sm, sm2, logMz, logL, P.g.tw[2], 2 * nz <= Mz, false);
-  for (int e = threadIdx.x; e < SPEC_ELEMS; e += SPEC_THREADS) {
-    const int i = e & (Mz - 1), c = e >> logMz, l = l0 + c;
+  const float2* res = fft_block<false, MP, LL>(sm, sm2, Mz, logL, P.g.tw[2], 2 * nz <= Mz, false);
+  for (int e = threadIdx.x; e < L * Mz; e += SPEC_THREADS) {
+    const int c = e / Mz, i = e - c * Mz, l = l0 + c;
     if (l < nl) pr.a[(size_t)l * Mz + i] = res[swz(i, c, L)];
   }
 }
 
 // y forward (A -> B) or inverse (B -> A): lines (x, kz) in blocks of L kz.
-template <bool INV, int LM, int LL>
+template <bool INV, int MP, int LL>
 __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_y_kernel(SpecLaunch P) {
   extern __shared__ float2 spec_sm[];
   float2* sm = spec_sm;
   float2* sm2 = spec_sm + SPEC_ELEMS;
   const SpecPair& pr = P.p[blockIdx.y];
-  const int logMy = LM >= 0 ? LM : P.g.logM[1], My = 1 << logMy, Mz = P.g.M[2], logMz = P.g.logM[2];
-  const int logL = LL >= 0 ? LL : min(12 - logMy, logMz), L = 1 << logL;
+  const int My = MP > 0 ? MP : P.g.M[1], Mz = P.g.M[2];
+  const int logL = MP > 0 ? LL : P.g.logL[1], L = 1 << logL;
   const int nkb = Mz >> logL;
   const int x = blockIdx.x / nkb, kz0 = (blockIdx.x - x * nkb) << logL;
   const int ny = P.g.n[1];
@@ -314,16 +379,16 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_y_kernel(
     for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
       const int e = threadIdx.x + q * SPEC_THREADS;
       const int c = e & (L - 1), i = e >> logL;
-      v[q] = (e < (L << logMy) && i < n_in) ? src[(size_t)i * Mz + c] : make_float2(0.0f, 0.0f);
+      v[q] = (i < n_in) ? src[(size_t)i * Mz + c] : make_float2(0.0f, 0.0f);
     }
 #pragma unroll
     for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
       const int e = threadIdx.x + q * SPEC_THREADS;
-      if (e < (L << logMy)) sm[swz(e >> logL, e & (L - 1), L)] = v[q];
+      if ((e >> logL) < My) sm[swz(e >> logL, e & (L - 1), L)] = v[q];
     }
   }
   __syncthreads();
-  const float2* res = fft_block<INV, LM, LL>(sm, sm2, logMy, logL, P.g.tw[1], !INV && 2 * ny <= My,
+  const float2* res = fft_block<INV, MP, LL>(sm, sm2, My, logL, P.g.tw[1], !INV && 2 * ny <= My,
                                              INV && 2 * ny <= My);
   for (int e = threadIdx.x; e < n_out * L; e += SPEC_THREADS) {
     const int c = e & (L - 1), i = e >> logL;
@@ -335,16 +400,15 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_y_kernel(
 // same lines of consecutive pairs, so each block of S^ is read from L2.
 // CONV: forward, times S^ (or its conjugate), inverse, x < nx kept;
 // otherwise forward only over the full period (building S^).
-template <bool CONV, int LM, int LL>
+template <bool CONV, int MP, int LL>
 __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(SpecLaunch P) {
   extern __shared__ float2 spec_sm[];
   float2* sm = spec_sm;
   float2* sm2 = spec_sm + SPEC_ELEMS;
   const int pair = blockIdx.x % P.n_pairs, blk = blockIdx.x / P.n_pairs;
   const SpecPair& pr = P.p[pair];
-  const int logMx = LM >= 0 ? LM : P.g.logM[0], Mx = 1 << logMx, My = P.g.M[1], Mz = P.g.M[2];
-  const int logMz = P.g.logM[2];
-  const int logL = LL >= 0 ? LL : min(12 - logMx, logMz), L = 1 << logL;
+  const int Mx = MP > 0 ? MP : P.g.M[0], My = P.g.M[1], Mz = P.g.M[2];
+  const int logL = MP > 0 ? LL : P.g.logL[0], L = 1 << logL;
   const int nkb = Mz >> logL;
   const int ky = blk / nkb, kz0 = (blk - ky * nkb) << logL;
   const size_t xs = (size_t)My * Mz, off = (size_t)ky * Mz + kz0;
@@ -356,28 +420,28 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(
     for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
       const int e = threadIdx.x + q * SPEC_THREADS;
       const int c = e & (L - 1), i = e >> logL;
-      v[q] = (e < (L << logMx) && i < nx) ? b[(size_t)i * xs + c] : make_float2(0.0f, 0.0f);
+      v[q] = (i < nx) ? b[(size_t)i * xs + c] : make_float2(0.0f, 0.0f);
     }
 #pragma unroll
     for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
       const int e = threadIdx.x + q * SPEC_THREADS;
-      if (e < (L << logMx)) sm[swz(e >> logL, e & (L - 1), L)] = v[q];
+      if ((e >> logL) < Mx) sm[swz(e >> logL, e & (L - 1), L)] = v[q];
     }
   }
   __syncthreads();
-  float2* res = fft_block<false, LM, LL>(sm, sm2, logMx, logL, P.g.tw[0], 2 * nx <= Mx, false);
+  float2* res = fft_block<false, MP, LL>(sm, sm2, Mx, logL, P.g.tw[0], 2 * nx <= Mx, false);
   if (CONV) {
     const float2* sh = P.g.shat + off;
     float2 sv[SPEC_ELEMS / SPEC_THREADS];
 #pragma unroll
     for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
       const int e = threadIdx.x + q * SPEC_THREADS;
-      sv[q] = e < (L << logMx) ? __ldg(sh + (size_t)(e >> logL) * xs + (e & (L - 1))) : make_float2(0.0f, 0.0f);
+      sv[q] = (e >> logL) < Mx ? __ldg(sh + (size_t)(e >> logL) * xs + (e & (L - 1))) : make_float2(0.0f, 0.0f);
     }
 #pragma unroll
     for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
       const int e = threadIdx.x + q * SPEC_THREADS;
-      if (e < (L << logMx)) {
+      if ((e >> logL) < Mx) {
         float2 s = sv[q];
         if (P.g.conj) s.y = -s.y;
         const int k = swz(e >> logL, e & (L - 1), L);
@@ -385,7 +449,7 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(
       }
     }
     __syncthreads();
-    res = fft_block<true, LM, LL>(res, res == sm ? sm2 : sm, logMx, logL, P.g.tw[0], false, 2 * nx <= Mx);
+    res = fft_block<true, MP, LL>(res, res == sm ? sm2 : sm, Mx, logL, P.g.tw[0], false, 2 * nx <= Mx);
   }
   for (int e = threadIdx.x; e < nx * L; e += SPEC_THREADS) {
     const int c = e & (L - 1), i = e >> logL;
@@ -394,14 +458,14 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(
 }
 
 // z inverse: lines (x, y), A in, dose pair out (real part, imaginary part).
-template <int LM>
+template <int MP, int LL>
 __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_inverse_kernel(SpecLaunch P) {
   extern __shared__ float2 spec_sm[];
   float2* sm = spec_sm;
   float2* sm2 = spec_sm + SPEC_ELEMS;
   const SpecPair& pr = P.p[blockIdx.y];
-  const int logMz = LM >= 0 ? LM : P.g.logM[2], Mz = 1 << logMz;
-  const int logL = 12 - logMz, L = 1 << logL;
+  const int Mz = MP > 0 ? MP : P.g.M[2];
+  const int logL = MP > 0 ? LL : P.g.logL[2], L = 1 << logL;
   const int nl = P.g.n[0] * P.g.n[1], nz = P.g.n[2];
   const int l0 = blockIdx.x * L;
   {
@@ -409,20 +473,20 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_inverse
 #pragma unroll
     for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
       const int e = threadIdx.x + q * SPEC_THREADS;
-      const int l = l0 + (e >> logMz);
-      v[q] = l < nl ? pr.a[(size_t)l * Mz + (e & (Mz - 1))] : make_float2(0.0f, 0.0f);
+      const int c = e / Mz, i = e - c * Mz, l = l0 + c;
+      v[q] = (c < L && l < nl) ? pr.a[(size_t)l * Mz + i] : make_float2(0.0f, 0.0f);
     }
 #pragma unroll
     for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
       const int e = threadIdx.x + q * SPEC_THREADS;
-      sm[swz(e & (Mz - 1), e >> logMz, L)] = v[q];
+      const int c = e / Mz, i = e - c * Mz;
+      if (c < L) sm[swz(i, c, L)] = v[q];
     }
   }
   __syncthreads();
-  const float2* res =
-      fft_block<true, LM, (LM >= 0 ? 12 - LM : -1)>(sm, sm2, logMz, logL, P.g.tw[2], false, 2 * nz <= Mz);
-  for (int e = threadIdx.x; e < SPEC_ELEMS; e += SPEC_THREADS) {
-    const int i = e & (Mz - 1), c = e >> logMz, l = l0 + c;
+  const float2* res = fft_block<true, MP, LL>(sm, sm2, Mz, logL, P.g.tw[2], false, 2 * nz <= Mz);
+  for (int e = threadIdx.x; e < L * Mz; e += SPEC_THREADS) {
+    const int c = e / Mz, i = e - c * Mz, l = l0 + c;
     if (l < nl && i < nz) {
       const float2 v = res[swz(i, c, L)];
       pr.d1[(size_t)l * nz + i] = v.x;
@@ -438,15 +502,26 @@ __global__ void spec_scatter_kernel(const long long* __restrict__ idx, const flo
 }
 
 // ---------------------------------------------------------------- host --
+// Periods: 2^a and 3 * 2^a (a >= 4) up to SPEC_MAX_PERIOD, ascending.
+std::vector<int> spec_periods() {
+  std::vector<int> p;
+  for (int m = SPEC_MIN_PERIOD; m <= SPEC_MAX_PERIOD; m *= 2) {
+    p.push_back(m);
+    if (3 * m <= SPEC_MAX_PERIOD) p.push_back(3 * m);
+  }
+  std::sort(p.begin(), p.end());
+  return p;
+}
+
 int spec_period(int n) {
-  int m = SPEC_MIN_PERIOD;
-  while (m < 2 * n - 1) m <<= 1;
-  return m;
+  for (int m : spec_periods())
+    if (m >= 2 * n - 1) return m;
+  return 0;
 }
 
 std::vector<float2> spec_twiddles() {
   std::vector<float2> t;
-  for (int M = SPEC_MIN_PERIOD; M <= SPEC_MAX_PERIOD; M <<= 1)
+  for (int M : spec_periods())
     for (int k = 0; k < M; ++k) {
       const double a = -2.0 * 3.14159265358979323846 * (double)k / (double)M;
       t.push_back(make_float2((float)std::cos(a), (float)std::sin(a)));
@@ -454,52 +529,68 @@ std::vector<float2> spec_twiddles() {
   return t;
 }
 
-size_t spec_twiddle_offset(int M) { return (size_t)M - SPEC_MIN_PERIOD; }
+size_t spec_twiddle_offset(int M) {
+  size_t o = 0;
+  for (int m : spec_periods()) {
+    if (m == M) return o;
+    o += m;
+  }
+  return o;
+}
+
+// log2 of the lines per CTA of a pass of period M: the largest power of two
+// L with L M <= SPEC_ELEMS, for passes along y and x also dividing Mz
+int spec_lines_log2(int M) {
+  int l = 0;
+  while ((2 << l) * M <= SPEC_ELEMS) ++l;
+  return l;
+}
+int spec_pass_lines_log2(int M, int Mz) {
+  int t = 0;
+  while (((Mz >> t) & 1) == 0) ++t;
+  return std::min(spec_lines_log2(M), t);
+}
 
 // Compile-time periods for the common shapes (grids of 17 to 256 voxels per
-// axis): a pass is specialised when its lines per CTA are 4096 / M.
-#define SPEC_FOR_PERIODS(X) X(6, 6) X(7, 5) X(8, 4) X(9, 3)
+// axis): a pass is specialised when its lines per CTA are the natural ones.
+#define SPEC_FOR_PERIODS(X) X(64, 6) X(96, 5) X(128, 5) X(192, 4) X(256, 4) X(384, 3) X(512, 3)
 
-template <int LM, int LL>
+template <int MP, int LL>
 cudaError_t set_smem() {
   cudaError_t e = cudaSuccess;
-  for (const void* f : {(const void*)spec_z_forward_kernel<LM>, (const void*)spec_y_kernel<false, LM, LL>,
-                        (const void*)spec_y_kernel<true, LM, LL>, (const void*)spec_x_kernel<false, LM, LL>,
-                        (const void*)spec_x_kernel<true, LM, LL>, (const void*)spec_z_inverse_kernel<LM>})
+  for (const void* f : {(const void*)spec_z_forward_kernel<MP, LL>, (const void*)spec_y_kernel<false, MP, LL>,
+                        (const void*)spec_y_kernel<true, MP, LL>, (const void*)spec_x_kernel<false, MP, LL>,
+                        (const void*)spec_x_kernel<true, MP, LL>, (const void*)spec_z_inverse_kernel<MP, LL>})
     if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_SMEM);
   return e;
 }
 
 cudaError_t setup_spec_kernels() {
   cudaError_t e = set_smem<-1, -1>();
-#define SPEC_SET(lm, ll) \
-  if (e == cudaSuccess) e = set_smem<lm, ll>();
+#define SPEC_SET(mp, ll) \
+  if (e == cudaSuccess) e = set_smem<mp, ll>();
   SPEC_FOR_PERIODS(SPEC_SET)
 #undef SPEC_SET
   return e;
 }
 
-// Each pass is launched specialised when (log2 M, log2 L) is one of
+// Each pass is launched specialised when (period, lines) is one of
 // SPEC_FOR_PERIODS, generic otherwise.
 void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
   const SpecGrid& g = L.g;
   const int nl = g.n[0] * g.n[1];
-  const int Lz = SPEC_ELEMS / g.M[2];
-  const int Ly = std::min(SPEC_ELEMS / g.M[1], g.M[2]);
-  const int Lx = std::min(SPEC_ELEMS / g.M[0], g.M[2]);
+  const int Lz = 1 << g.logL[2], Ly = 1 << g.logL[1], Lx = 1 << g.logL[0];
   const dim3 gz((nl + Lz - 1) / Lz, L.n_pairs), gy(g.n[0] * (g.M[2] / Ly), L.n_pairs);
   const unsigned gx = g.M[1] * (g.M[2] / Lx) * L.n_pairs;
-  const int lz = g.logM[2], ly = g.logM[1], lx = g.logM[0];
-  const bool sy = (SPEC_ELEMS / g.M[1]) == Ly, sx = (SPEC_ELEMS / g.M[0]) == Lx;
   bool z_done = false, y_done = false, x_done = false;
-#define SPEC_Z(lm, ll) \
-  if (!z_done && lz == lm) { spec_z_forward_kernel<lm><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L); z_done = true; }
-#define SPEC_Y(lm, ll) \
-  if (!y_done && sy && ly == lm) { spec_y_kernel<false, lm, ll><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L); y_done = true; }
-#define SPEC_X(lm, ll) \
-  if (!x_done && sx && lx == lm) { spec_x_kernel<true, lm, ll><<<gx, SPEC_THREADS, SPEC_SMEM, st>>>(L); x_done = true; }
+#define SPEC_Z(mp, ll) \
+  if (!z_done && g.M[2] == mp && g.logL[2] == ll) { spec_z_forward_kernel<mp, ll><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L); z_done = true; }
+#define SPEC_Y(mp, ll) \
+  if (!y_done && g.M[1] == mp && g.logL[1] == ll) { spec_y_kernel<false, mp, ll><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L); y_done = true; }
+#define SPEC_X(mp, ll) \
+  if (!x_done && g.M[0] == mp && g.logL[0] == ll) { spec_x_kernel<true, mp, ll><<<gx, SPEC_THREADS, SPEC_SMEM, st>>>(L); x_done = true; }
   SPEC_FOR_PERIODS(SPEC_Z)
-  if (!z_done) spec_z_forward_kernel<-1><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  if (!z_done) spec_z_forward_kernel<-1, -1><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
   SPEC_FOR_PERIODS(SPEC_Y)
   if (!y_done) spec_y_kernel<false, -1, -1><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L);
   SPEC_FOR_PERIODS(SPEC_X)
@@ -508,14 +599,14 @@ void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
 #undef SPEC_Y
 #undef SPEC_X
   y_done = z_done = false;
-#define SPEC_YI(lm, ll) \
-  if (!y_done && sy && ly == lm) { spec_y_kernel<true, lm, ll><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L); y_done = true; }
-#define SPEC_ZI(lm, ll) \
-  if (!z_done && lz == lm) { spec_z_inverse_kernel<lm><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L); z_done = true; }
+#define SPEC_YI(mp, ll) \
+  if (!y_done && g.M[1] == mp && g.logL[1] == ll) { spec_y_kernel<true, mp, ll><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L); y_done = true; }
+#define SPEC_ZI(mp, ll) \
+  if (!z_done && g.M[2] == mp && g.logL[2] == ll) { spec_z_inverse_kernel<mp, ll><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L); z_done = true; }
   SPEC_FOR_PERIODS(SPEC_YI)
   if (!y_done) spec_y_kernel<true, -1, -1><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L);
   SPEC_FOR_PERIODS(SPEC_ZI)
-  if (!z_done) spec_z_inverse_kernel<-1><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  if (!z_done) spec_z_inverse_kernel<-1, -1><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
 #undef SPEC_YI
 #undef SPEC_ZI
 }
@@ -524,11 +615,9 @@ void launch_spec_build(const SpecLaunch& L, const long long* idx, const float* v
                        cudaStream_t st) {
   const SpecGrid& g = L.g;
   const int nl = g.n[0] * g.n[1];
-  const int Lz = SPEC_ELEMS / g.M[2];
-  const int Ly = std::min(SPEC_ELEMS / g.M[1], g.M[2]);
-  const int Lx = std::min(SPEC_ELEMS / g.M[0], g.M[2]);
+  const int Lz = 1 << g.logL[2], Ly = 1 << g.logL[1], Lx = 1 << g.logL[0];
   if (n_val > 0) spec_scatter_kernel<<<(n_val + 255) / 256, 256, 0, st>>>(idx, val, n_val, s_real);
-  spec_z_forward_kernel<-1><<<dim3((nl + Lz - 1) / Lz, 1), SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  spec_z_forward_kernel<-1, -1><<<dim3((nl + Lz - 1) / Lz, 1), SPEC_THREADS, SPEC_SMEM, st>>>(L);
   spec_y_kernel<false, -1, -1><<<dim3(g.n[0] * (g.M[2] / Ly), 1), SPEC_THREADS, SPEC_SMEM, st>>>(L);
   spec_x_kernel<false, -1, -1><<<g.M[1] * (g.M[2] / Lx), SPEC_THREADS, SPEC_SMEM, st>>>(L);
 }

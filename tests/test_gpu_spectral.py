@@ -123,7 +123,7 @@ def test_spectrum_cache_follows_prepare_and_kernel(eng, settings):
         N.check(eng.L.ch_plan_memory(eng.plan, ctypes.byref(t), ctypes.byref(s)), "ch_plan_memory")
         return t.value
 
-    spectrum = 64 * 64 * 64 * 8                          # periods of 24 x 20 x 18: 64 each, complex float32
+    spectrum = 48 * 48 * 48 * 8                          # periods of 24 x 20 x 18: 48 (3 x 16) each, complex float32
     eng.set_kernel(settings["energy_weights"])
     eng.prepare((32, 32, 32), (0.5, 0.5, 0.5))          # stencils for this spacing (and 32^3's spectrum)
     before = tables()
