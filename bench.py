@@ -327,6 +327,24 @@ def batched_extras(args, dev):
             "kernels_per_batch": 2 * args.batch_beams + 3, "graph_launches_per_batch": 1}
 
 
+def stage_rooflines(stats, beams, n_vox, cone_bytes, cone_ms, hbm_peak, method):
+    """Each stage's achieved HBM rate on its algorithmic bytes (CUDA events
+    the library records on the launching stream), against the measured peak.
+    prologue: the density read and the TERMA write, 8 N bytes per beam (the
+    per-ray density gathers hit L2); cone: as in `roofline`."""
+    pro_ms = statistics.mean(x["ms_prologue"] for x in stats)
+    pro_bytes = beams * 8 * n_vox
+    out = {"prologue": {"ms": pro_ms, "algorithmic_bytes": pro_bytes,
+                        "achieved_gbs": pro_bytes / (pro_ms * 1e-3) / 1e9,
+                        "frac": pro_bytes / (pro_ms * 1e-3) / 1e9 / hbm_peak,
+                        "bound": "instruction issue (exact DDA per listed voxel)"},
+           "cone": {"ms": cone_ms, "algorithmic_bytes": cone_bytes,
+                    "achieved_gbs": cone_bytes / (cone_ms * 1e-3) / 1e9,
+                    "frac": cone_bytes / (cone_ms * 1e-3) / 1e9 / hbm_peak,
+                    "method": method}}
+    return out
+
+
 def spectral_period(n):
     """FFT period of one axis: the smallest 2^a or 3 * 2^a (a >= 4) >= 2 n - 1."""
     periods = sorted({16 << a for a in range(9)} | {48 << a for a in range(7)})
@@ -461,10 +479,11 @@ def run_ours(args):
 
     # ---- e2e through the C ABI with pinned host buffers.  Every step copies
     # its density and block crops host -> device, runs the batch and copies
-    # every dose device -> host.  Two buffer sets let step s's dose copies
-    # (on a copy stream) overlap step s + 1's compute; the timed region runs
-    # from the first copy in to the last copy out, the L2 flush of each step
-    # included.
+    # every dose device -> host.  Two buffer sets and three streams pipeline
+    # the steps: step s + 1's inputs go up (copy-in stream) and step s - 1's
+    # doses come down (copy-out stream) while step s computes.  The timed
+    # region runs from the first copy in to the last copy out, the L2 flush
+    # of each step included.
     e2e = None
     if rank == 0 or True:
         from conehead_gb300.engine import DeviceBlock
@@ -476,41 +495,60 @@ def run_ours(args):
         d_rho = [torch.empty_like(rho) for _ in range(sets)]
         d_blocks = [[torch.empty_like(db.crop) for db in dblocks[:B]] for _ in range(sets)]
         d_doses = [[torch.empty(ph.size, dtype=torch.float32, device=dev) for _ in range(B)] for _ in range(sets)]
-        copy_st = torch.cuda.Stream(dev)
-        copied = [None] * sets
+        in_st, out_st = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+        computed, uploaded, copied = [None] * sets, [None] * sets, [None] * sets
+        # the job descriptors of a buffer set point at its device buffers and
+        # do not change between steps (the data they point at does): built once
+        set_jobs = [[eng.job(ph, d_rho[k], beams[i][0],
+                             DeviceBlock(d_blocks[k][i], dblocks[i].r0, dblocks[i].c0, dblocks[i].full_shape,
+                                         dblocks[i].uniform),
+                             SETTINGS, dose=d_doses[k][i]) for i in range(B)] for k in range(sets)]
 
-        def e2e_step(s):
+        def upload(s):
+            k = s % sets
+            if computed[k] is not None:
+                in_st.wait_event(computed[k])     # step s - 2 no longer reads set k's inputs
+            with torch.cuda.stream(in_st):
+                d_rho[k].copy_(h_rho, non_blocking=True)
+                for i in range(B):
+                    d_blocks[k][i].copy_(h_blocks[i], non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(in_st)
+            uploaded[k] = ev
+
+        def compute(s):
             k = s % sets
             flush.fill_(float(s))
+            st.wait_event(uploaded[k])
             if copied[k] is not None:
                 st.wait_event(copied[k])          # set k's doses of step s - 2 are on the host
-            d_rho[k].copy_(h_rho, non_blocking=True)
-            jobs = []
-            for i in range(B):
-                d_blocks[k][i].copy_(h_blocks[i], non_blocking=True)
-                db = dblocks[i]
-                jobs.append(eng.job(ph, d_rho[k], beams[i][0],
-                                    DeviceBlock(d_blocks[k][i], db.r0, db.c0, db.full_shape, db.uniform),
-                                    SETTINGS, dose=d_doses[k][i]))
-            eng.run_batch(jobs)
+            eng.run_batch(set_jobs[k])
             done = torch.cuda.Event()
             done.record(st)
-            copy_st.wait_event(done)
-            with torch.cuda.stream(copy_st):
+            computed[k] = done
+            out_st.wait_event(done)
+            with torch.cuda.stream(out_st):
                 for i in range(B):
                     h_doses[k][i].copy_(d_doses[k][i], non_blocking=True)
             ev = torch.cuda.Event()
-            ev.record(copy_st)
+            ev.record(out_st)
             copied[k] = ev
 
-        for s in range(args.warmup):
-            e2e_step(s)
+        def run_steps(first, count):
+            upload(first)
+            for s in range(first, first + count):
+                if s + 1 < first + count:
+                    upload(s + 1)
+                compute(s)
+
+        run_steps(0, args.warmup)
         torch.cuda.synchronize(dev)
         barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        # e0 is recorded on the compute stream before the first upload is issued
         e0.record(st)
-        for s in range(args.warmup, args.warmup + args.steps):
-            e2e_step(s)
+        in_st.wait_event(e0)
+        run_steps(args.warmup, args.steps)
         for ev in copied:
             if ev is not None:
                 st.wait_event(ev)
@@ -521,7 +559,8 @@ def run_ours(args):
         h2d = h_rho.numel() * 4 + sum(h.numel() * 4 for h in h_blocks)
         e2e = {"value": world * args.steps * B / e2e_s, "unit": "beams/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(B * N * 4),
-               "pipelined": "two buffer sets: step s's dose copies overlap step s+1's compute"}
+               "pipelined": "two buffer sets, copy-in / compute / copy-out streams: step s+1's inputs and "
+                            "step s-1's doses move while step s computes; each set's job descriptors built once"}
 
     # ---- extras: single-beam latency, plain scatter path, CPU baseline (rank 0)
     extras = {}
@@ -580,6 +619,7 @@ def run_ours(args):
             "e2e": e2e,
             "clocks": clk,
             "cone_method": method,
+            "stages": stage_rooflines(stats, B, N, alg_bytes, cone_ms, hbm_peak, method),
             "gpu_launches": args.steps * launches_per_step,
             "schedule": schedule,
         }
