@@ -327,6 +327,43 @@ def batched_extras(args, dev):
             "kernels_per_batch": 2 * args.batch_beams + 3, "graph_launches_per_batch": 1}
 
 
+def reference_updates(eng, ph, jobs):
+    """Voxel·direction updates the reference's cone scatter does per beam
+    (conehead/conehead.py:385-488): for every voxel with TERMA != 0, each of
+    the 576 directions (the 12 phi = 180 deg repeats included), one update per
+    voxel its DDA walk visits inside the grid.  Walk offsets come from the
+    library's DDA hook traced from the centre of a (2n - 1) grid (every offset
+    two voxels of the n grid can have), the TERMA support from the beam's
+    intermediates; counted with a summed-area table.  Mean over `jobs`."""
+    from conehead_gb300.engine import dda_trace
+    n = [int(k) for k in ph.size]
+    dirs = eng.cone_directions()
+    big = [2 * k - 1 for k in n]
+    c = np.array([k - 1 for k in n], dtype=np.int32)
+    vox, _, ln = dda_trace(big, [float(x) for x in ph.spacing], np.tile(c, (len(dirs), 1)), dirs,
+                           cap=sum(big) + 2, device=eng.device.index)
+    offs = [vox[u, :ln[u]] - c for u in range(len(dirs))]
+    per_beam = []
+    for job in jobs:
+        _, inter = eng.run(job, intermediates=True)
+        eng.sync()
+        mask = (inter["terma"] != 0).cpu().numpy()
+        S = np.zeros([k + 1 for k in n], dtype=np.int64)
+        S[1:, 1:, 1:] = mask.astype(np.int64).cumsum(0).cumsum(1).cumsum(2)
+        total = 0
+        for O in offs:
+            lo = np.clip(-O, 0, None)                          # sources s with s + O inside the grid
+            hi = np.minimum(np.array(n) - 1 - O, np.array(n) - 1) + 1
+            ok = np.all(hi > lo, axis=1)
+            lo, hi = lo[ok], hi[ok]
+            x0, y0, z0 = lo.T
+            x1, y1, z1 = hi.T
+            total += int((S[x1, y1, z1] - S[x0, y1, z1] - S[x1, y0, z1] - S[x1, y1, z0] + S[x0, y0, z1]
+                          + S[x0, y1, z0] + S[x1, y0, z0] - S[x0, y0, z0]).sum())
+        per_beam.append(total)
+    return float(np.mean(per_beam))
+
+
 def stage_rooflines(stats, beams, n_vox, cone_bytes, cone_ms, hbm_peak, method):
     """Each stage's achieved HBM rate on its algorithmic bytes (CUDA events
     the library records on the launching stream), against the measured peak.
@@ -562,6 +599,17 @@ def run_ours(args):
                "pipelined": "two buffer sets, copy-in / compute / copy-out streams: step s+1's inputs and "
                             "step s-1's doses move while step s computes; each set's job descriptors built once"}
 
+    # ---- reference-equivalent voxel·direction updates/s (untimed, a few beams)
+    updates_line = None
+    if rank == 0 and args.update_beams > 0:
+        w = reference_updates(eng, ph, [eng.job(ph, rho, beams[i][0], dblocks[i], SETTINGS)
+                                        for i in range(min(args.update_beams, B))])
+        updates_line = {"metric": "reference-equivalent voxel·direction updates/s", "per_beam": w,
+                        "value": w * value, "e2e_value": w * e2e["value"] if e2e else None,
+                        "basis": "updates the reference's per-voxel cone scatter does per beam (every "
+                                 "TERMA voxel, 576 directions, every in-grid walk voxel), mean of "
+                                 f"{min(args.update_beams, B)} beams of the workload, times beams/s"}
+
     # ---- extras: single-beam latency, plain scatter path, CPU baseline (rank 0)
     extras = {}
     if rank == 0 and not args.no_extras:
@@ -620,6 +668,7 @@ def run_ours(args):
             "clocks": clk,
             "cone_method": method,
             "stages": stage_rooflines(stats, B, N, alg_bytes, cone_ms, hbm_peak, method),
+            "updates": updates_line,
             "gpu_launches": args.steps * launches_per_step,
             "schedule": schedule,
         }
@@ -649,6 +698,8 @@ def main(argv=None):
     ap.add_argument("--batch-beams", type=int, default=64, help="beams of the captured mixed batch (0: skip)")
     ap.add_argument("--batch-iters", type=int, default=5)
     ap.add_argument("--no-autotune", action="store_true", help="time the default schedule")
+    ap.add_argument("--update-beams", type=int, default=4,
+                    help="beams sampled for the reference-equivalent updates/s (0: skip)")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only", choices=["serving", "adjoint", "batched"], default=None,
