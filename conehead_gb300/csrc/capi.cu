@@ -596,7 +596,8 @@ ch_status spec_shat(ch_plan* P, const StencilSet& S, const int* n, cudaStream_t 
   SpecLaunch L{};
   L.g = spec_grid(P, M, M, M[2], 0, nullptr);
   L.n_pairs = 1;
-  L.p[0] = SpecPair{s_real.as<float>(), nullptr, work.as<float2>(), E->shat.as<float2>(), nullptr, nullptr};
+  L.p[0] = SpecPair{s_real.as<float>(), nullptr, nullptr, nullptr, work.as<float2>(), E->shat.as<float2>(),
+                    nullptr, nullptr};
   launch_spec_build(L, d_idx.as<long long>(), d_val.as<float>(), (int)idx.size(), s_real.as<float>(), s);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -779,6 +780,7 @@ struct BeamJob {
   size_t t_off;        // float offset in the T arena
   size_t r_off;        // uint32 offset in the ranges arena
   size_t l_off;        // int offset of the beam's voxel list
+  size_t f_off;        // int offset of its per-line flags (one byte per (x, y) line)
   int ntile[3];
   int n_tiles;
   int n_units;
@@ -939,6 +941,7 @@ ScratchNeed scratch_need(int n, const ch_grid* grids, int U, bool spectral = fal
                          ((grids[i].n[2] + TZ - 1) / TZ);
     r_total += tiles * U;
     l_total += ((size_t)grids[i].n[0] * grids[i].n[1] * grids[i].n[2] + 63) / 64 * 64;
+    l_total += ((size_t)grids[i].n[0] * grids[i].n[1] + 255) / 256 * 64;     // line flags
   }
   ScratchNeed r;
   r.bytes[0] = t_total * sizeof(float);
@@ -1050,6 +1053,8 @@ ch_status plan_batch(ch_plan* P, int n, const ch_grid* grids, const float* const
     t_total = (t_total + 63) / 64 * 64;
     J.l_off = l_total;
     l_total += ((size_t)J.g.n[0] * J.g.n[1] * J.g.n[2] + 63) / 64 * 64;
+    J.f_off = l_total;
+    l_total += ((size_t)J.g.n[0] * J.g.n[1] + 255) / 256 * 64;
     J.ntile[0] = (J.g.n[0] + TX - 1) / TX;
     J.ntile[1] = (J.g.n[1] + TY - 1) / TY;
     J.ntile[2] = (J.g.n[2] + TZ - 1) / TZ;
@@ -1120,6 +1125,8 @@ std::vector<PrologueBeam> make_prologue_records(const BatchPlan& B, const Scratc
     R.T = S.T + J.t_off;
     R.aabb = S.aabb + 8 * i;
     R.list_v = S.list_v + J.l_off;
+    R.line_any = reinterpret_cast<unsigned char*>(S.list_v + J.f_off);
+    R.zero_all = B.spectral ? 0 : 1;
   }
   return pb;
 }
@@ -1187,8 +1194,12 @@ ch_status enqueue_batch(ch_plan* P, const BatchPlan& B, const Scratch& S, const 
         const SpecPlanPair& pr = l.pairs[q];
         const BeamJob& J1 = B.jobs[pr.j1];
         const BeamJob* J2 = pr.j2 >= 0 ? &B.jobs[pr.j2] : nullptr;
-        L.p[q] = SpecPair{S.T + J1.t_off, J2 ? S.T + J2->t_off : nullptr, S.spec + pr.a_off, S.spec + pr.b_off,
-                          J1.dose, J2 ? J2->dose : nullptr};
+        // line flags exist when the batched prologue ran (no intermediates)
+        const unsigned char* f1 = inter ? nullptr : reinterpret_cast<const unsigned char*>(S.list_v + J1.f_off);
+        const unsigned char* f2 =
+            (inter || !J2) ? nullptr : reinterpret_cast<const unsigned char*>(S.list_v + J2->f_off);
+        L.p[q] = SpecPair{S.T + J1.t_off, J2 ? S.T + J2->t_off : nullptr, f1, f2, S.spec + pr.a_off,
+                          S.spec + pr.b_off, J1.dose, J2 ? J2->dose : nullptr};
       }
       launch_spec_pairs(L, s);
       CH_CUDA(cudaGetLastError());
@@ -1598,7 +1609,8 @@ ch_status cone_operator(ch_plan* P, const ch_grid& grid, const float* in_dense, 
     SL.g = spec_grid(P, l.n, l.M, grid.n[2], transpose ? 1 : 0, shat);
     SL.n_pairs = 1;
     float2* w = P->spec_work.as<float2>();
-    SL.p[0] = SpecPair{in_dense, nullptr, w + l.pairs[0].a_off, w + l.pairs[0].b_off, out, nullptr};
+    SL.p[0] = SpecPair{in_dense, nullptr, nullptr, nullptr, w + l.pairs[0].a_off, w + l.pairs[0].b_off, out,
+                       nullptr};
     launch_spec_pairs(SL, s);
     CH_CUDA(cudaGetLastError());
     return CH_OK;

@@ -237,6 +237,8 @@ constexpr int SPEC_SMEM = 2 * SPEC_ELEMS * 8;   // two ping-pong buffers of floa
 struct SpecPair {
   const float* t1;   // TERMA of the first beam [nx][ny][zp]
   const float* t2;   // of the second (NULL: none)
+  const unsigned char* l1;  // lines of t1 that may be nonzero (NULL: every line is read)
+  const unsigned char* l2;  // of t2
   float2* a;         // [nx][ny][Mz]
   float2* b;         // [nx][My][Mz]
   float* d1;         // dose of the first beam [nx][ny][nz]
@@ -277,6 +279,9 @@ struct PrologueBeam {
   float* T;          // [nx][ny][zp]
   int* aabb;         // 8 ints: TERMA box, list count at [6]
   int* list_v;       // this beam's voxel list (nx ny nz entries)
+  unsigned char* line_any;  // per (x, y) line: 1 when the line holds a listed voxel
+  int zero_all;      // 1: zero TERMA on every line (the gather reads it anywhere);
+                     // 0: only on lines with listed voxels (the spectral path reads line_any)
 };
 
 // ------------------------------------------------------------ launchers --

@@ -331,15 +331,20 @@ __device__ float radiological_depth(const float* __restrict__ rho, const GridDev
 // blocking/depth/TERMA pass runs on full warps.
 // One warp per (x, y) line of the grid, lanes along z: the index arithmetic
 // runs once per line and the zeroing of TERMA is coalesced.
+// zero_all = 0: TERMA is zeroed only on lines with listed voxels, and
+// line_any (if set) records which lines those are.
 __device__ __forceinline__ void cull_line(const GridDev& g, const BeamDev& b, float* __restrict__ T,
                                           const Inter& inter, int all_voxels, int* __restrict__ list_count,
-                                          int* __restrict__ list_v, int line) {
+                                          int* __restrict__ list_v, int line, unsigned char* line_any = nullptr,
+                                          int zero_all = 1) {
   // volumes hold fewer than 2^31 voxels (checked on the host)
   if (line >= g.n[0] * g.n[1]) return;   // whole warp
   const int lane = threadIdx.x & 31;
   const int x = line / g.n[1], y = line - x * g.n[1];
   const float px = voxel_centre(g.origin[0], g.spacing[0], x);
   const float py = voxel_centre(g.origin[1], g.spacing[1], y);
+  float* Tl = T + ((size_t)x * g.n[1] + y) * g.zp;
+  bool any = false;
   for (int z0 = 0; z0 < g.n[2]; z0 += 32) {
     const int z = z0 + lane;
     const bool live = z < g.n[2];
@@ -372,7 +377,7 @@ __device__ __forceinline__ void cull_line(const GridDev& g, const BeamDev& b, fl
         }
       }
       keep = candidate || all_voxels;
-      T[((size_t)x * g.n[1] + y) * g.zp + z] = 0.0f;
+      if (zero_all) Tl[z] = 0.0f;
       if (!keep) {
         if (inter.blocked) inter.blocked[v] = 0.0;
         if (inter.d_eff) inter.d_eff[v] = 0.0f;
@@ -385,12 +390,16 @@ __device__ __forceinline__ void cull_line(const GridDev& g, const BeamDev& b, fl
     }
     const unsigned m = __ballot_sync(0xffffffffu, keep);
     if (m) {
+      any = true;
       int base = 0;
       if (lane == 0) base = atomicAdd(list_count, __popc(m));
       base = __shfl_sync(0xffffffffu, base, 0);
       if (keep) list_v[base + __popc(m & ((1u << lane) - 1u))] = v;
     }
   }
+  if (!zero_all && any)
+    for (int z = lane; z < g.n[2]; z += 32) Tl[z] = 0.0f;
+  if (line_any && lane == 0) line_any[line] = any ? 1 : 0;
 }
 
 __global__ void __launch_bounds__(256) cull_kernel(GridDev g, BeamDev b, float* __restrict__ T, Inter inter,
@@ -412,7 +421,8 @@ __device__ __forceinline__ void load_record(const PrologueBeam* __restrict__ rec
 __global__ void __launch_bounds__(256) cull_batch_kernel(const PrologueBeam* __restrict__ recs) {
   __shared__ PrologueBeam R;
   load_record(recs, R);
-  cull_line(R.g, R.b, R.T, Inter{}, 0, R.aabb + 6, R.list_v, (blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  cull_line(R.g, R.b, R.T, Inter{}, 0, R.aabb + 6, R.list_v, (blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+            R.line_any, R.zero_all);
 }
 
 // Pass 2, listed voxels: blocked fraction, then (where the beam is not

@@ -327,6 +327,28 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward
   const int logL = MP > 0 ? LL : P.g.logL[2], L = 1 << logL;
   const int nl = P.g.n[0] * P.g.n[1], nz = P.g.n[2];
   const int l0 = blockIdx.x * L;
+  // lines of each beam that may hold TERMA (the others are zero and are not
+  // read); a block without any transforms to zero
+  __shared__ unsigned char zf[2][SPEC_ELEMS / SPEC_MIN_PERIOD];
+  __shared__ int zany;
+  if (threadIdx.x == 0) zany = 0;
+  __syncthreads();
+  for (int c = threadIdx.x; c < L; c += SPEC_THREADS) {
+    const int l = l0 + c;
+    const bool f1 = l < nl && (!pr.l1 || pr.l1[l]);
+    const bool f2 = l < nl && pr.t2 && (!pr.l2 || pr.l2[l]);
+    zf[0][c] = f1;
+    zf[1][c] = f2;
+    if (f1 || f2) zany = 1;
+  }
+  __syncthreads();
+  if (!zany) {
+    for (int e = threadIdx.x; e < L * Mz; e += SPEC_THREADS) {
+      const int c = e / Mz, i = e - c * Mz, l = l0 + c;
+      if (l < nl) pr.a[(size_t)l * Mz + i] = make_float2(0.0f, 0.0f);
+    }
+    return;
+  }
   {
     // every load of the thread first, then the shared-memory stores
     float2 v[SPEC_ELEMS / SPEC_THREADS];
@@ -337,8 +359,8 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward
       v[q] = make_float2(0.0f, 0.0f);
       if (c < L && l < nl && i < nz) {
         const size_t o = (size_t)l * P.g.zp + i;
-        v[q].x = __ldg(pr.t1 + o);
-        if (pr.t2) v[q].y = __ldg(pr.t2 + o);
+        if (zf[0][c]) v[q].x = __ldg(pr.t1 + o);
+        if (zf[1][c]) v[q].y = __ldg(pr.t2 + o);
       }
     }
 #pragma unroll
