@@ -295,20 +295,22 @@ __device__ float radiological_depth(const float* __restrict__ rho, const GridDev
     for (int q = 0; q < DDA_UNROLL; ++q) {
       if (inside) {
         vi[q] = idx;
-        // the reference's choice, without divergent branches
-        const int ax = (t0 < t1) ? ((t0 < t2) ? 0 : 2) : ((t1 < t2) ? 1 : 2);
-        tv[q] = ax == 0 ? t0 : (ax == 1 ? t1 : t2);
-        const float n0t = fadd(t0, d0), n1t = fadd(t1, d1), n2t = fadd(t2, d2);
-        t0 = ax == 0 ? n0t : t0;
-        t1 = ax == 1 ? n1t : t1;
-        t2 = ax == 2 ? n2t : t2;
-        idx += ax == 0 ? dx : (ax == 1 ? dy : dz);
-        const int left = (ax == 0 ? left0 : (ax == 1 ? left1 : left2)) - 1;
-        left0 = ax == 0 ? left : left0;
-        left1 = ax == 1 ? left : left1;
-        left2 = ax == 2 ? left : left2;
+        const bool a01 = t0 < t1, s0 = a01 && t0 < t2, s1 = !a01 && t1 < t2;
+        tv[q] = s0 ? t0 : (s1 ? t1 : t2);
+        if (s0) {
+          t0 = fadd(t0, d0);
+          idx += dx;
+          inside = --left0 >= 0;
+        } else if (s1) {
+          t1 = fadd(t1, d1);
+          idx += dy;
+          inside = --left1 >= 0;
+        } else {
+          t2 = fadd(t2, d2);
+          idx += dz;
+          inside = --left2 >= 0;
+        }
         cnt = q + 1;
-        inside = left >= 0;
       }
     }
     float r[DDA_UNROLL];
