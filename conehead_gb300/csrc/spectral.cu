@@ -310,6 +310,50 @@ __device__ __forceinline__ float2* fft_block(float2* src, float2* dst, int M_rt,
   return src;
 }
 
+// ------------------------------------------------- line block transfers --
+// L lines of a pass along y or x: element (i, c) at base + i * stride + c
+// (the lines are L consecutive kz).  Two adjacent lines move in one 16-byte
+// access (stride, base and c are even); every load of a thread is issued
+// before its shared-memory stores.  Rows i >= n are zero (the padding).
+__device__ __forceinline__ void load_lines(const float2* __restrict__ base, size_t stride, int n, int M, int L,
+                                           int logL, float2* sm) {
+  if (L >= 2) {
+    float4 v[SPEC_ELEMS / SPEC_THREADS / 2];
+#pragma unroll
+    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS / 2; ++q) {
+      const int e = threadIdx.x + q * SPEC_THREADS;
+      const int c = (e & (L / 2 - 1)) * 2, i = e >> (logL - 1);
+      v[q] = i < n ? __ldg(reinterpret_cast<const float4*>(base + (size_t)i * stride + c))
+                   : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS / 2; ++q) {
+      const int e = threadIdx.x + q * SPEC_THREADS;
+      const int c = (e & (L / 2 - 1)) * 2, i = e >> (logL - 1);
+      if (i < M) {
+        sm[swz(i, c, L)] = make_float2(v[q].x, v[q].y);
+        sm[swz(i, c + 1, L)] = make_float2(v[q].z, v[q].w);
+      }
+    }
+  } else {
+    for (int i = threadIdx.x; i < M; i += SPEC_THREADS)
+      sm[swz(i, 0, L)] = i < n ? base[(size_t)i * stride] : make_float2(0.0f, 0.0f);
+  }
+}
+
+__device__ __forceinline__ void store_lines(const float2* res, float2* __restrict__ base, size_t stride, int n,
+                                            int L, int logL) {
+  if (L >= 2) {
+    for (int e = threadIdx.x; e < n * L / 2; e += SPEC_THREADS) {
+      const int c = (e & (L / 2 - 1)) * 2, i = e >> (logL - 1);
+      const float2 a = res[swz(i, c, L)], b = res[swz(i, c + 1, L)];
+      *reinterpret_cast<float4*>(base + (size_t)i * stride + c) = make_float4(a.x, a.y, b.x, b.y);
+    }
+  } else {
+    for (int i = threadIdx.x; i < n; i += SPEC_THREADS) base[(size_t)i * stride] = res[swz(i, 0, L)];
+  }
+}
+
 // ---------------------------------------------------------------- passes --
 // Every pass is a template on MP, its period, and LL, log2 of its lines per
 // CTA: MP > 0 fixes both at compile time, MP = -1 reads them from the launch
@@ -395,27 +439,11 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_y_kernel(
   float2* dst = INV ? pr.a + (size_t)x * ny * Mz : pr.b + (size_t)x * My * Mz;
   src += kz0;
   dst += kz0;
-  {
-    float2 v[SPEC_ELEMS / SPEC_THREADS];
-#pragma unroll
-    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
-      const int e = threadIdx.x + q * SPEC_THREADS;
-      const int c = e & (L - 1), i = e >> logL;
-      v[q] = (i < n_in) ? src[(size_t)i * Mz + c] : make_float2(0.0f, 0.0f);
-    }
-#pragma unroll
-    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
-      const int e = threadIdx.x + q * SPEC_THREADS;
-      if ((e >> logL) < My) sm[swz(e >> logL, e & (L - 1), L)] = v[q];
-    }
-  }
+  load_lines(src, Mz, n_in, My, L, logL, sm);
   __syncthreads();
   const float2* res = fft_block<INV, MP, LL>(sm, sm2, My, logL, P.g.tw[1], !INV && 2 * ny <= My,
                                              INV && 2 * ny <= My);
-  for (int e = threadIdx.x; e < n_out * L; e += SPEC_THREADS) {
-    const int c = e & (L - 1), i = e >> logL;
-    dst[(size_t)i * Mz + c] = res[swz(i, c, L)];
-  }
+  store_lines(res, dst, Mz, n_out, L, logL);
 }
 
 // x pass on B, lines (ky, kz) in blocks of L kz; consecutive CTAs take the
@@ -436,20 +464,7 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(
   const size_t xs = (size_t)My * Mz, off = (size_t)ky * Mz + kz0;
   float2* b = pr.b + off;
   const int nx = CONV ? P.g.n[0] : Mx;
-  {
-    float2 v[SPEC_ELEMS / SPEC_THREADS];
-#pragma unroll
-    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
-      const int e = threadIdx.x + q * SPEC_THREADS;
-      const int c = e & (L - 1), i = e >> logL;
-      v[q] = (i < nx) ? b[(size_t)i * xs + c] : make_float2(0.0f, 0.0f);
-    }
-#pragma unroll
-    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
-      const int e = threadIdx.x + q * SPEC_THREADS;
-      if ((e >> logL) < Mx) sm[swz(e >> logL, e & (L - 1), L)] = v[q];
-    }
-  }
+  load_lines(b, xs, nx, Mx, L, logL, sm);
   __syncthreads();
   float2* res = fft_block<false, MP, LL>(sm, sm2, Mx, logL, P.g.tw[0], 2 * nx <= Mx, false);
   if (CONV) {
@@ -473,10 +488,7 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(
     __syncthreads();
     res = fft_block<true, MP, LL>(res, res == sm ? sm2 : sm, Mx, logL, P.g.tw[0], false, 2 * nx <= Mx);
   }
-  for (int e = threadIdx.x; e < nx * L; e += SPEC_THREADS) {
-    const int c = e & (L - 1), i = e >> logL;
-    b[(size_t)i * xs + c] = res[swz(i, c, L)];
-  }
+  store_lines(res, b, xs, nx, L, logL);
 }
 
 // z inverse: lines (x, y), A in, dose pair out (real part, imaginary part).
