@@ -310,6 +310,55 @@ __device__ __forceinline__ float2* fft_block(float2* src, float2* dst, int M_rt,
   return src;
 }
 
+// ------------------------------------- period 256 with 16 lines per CTA --
+// 256 = 16 x 16 and 16 lines x 16 butterflies = SPEC_THREADS: each thread
+// takes butterfly j of line c in both stages (passes along y and x: c = t
+// mod 16, j = t / 16; along z, where lines are contiguous: j = t mod 16,
+// c = t / 16).  Stage 1 reads rows j + 16 r of the line (straight from
+// global memory); stage 2 ends with rows j + 16 q, q = k1 + 4 k2, in
+// v[4 k1 + k2] - the rows a first stage of butterfly j reads, so a transform
+// that follows on the same line starts from registers, and the last stage
+// stores to global memory: one shared-memory exchange and one barrier per
+// transform.  Element (i, c) sits at 16 i + (c ^ (i mod 16)) when 16 lanes
+// share j (the layout of the other periods) and at 16 i + (c ^ ((i ^ i / 16)
+// mod 16)) when they share c: either way the stage-1 writes (rows 16 j + q)
+// and stage-2 reads (rows j + 16 r) of 16 lanes fall in 16 different banks.
+constexpr int R16_LINES = 16;
+static_assert(R16_LINES * 16 == SPEC_THREADS, "one butterfly per thread and stage");
+template <bool ZL>
+__device__ __forceinline__ int swz16(int i, int c) {
+  return i * 16 + (c ^ ((ZL ? i ^ (i >> 4) : i) & 15));
+}
+
+// stage 1 (no twiddles) of the rows in v (v[8..15] zero with hin), out to sm
+template <bool INV, bool ZL>
+__device__ __forceinline__ void r16_first(float2 (&v)[16], bool hin, float2* sm, int j, int c) {
+  if (hin)
+    dft16_half_in<INV>(v);
+  else
+    dft16<INV>(v);
+  const int o = j << 4;
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) sm[swz16<ZL>(o + k1 + 4 * k2, c)] = v[4 * k1 + k2];
+}
+
+// stage 2 from sm: twiddles tw[r j] (conjugate for INV), then the DFT
+template <bool INV, bool ZL>
+__device__ __forceinline__ void r16_second(const float2* sm, float2 (&v)[16], int j, int c,
+                                           const float2* __restrict__ tw) {
+#pragma unroll
+  for (int r = 0; r < 16; ++r) v[r] = sm[swz16<ZL>(j + 16 * r, c)];
+#pragma unroll
+  for (int r = 1; r < 16; ++r) {
+    float2 w = __ldg(tw + r * j);
+    if (INV) w.y = -w.y;
+    v[r] = cmul(v[r], w);
+  }
+  dft16<INV>(v);
+}
+
 // ------------------------------------------------- line block transfers --
 // L lines of a pass along y or x: element (i, c) at base + i * stride + c
 // (the lines are L consecutive kz).  Two adjacent lines move in one 16-byte
@@ -393,6 +442,33 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward
     }
     return;
   }
+  if constexpr (MP == 256 && LL == 4) {
+    // TERMA rows z < nz <= 128 (the upper half is zero) straight from global
+    // memory; A written from the last stage
+    const int j = threadIdx.x & 15, c = threadIdx.x >> 4, l = l0 + c;
+    const bool ok = l < nl, f1 = zf[0][c], f2 = zf[1][c];
+    const size_t o = (size_t)(ok ? l : 0) * P.g.zp;
+    float2 v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const int i = j + 16 * r;
+      v[r] = make_float2(0.0f, 0.0f);
+      if (r < 8 && i < nz) {
+        if (f1) v[r].x = __ldg(pr.t1 + o + i);
+        if (f2) v[r].y = __ldg(pr.t2 + o + i);
+      }
+    }
+    r16_first<false, true>(v, true, sm, j, c);
+    __syncthreads();
+    r16_second<false, true>(sm, v, j, c, P.g.tw[2]);
+    if (ok) {
+#pragma unroll
+      for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+        for (int k2 = 0; k2 < 4; ++k2) pr.a[(size_t)l * Mz + j + 16 * (k1 + 4 * k2)] = v[4 * k1 + k2];
+    }
+    return;
+  }
   {
     // every load of the thread first, then the shared-memory stores
     float2 v[SPEC_ELEMS / SPEC_THREADS];
@@ -439,6 +515,32 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_y_kernel(
   float2* dst = INV ? pr.a + (size_t)x * ny * Mz : pr.b + (size_t)x * My * Mz;
   src += kz0;
   dst += kz0;
+  if constexpr (MP == 256 && LL == 4) {
+    // rows of the forward input y < ny <= 128: the upper half is zero
+    const int c = threadIdx.x & (R16_LINES - 1), j = threadIdx.x >> 4;
+    const float2* sl = src + c;
+    float2* dl = dst + c;
+    float2 v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const int i = j + 16 * r;
+      if (INV)
+        v[r] = __ldg(sl + (size_t)i * Mz);
+      else
+        v[r] = (r < 8 && i < ny) ? __ldg(sl + (size_t)i * Mz) : make_float2(0.0f, 0.0f);
+    }
+    r16_first<INV, false>(v, !INV, sm, j, c);
+    __syncthreads();
+    r16_second<INV, false>(sm, v, j, c, P.g.tw[1]);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+      for (int k2 = 0; k2 < (INV ? 2 : 4); ++k2) {
+        const int i = j + 16 * (k1 + 4 * k2);
+        if (!INV || i < ny) dl[(size_t)i * Mz] = v[4 * k1 + k2];
+      }
+    return;
+  }
   load_lines(src, Mz, n_in, My, L, logL, sm);
   __syncthreads();
   const float2* res = fft_block<INV, MP, LL>(sm, sm2, My, logL, P.g.tw[1], !INV && 2 * ny <= My,
@@ -464,6 +566,55 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(
   const size_t xs = (size_t)My * Mz, off = (size_t)ky * Mz + kz0;
   float2* b = pr.b + off;
   const int nx = CONV ? P.g.n[0] : Mx;
+  if constexpr (CONV && MP == 256 && LL == 4) {
+    // forward (input rows x < nx <= 128), times S^, inverse (rows x < nx
+    // kept); forward stage 2, the product and inverse stage 1 in registers
+    const int c = threadIdx.x & (R16_LINES - 1), j = threadIdx.x >> 4;
+    float2* bl = b + c;
+    {
+      // the S^ values this thread multiplies, copied to sm2 while the
+      // forward transform runs
+      const float2* sl = P.g.shat + off + c;
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const unsigned d = (unsigned)__cvta_generic_to_shared(sm2 + swz16<false>(j + 16 * q, c));
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(sl + (size_t)(j + 16 * q) * xs));
+      }
+      asm volatile("cp.async.commit_group;\n" ::);
+    }
+    float2 v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const int i = j + 16 * r;
+      v[r] = (r < 8 && i < nx) ? __ldg(bl + (size_t)i * xs) : make_float2(0.0f, 0.0f);
+    }
+    r16_first<false, false>(v, true, sm, j, c);
+    __syncthreads();
+    r16_second<false, false>(sm, v, j, c, P.g.tw[0]);
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    const float cs = P.g.conj ? -1.0f : 1.0f;
+    float2 u[16];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+      for (int k2 = 0; k2 < 4; ++k2) {
+        const int q = k1 + 4 * k2;
+        const float2 s = sm2[swz16<false>(j + 16 * q, c)];
+        u[q] = cmul(v[4 * k1 + k2], make_float2(s.x, cs * s.y));
+      }
+    __syncthreads();   // every read of sm (stage 2) and sm2 (S^) done
+    r16_first<true, false>(u, false, sm, j, c);
+    __syncthreads();
+    r16_second<true, false>(sm, u, j, c, P.g.tw[0]);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+      for (int k2 = 0; k2 < 2; ++k2) {
+        const int i = j + 16 * (k1 + 4 * k2);
+        if (i < nx) bl[(size_t)i * xs] = u[4 * k1 + k2];
+      }
+    return;
+  }
   load_lines(b, xs, nx, Mx, L, logL, sm);
   __syncthreads();
   float2* res = fft_block<false, MP, LL>(sm, sm2, Mx, logL, P.g.tw[0], 2 * nx <= Mx, false);
@@ -502,6 +653,31 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_inverse
   const int logL = MP > 0 ? LL : P.g.logL[2], L = 1 << logL;
   const int nl = P.g.n[0] * P.g.n[1], nz = P.g.n[2];
   const int l0 = blockIdx.x * L;
+  if constexpr (MP == 256 && LL == 4) {
+    // all of A's line in; rows z < nz <= 128 of the result out
+    const int j = threadIdx.x & 15, c = threadIdx.x >> 4, l = l0 + c;
+    const bool ok = l < nl;
+    const float2* al = pr.a + (size_t)(ok ? l : 0) * Mz;
+    float2 v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[r] = ok ? __ldg(al + j + 16 * r) : make_float2(0.0f, 0.0f);
+    r16_first<true, true>(v, false, sm, j, c);
+    __syncthreads();
+    r16_second<true, true>(sm, v, j, c, P.g.tw[2]);
+    if (ok) {
+#pragma unroll
+      for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+        for (int k2 = 0; k2 < 2; ++k2) {
+          const int i = j + 16 * (k1 + 4 * k2);
+          if (i < nz) {
+            pr.d1[(size_t)l * nz + i] = v[4 * k1 + k2].x;
+            if (pr.d2) pr.d2[(size_t)l * nz + i] = v[4 * k1 + k2].y;
+          }
+        }
+    }
+    return;
+  }
   {
     float2 v[SPEC_ELEMS / SPEC_THREADS];
 #pragma unroll

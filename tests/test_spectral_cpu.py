@@ -71,3 +71,44 @@ def test_the_transpose_is_a_correlation(oracle_lib, tables):
     rp[:n[0], :n[1], :n[2]] = r
     got = np.real(np.fft.ifftn(np.fft.fftn(rp) * np.conj(np.fft.fftn(circ))))[:n[0], :n[1], :n[2]]
     assert np.abs(got - ct).max() <= 1e-12 * np.abs(ct).max()
+
+
+def _swz16(i, c, z_lines):
+    """The period-256 passes' shared-memory slot of element (row i, line c)."""
+    return i * 16 + (c ^ ((i ^ (i >> 4)) if z_lines else i) & 15)
+
+
+def test_period_256_schedule_and_layouts():
+    """Period 256 as two radix-16 stages with butterfly j of a line reading
+    rows j + 16 r: stage 1 (no twiddles) leaves X1[j][q] at row 16 j + q,
+    stage 2 reads rows j + 16 r, multiplies by tw[r j] and its outputs land at
+    rows j + 16 q, the very rows stage 1 of a following transform of
+    butterfly j reads.  Both shared-memory layouts are permutations of the
+    4096 slots, and the 16 lanes of a stage access (16 lines at one j, or 16
+    j at one line on lines along z) fall in 16 different banks of 8 bytes."""
+    rng = np.random.default_rng(256)
+    x = rng.standard_normal((16, 256)) + 1j * rng.standard_normal((16, 256))
+    j = np.arange(16)
+    r = np.arange(16)
+    stage1 = np.fft.fft(x[:, j[:, None] + 16 * r[None, :]], axis=2)          # [line][j][q]
+    rows = np.empty((16, 256), complex)
+    rows[:, (16 * j[:, None] + r[None, :]).ravel()] = stage1.reshape(16, -1)
+    tw = np.exp(-2j * np.pi * np.arange(256) / 256)
+    z = rows[:, j[:, None] + 16 * r[None, :]] * tw[(r[None, :] * j[:, None])]   # [line][j][r]
+    out = np.fft.fft(z, axis=2)                                                # [line][j][q]
+    ref = np.fft.fft(x, axis=1)
+    got = ref[:, j[:, None] + 16 * r[None, :]]
+    assert np.abs(out - got).max() <= 1e-12 * np.abs(ref).max()
+    i, c = np.meshgrid(np.arange(256), np.arange(16), indexing="ij")
+    for zl in (False, True):
+        slots = _swz16(i, c, zl)
+        assert sorted(slots.ravel().tolist()) == list(range(4096))
+        for q in range(16):
+            for fixed in range(16):
+                if zl:   # 16 lanes share the line, j varies
+                    w = _swz16(16 * j + q, fixed, zl) % 16
+                    rd = _swz16(j + 16 * q, fixed, zl) % 16
+                else:    # 16 lanes share j, the line varies
+                    w = _swz16(16 * fixed + q, j, zl) % 16
+                    rd = _swz16(fixed + 16 * q, j, zl) % 16
+                assert len(set(w.tolist())) == 16 and len(set(rd.tolist())) == 16
