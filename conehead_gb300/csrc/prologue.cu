@@ -238,8 +238,16 @@ __device__ double blocked_fraction(const BeamDev& b, const GridDev& g, int S, co
     if (ok) {
       const int i0 = floor_cell(umin - SAMPLE_DELTA), i1 = floor_cell(umax + SAMPLE_DELTA);
       const int k0 = floor_cell(wmin - SAMPLE_DELTA), k1 = floor_cell(wmax + SAMPLE_DELTA);
-      if (i0 > -2000 && k0 > -2000 && cell_value(b, i0, k0) == 1.0f && cell_value(b, i1, k1) == 1.0f)
-        return c_unit_partial[27];
+      if (i0 > -2000 && k0 > -2000) {
+        if (cell_value(b, i0, k0) == 1.0f && cell_value(b, i1, k1) == 1.0f) return c_unit_partial[27];
+        // Wholly closed: the box misses the open rectangle of cells
+        // i in [br0 - 1999, br0 + brows - 2000], k likewise (within the map's
+        // [-1999, 1999]; the wrapped index -2000 is outside the box), so
+        // every sample reads 0 and blocked is the reference's sum of zeros.
+        const int oi0 = max(b.br0 - 1999, -1999), oi1 = min(b.br0 + b.brows - 2000, 1999);
+        const int ok0 = max(b.bc0 - 1999, -1999), ok1 = min(b.bc0 + b.bcols - 2000, 1999);
+        if (i1 < oi0 || i0 > oi1 || k1 < ok0 || k0 > ok1) return c_unit_partial[0];
+      }
     }
   }
   int n_one = 0;

@@ -74,7 +74,7 @@ __device__ __forceinline__ void dft16(float2 (&v)[16]) {
   v[9] = rot<INV>(v[9], R2, R2);     // 2
   v[13] = rot<INV>(v[13], S1, C1);   // 3
   v[6] = rot<INV>(v[6], R2, R2);     // 2
-  v[10] = rot<INV>(v[10], 0.0f, 1.0f);   // 4
+  v[10] = INV ? make_float2(-v[10].y, v[10].x) : make_float2(v[10].y, -v[10].x);   // times -+i   // 4
   v[14] = rot<INV>(v[14], -R2, R2);  // 6
   v[7] = rot<INV>(v[7], S1, C1);     // 3
   v[11] = rot<INV>(v[11], -R2, R2);  // 6
@@ -103,7 +103,7 @@ __device__ __forceinline__ void dft16_half_in(float2 (&v)[16]) {
   v[9] = rot<INV>(v[9], R2, R2);
   v[13] = rot<INV>(v[13], S1, C1);
   v[6] = rot<INV>(v[6], R2, R2);
-  v[10] = rot<INV>(v[10], 0.0f, 1.0f);
+  v[10] = INV ? make_float2(-v[10].y, v[10].x) : make_float2(v[10].y, -v[10].x);   // times -+i
   v[14] = rot<INV>(v[14], -R2, R2);
   v[7] = rot<INV>(v[7], S1, C1);
   v[11] = rot<INV>(v[11], -R2, R2);
@@ -572,13 +572,16 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(
     const int c = threadIdx.x & (R16_LINES - 1), j = threadIdx.x >> 4;
     float2* bl = b + c;
     {
-      // the S^ values this thread multiplies, copied to sm2 while the
-      // forward transform runs
-      const float2* sl = P.g.shat + off + c;
+      // S^ of the CTA's lines, copied to sm2 while the forward transform
+      // runs: two adjacent lines per 16-byte copy, element (i, c) at
+      // 16 i + (c ^ (i & 14)) (pairs stay adjacent; the reads below of 16
+      // lines at one row fall in 16 banks)
+      const float2* sh = P.g.shat + off;
 #pragma unroll
-      for (int q = 0; q < 16; ++q) {
-        const unsigned d = (unsigned)__cvta_generic_to_shared(sm2 + swz16<false>(j + 16 * q, c));
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(sl + (size_t)(j + 16 * q) * xs));
+      for (int q = 0; q < 8; ++q) {
+        const int e = threadIdx.x + q * SPEC_THREADS, i = e >> 3, cp = (e & 7) * 2;
+        const unsigned d = (unsigned)__cvta_generic_to_shared(sm2 + i * 16 + (cp ^ (i & 14)));
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(sh + (size_t)i * xs + cp));
       }
       asm volatile("cp.async.commit_group;\n" ::);
     }
@@ -589,9 +592,10 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(
       v[r] = (r < 8 && i < nx) ? __ldg(bl + (size_t)i * xs) : make_float2(0.0f, 0.0f);
     }
     r16_first<false, false>(v, true, sm, j, c);
-    __syncthreads();
-    r16_second<false, false>(sm, v, j, c, P.g.tw[0]);
     asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncthreads();   // stage 1 and every thread's S^ copies are in shared memory
+    r16_second<false, false>(sm, v, j, c, P.g.tw[0]);
+
     const float cs = P.g.conj ? -1.0f : 1.0f;
     float2 u[16];
 #pragma unroll
@@ -599,7 +603,8 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(
 #pragma unroll
       for (int k2 = 0; k2 < 4; ++k2) {
         const int q = k1 + 4 * k2;
-        const float2 s = sm2[swz16<false>(j + 16 * q, c)];
+        const int i = j + 16 * q;
+        const float2 s = sm2[i * 16 + (c ^ (i & 14))];
         u[q] = cmul(v[4 * k1 + k2], make_float2(s.x, cs * s.y));
       }
     __syncthreads();   // every read of sm (stage 2) and sm2 (S^) done
