@@ -197,10 +197,16 @@ __device__ __noinline__ double blocked_general(const BeamDev& b, const GridDev& 
   return acc;
 }
 
-// blocked fraction of one voxel; the 3x3x3 jaw case (values 0 and 1 only)
-// counts open samples and sums through the precomputed float64 partial sums
-__device__ double blocked_fraction(const BeamDev& b, const GridDev& g, int S, const float* pos, int& bad) {
-  if (S != 3 || b.geom_f32) return blocked_general(b, g, S, pos, bad);
+// Blocked fraction of one voxel where it is decided without classifying the
+// 3x3x3 samples one by one (returns false when they are needed): the general
+// sum (other sample counts, float32 source arrays), and for a uniform jaw
+// crop a voxel wholly inside or wholly outside the opening.
+__device__ __forceinline__ bool blocked_quick(const BeamDev& b, const GridDev& g, int S, const float* pos, int& bad,
+                                              double& out) {
+  if (S != 3 || b.geom_f32) {
+    out = blocked_general(b, g, S, pos, bad);
+    return true;
+  }
   float off[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) off[k] = fdiv(g.spacing[k], 3.0f);
@@ -239,17 +245,46 @@ __device__ double blocked_fraction(const BeamDev& b, const GridDev& g, int S, co
       const int i0 = floor_cell(umin - SAMPLE_DELTA), i1 = floor_cell(umax + SAMPLE_DELTA);
       const int k0 = floor_cell(wmin - SAMPLE_DELTA), k1 = floor_cell(wmax + SAMPLE_DELTA);
       if (i0 > -2000 && k0 > -2000) {
-        if (cell_value(b, i0, k0) == 1.0f && cell_value(b, i1, k1) == 1.0f) return c_unit_partial[27];
+        if (cell_value(b, i0, k0) == 1.0f && cell_value(b, i1, k1) == 1.0f) {
+          out = c_unit_partial[27];
+          return true;
+        }
         // Wholly closed: the box misses the open rectangle of cells
         // i in [br0 - 1999, br0 + brows - 2000], k likewise (within the map's
         // [-1999, 1999]; the wrapped index -2000 is outside the box), so
         // every sample reads 0 and blocked is the reference's sum of zeros.
         const int oi0 = max(b.br0 - 1999, -1999), oi1 = min(b.br0 + b.brows - 2000, 1999);
         const int ok0 = max(b.bc0 - 1999, -1999), ok1 = min(b.bc0 + b.bcols - 2000, 1999);
-        if (i1 < oi0 || i0 > oi1 || k1 < ok0 || k0 > ok1) return c_unit_partial[0];
+        if (i1 < oi0 || i0 > oi1 || k1 < ok0 || k0 > ok1) {
+          out = c_unit_partial[0];
+          return true;
+        }
       }
     }
   }
+  return false;
+}
+
+// sample sidx = 9 ix + 3 iy + iz of the 3x3x3 set: its float32 offset from
+// the voxel centre
+__device__ __forceinline__ float sample_of(const BeamDev& b, const GridDev& g, const float* pos, const float* off,
+                                           int sidx, int& bad) {
+  const int ix = sidx / 9, iy = (sidx / 3) % 3, iz = sidx % 3;
+  const float rx = off[0] * ((float)ix + 0.5f) - g.spacing[0] * 0.5f;
+  const float ry = off[1] * ((float)iy + 0.5f) - g.spacing[1] * 0.5f;
+  const float rz = off[2] * ((float)iz + 0.5f) - g.spacing[2] * 0.5f;
+  return sample_value(b, g, pos, off, rx, ry, rz, ix, iy, iz, bad);
+}
+
+// blocked fraction of one voxel; the 3x3x3 jaw case (values 0 and 1 only)
+// counts open samples and sums through the precomputed float64 partial sums
+// (the reference's float64 sum of n ones and 27 - n zeros, in any order)
+__device__ double blocked_fraction(const BeamDev& b, const GridDev& g, int S, const float* pos, int& bad) {
+  double quick;
+  if (blocked_quick(b, g, S, pos, bad, quick)) return quick;
+  float off[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) off[k] = fdiv(g.spacing[k], 3.0f);
   int n_one = 0;
   bool other = false;
   // a rolled loop: one copy of the sample code keeps the kernel inside the
@@ -257,16 +292,50 @@ __device__ double blocked_fraction(const BeamDev& b, const GridDev& g, int S, co
   // whose ambiguous samples are recomputed exactly from ix, iy, iz)
 #pragma unroll 1
   for (int sidx = 0; sidx < 27; ++sidx) {
-    const int ix = sidx / 9, iy = (sidx / 3) % 3, iz = sidx % 3;
-    const float rx = off[0] * ((float)ix + 0.5f) - g.spacing[0] * 0.5f;
-    const float ry = off[1] * ((float)iy + 0.5f) - g.spacing[1] * 0.5f;
-    const float rz = off[2] * ((float)iz + 0.5f) - g.spacing[2] * 0.5f;
-    const float v = sample_value(b, g, pos, off, rx, ry, rz, ix, iy, iz, bad);
+    const float v = sample_of(b, g, pos, off, sidx, bad);
     n_one += v == 1.0f ? 1 : 0;
     other |= v != 0.0f && v != 1.0f;
   }
   if (!other) return c_unit_partial[n_one];
   return blocked_general(b, g, 3, pos, bad);
+}
+
+// blocked_fraction for the voxels of a converged warp: the quick decisions
+// per lane, then, for each voxel that needs its samples classified, lanes
+// 0..26 classify one sample each (a warp's field-edge voxels cost one sample
+// time each instead of the whole warp running 27).  have: the lane holds a
+// voxel at pos.
+__device__ __forceinline__ double blocked_fraction_warp(const BeamDev& b, const GridDev& g, int S, bool have,
+                                                        const float* pos, int& bad) {
+  double out = 0.0;
+  const bool need = have && !blocked_quick(b, g, S, pos, bad, out);
+  unsigned m = __ballot_sync(0xffffffffu, need);
+  if (!m) return out;
+  const int lane = threadIdx.x & 31;
+  float off[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) off[k] = fdiv(g.spacing[k], 3.0f);
+  int n_one = 0;
+  bool other = false;
+  while (m) {
+    const int src = __ffs(m) - 1;
+    m &= m - 1;
+    float p[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) p[k] = __shfl_sync(0xffffffffu, pos[k], src);
+    int sbad = 0;
+    const float v = lane < 27 ? sample_of(b, g, p, off, lane, sbad) : 0.0f;
+    const unsigned ones = __ballot_sync(0xffffffffu, v == 1.0f);
+    const unsigned oth = __ballot_sync(0xffffffffu, v != 0.0f && v != 1.0f);
+    const unsigned bd = __ballot_sync(0xffffffffu, sbad != 0);
+    if (lane == src) {
+      n_one = __popc(ones);
+      other = oth != 0;
+      if (bd) bad = 1;
+    }
+  }
+  if (need) out = other ? blocked_general(b, g, 3, pos, bad) : c_unit_partial[n_one];
+  return out;
 }
 
 // ------------------------------------------------------------------ DDA --
@@ -451,19 +520,22 @@ __device__ __forceinline__ void terma_body(const float* __restrict__ rho, const 
   for (int it = 0; it < rounds; ++it) {
     const int e = (it * n_ctas + cta) * blockDim.x + threadIdx.x;
     const bool live = e < count;
-    int x = 0, y = 0, z = 0, bad = 0;
+    int x = 0, y = 0, z = 0, bad = 0, v = 0;
     float Tv = 0.0f;
+    float pos[3] = {0.0f, 0.0f, 0.0f};
     if (live) {
-      const int v = list_v[e];
+      v = list_v[e];
       z = v % g.n[2];
       const int r = v / g.n[2];
       y = r % g.n[1];
       x = r / g.n[1];
-      float pos[3];
       pos[0] = voxel_centre(g.origin[0], g.spacing[0], x);
       pos[1] = voxel_centre(g.origin[1], g.spacing[1], y);
       pos[2] = voxel_centre(g.origin[2], g.spacing[2], z);
-      const double blocked = blocked_fraction(b, g, s.samples, pos, bad);
+    }
+    // (every lane of the warp: the sample classification is shared)
+    const double blocked = blocked_fraction_warp(b, g, s.samples, live, pos, bad);
+    if (live) {
       if (inter.blocked) inter.blocked[v] = blocked;
       if (blocked == 0.0 && !all_voxels) {
         if (inter.terma) inter.terma[v] = 0.0f;
@@ -549,7 +621,7 @@ __global__ void __launch_bounds__(256) terma_kernel(const float* __restrict__ rh
   terma_body(rho, g, b, s, T, inter, all_voxels, list_count, list_v, aabb, flags, blockIdx.x, gridDim.x);
 }
 
-__global__ void __launch_bounds__(256) terma_batch_kernel(const PrologueBeam* __restrict__ recs,
+__global__ void __launch_bounds__(256, 3) terma_batch_kernel(const PrologueBeam* __restrict__ recs,
                                                           int* __restrict__ flags) {
   __shared__ PrologueBeam R;
   load_record(recs, R);
