@@ -9,8 +9,10 @@ fluence -> TERMA -> collapsed-cone dose (float32 dose and accumulation).
 
   value       beams/s with inputs resident in HBM (one batched call per
               step), L2 flushed (256 MiB write) between steps
-  e2e         beams/s through the C ABI with pinned host buffers: density and
-              block-map H2D plus dose D2H inside the timed region
+  e2e         beams/s through the C ABI with pinned host buffers: density
+              (and any block map that exists; a jaw field travels as its
+              rectangle in the beam record) H2D plus dose D2H inside the
+              timed region
   roofline    the cone stage of the schedule in use, from the library's stage
               events on the launching stream, against the measured HBM peak:
               spectral (default) = the five FFT passes, achieved = the bytes
@@ -436,7 +438,9 @@ def run_ours(args):
     B = args.beams
     total = (args.warmup + args.steps) * B
     beams = [make_beam(beam_seed(rank, i), args.field) for i in range(total)]
-    dblocks = [eng.upload_block(blk.block_values) for _, blk in beams]
+    # each beam's block through the public path: a jaw rectangle goes to the
+    # device as a rectangle (no map), anything else as its cropped map
+    dblocks = [eng.block_for(blk) for _, blk in beams]
     doses = [torch.empty(ph.size, dtype=torch.float32, device=dev) for _ in range(B)]
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     st = torch.cuda.current_stream(dev)
@@ -525,12 +529,15 @@ def run_ours(args):
     if rank == 0 or True:
         from conehead_gb300.engine import DeviceBlock
         h_rho = torch.from_numpy(np.ascontiguousarray(ph.densities)).pin_memory()
-        h_blocks = [torch.from_numpy(np.ascontiguousarray(db.crop.cpu().numpy())).pin_memory()
-                    for db in dblocks[:B]]
+        # block maps that exist (MLC or drawn maps) are inputs copied every
+        # step; a jaw rectangle travels in the beam record
+        crops = [i for i in range(B) if dblocks[i].crop is not None]
+        h_blocks = {i: torch.from_numpy(np.ascontiguousarray(dblocks[i].crop.cpu().numpy())).pin_memory()
+                    for i in crops}
         sets = 2
         h_doses = [[torch.empty(ph.size, dtype=torch.float32).pin_memory() for _ in range(B)] for _ in range(sets)]
         d_rho = [torch.empty_like(rho) for _ in range(sets)]
-        d_blocks = [[torch.empty_like(db.crop) for db in dblocks[:B]] for _ in range(sets)]
+        d_blocks = [{i: torch.empty_like(dblocks[i].crop) for i in crops} for _ in range(sets)]
         d_doses = [[torch.empty(ph.size, dtype=torch.float32, device=dev) for _ in range(B)] for _ in range(sets)]
         in_st, out_st = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
         computed, uploaded, copied = [None] * sets, [None] * sets, [None] * sets
@@ -538,7 +545,7 @@ def run_ours(args):
         # do not change between steps (the data they point at does): built once
         set_jobs = [[eng.job(ph, d_rho[k], beams[i][0],
                              DeviceBlock(d_blocks[k][i], dblocks[i].r0, dblocks[i].c0, dblocks[i].full_shape,
-                                         dblocks[i].uniform),
+                                         dblocks[i].uniform) if i in d_blocks[k] else dblocks[i],
                              SETTINGS, dose=d_doses[k][i]) for i in range(B)] for k in range(sets)]
 
         def upload(s):
@@ -547,7 +554,7 @@ def run_ours(args):
                 in_st.wait_event(computed[k])     # step s - 2 no longer reads set k's inputs
             with torch.cuda.stream(in_st):
                 d_rho[k].copy_(h_rho, non_blocking=True)
-                for i in range(B):
+                for i in crops:
                     d_blocks[k][i].copy_(h_blocks[i], non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(in_st)
@@ -593,7 +600,7 @@ def run_ours(args):
         e1.synchronize()
         eng.sync()
         e2e_s = max_over_ranks(e0.elapsed_time(e1) / 1000.0, dev)
-        h2d = h_rho.numel() * 4 + sum(h.numel() * 4 for h in h_blocks)
+        h2d = h_rho.numel() * 4 + sum(h.numel() * 4 for h in h_blocks.values())
         e2e = {"value": world * args.steps * B / e2e_s, "unit": "beams/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(B * N * 4),
                "pipelined": "two buffer sets, copy-in / compute / copy-out streams: step s+1's inputs and "
