@@ -1177,7 +1177,9 @@ ch_status enqueue_batch(ch_plan* P, const BatchPlan& B, const Scratch& S, const 
       max_vox = std::max(max_vox, (long long)J.g.n[0] * J.g.n[1] * J.g.n[2]);
       max_lines = std::max(max_lines, (long long)J.g.n[0] * J.g.n[1]);
     }
-    launch_prologue_batch(S.pro, n, max_vox, max_lines, P->n_sm, flags, s, P->tuning.terma_ctas_per_sm);
+    // counters[4]: the TERMA chunk counter (zeroed by launch_init_scratch)
+    launch_prologue_batch(S.pro, n, max_vox, max_lines, P->n_sm, flags, S.counters + 4, s,
+                          P->tuning.terma_ctas_per_sm);
     CH_CUDA(cudaGetLastError());
   }
   if (ev) CH_CUDA(cudaEventRecord(ev[1], s));

@@ -286,8 +286,9 @@ struct PrologueBeam {
 
 // ------------------------------------------------------------ launchers --
 void upload_unit_partials();
+// work: a zeroed int, the TERMA launch's chunk counter
 void launch_prologue_batch(const PrologueBeam* recs, int n_beams, long long max_voxels, long long max_lines,
-                           int n_sm, int* flags, cudaStream_t st, int ctas_per_sm);
+                           int n_sm, int* flags, int* work, cudaStream_t st, int ctas_per_sm);
 void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const SettingsDev& s, float* T,
                      const Inter& inter, int all_voxels, int* aabb, int* list_v, int n_sm, int* flags,
                      cudaStream_t st, int ctas_per_sm = 8);

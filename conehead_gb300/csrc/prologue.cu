@@ -405,6 +405,41 @@ __device__ float radiological_depth(const float* __restrict__ rho, const GridDev
 }
 
 // ------------------------------------------------------------ kernels --
+// Whole-line rejection for the cull.  Along an (x, y) line the voxel centres
+// lie on one segment.  While the depth stays positive, the projected
+// coordinates xb(z), zb(z) and the lateral ratio are ratios of linear
+// functions of z without a pole, hence monotone: their ranges over the line
+// are spanned by the two end voxels, and 1/depth and the lateral ratio (and
+// so the per-voxel margin) are bounded by their largest end values.  Depth
+// is linear, so its minimum is at an end too.  True only when no voxel of
+// the line can pass the per-voxel test below; 0.01 cm on top of the margin
+// covers the float32 rounding of both tests (about 1e-5 cm here).
+__device__ __forceinline__ bool line_outside(const GridDev& g, const BeamDev& b, float px, float py) {
+  float xlo = INFINITY, xhi = -INFINITY, zlo = INFINITY, zhi = -INFINITY, inv_max = 0.0f, lat_max = 0.0f;
+  const float kk = fabsf(b.a_K);
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    const float pz = voxel_centre(g.origin[2], g.spacing[2], e ? g.n[2] - 1 : 0);
+    const float np_ = b.vyf[0] * px + b.vyf[1] * py + b.vyf[2] * pz;
+    const float m0p = b.m0f[0] * px + b.m0f[1] * py + b.m0f[2] * pz;
+    const float m2p = b.m2f[0] * px + b.m2f[1] * py + b.m2f[2] * pz;
+    const float depth = np_ - b.a_nS;
+    if (!(depth > 0.2f * kk)) return false;   // near or behind the source plane: test per voxel
+    const float inv = 1.0f / depth;
+    const float si = -b.a_K * inv;
+    const float xb = b.a_c0 + si * (b.a_m0S - m0p);
+    const float zb = b.a_c2 + si * (b.a_m2S - m2p);
+    xlo = fminf(xlo, xb);
+    xhi = fmaxf(xhi, xb);
+    zlo = fminf(zlo, zb);
+    zhi = fmaxf(zhi, zb);
+    inv_max = fmaxf(inv_max, inv);
+    lat_max = fmaxf(lat_max, fmaxf(fabsf(b.a_m0S - m0p), fabsf(b.a_m2S - m2p)) * inv);
+  }
+  const float M = b.cull_margin_k * kk * inv_max * (1.0f + lat_max) + 0.02f;
+  return xhi < b.cx_lo - M || xlo > b.cx_hi + M || zhi < b.cz_lo - M || zlo > b.cz_hi + M;
+}
+
 // Pass 1, every voxel: zero TERMA and keep the voxels the beam may reach
 // (all voxels when intermediates are requested) on a compact list, so the
 // blocking/depth/TERMA pass runs on full warps.
@@ -423,6 +458,16 @@ __device__ __forceinline__ void cull_line(const GridDev& g, const BeamDev& b, fl
   const float px = voxel_centre(g.origin[0], g.spacing[0], x);
   const float py = voxel_centre(g.origin[1], g.spacing[1], y);
   float* Tl = T + ((size_t)x * g.n[1] + y) * g.zp;
+  // a line the beam cannot reach lists nothing (intermediates of every voxel
+  // are written by the per-voxel loop, so it runs whenever they are asked)
+  const bool no_inter = !inter.blocked && !inter.d_eff && !inter.oad && !inter.fluence && !inter.f_soften &&
+                        !inter.f_horn && !inter.terma;
+  if (b.cull_enable && !all_voxels && no_inter && line_outside(g, b, px, py)) {
+    if (zero_all)
+      for (int z = lane; z < g.n[2]; z += 32) Tl[z] = 0.0f;
+    if (line_any && lane == 0) line_any[line] = 0;
+    return;
+  }
   bool any = false;
   for (int z0 = 0; z0 < g.n[2]; z0 += 32) {
     const int z = z0 + lane;
@@ -508,17 +553,13 @@ __global__ void __launch_bounds__(256) cull_batch_kernel(const PrologueBeam* __r
 // fully blocked, or for every voxel when intermediates are requested)
 // radiological depth, oad, fluence, softening/horn and TERMA; TERMA support
 // box for the cone stage.
-// The listed voxels of one beam, taken by n_ctas CTAs (this one is cta) in
-// rounds of n_ctas * blockDim.x.
-__device__ __forceinline__ void terma_body(const float* __restrict__ rho, const GridDev& g, const BeamDev& b,
-                                           const SettingsDev& s, float* __restrict__ T, const Inter& inter,
-                                           int all_voxels, const int* __restrict__ list_count,
-                                           const int* __restrict__ list_v, int* __restrict__ aabb,
-                                           int* __restrict__ flags, int cta, int n_ctas) {
-  const int count = *list_count;
-  const int rounds = (count + blockDim.x * n_ctas - 1) / (blockDim.x * n_ctas);
-  for (int it = 0; it < rounds; ++it) {
-    const int e = (it * n_ctas + cta) * blockDim.x + threadIdx.x;
+// Entry e of a beam's list of count voxels; every lane of the warp calls it
+// (the blocking classification and the box reduction are warp-wide).
+__device__ __forceinline__ void terma_entry(const float* __restrict__ rho, const GridDev& g, const BeamDev& b,
+                                            const SettingsDev& s, float* __restrict__ T, const Inter& inter,
+                                            int all_voxels, int count, int e, const int* __restrict__ list_v,
+                                            int* __restrict__ aabb, int* __restrict__ flags) {
+  {
     const bool live = e < count;
     int x = 0, y = 0, z = 0, bad = 0, v = 0;
     float Tv = 0.0f;
@@ -613,6 +654,20 @@ __device__ __forceinline__ void terma_body(const float* __restrict__ rho, const 
   }
 }
 
+// The listed voxels of one beam, taken by n_ctas CTAs (this one is cta) in
+// rounds of n_ctas * blockDim.x.
+__device__ __forceinline__ void terma_body(const float* __restrict__ rho, const GridDev& g, const BeamDev& b,
+                                           const SettingsDev& s, float* __restrict__ T, const Inter& inter,
+                                           int all_voxels, const int* __restrict__ list_count,
+                                           const int* __restrict__ list_v, int* __restrict__ aabb,
+                                           int* __restrict__ flags, int cta, int n_ctas) {
+  const int count = *list_count;
+  const int rounds = (count + blockDim.x * n_ctas - 1) / (blockDim.x * n_ctas);
+  for (int it = 0; it < rounds; ++it)
+    terma_entry(rho, g, b, s, T, inter, all_voxels, count, (it * n_ctas + cta) * blockDim.x + threadIdx.x,
+                list_v, aabb, flags);
+}
+
 __global__ void __launch_bounds__(256) terma_kernel(const float* __restrict__ rho, GridDev g, BeamDev b,
                                                     SettingsDev s, float* __restrict__ T, Inter inter,
                                                     int all_voxels, const int* __restrict__ list_count,
@@ -621,11 +676,47 @@ __global__ void __launch_bounds__(256) terma_kernel(const float* __restrict__ rh
   terma_body(rho, g, b, s, T, inter, all_voxels, list_count, list_v, aabb, flags, blockIdx.x, gridDim.x);
 }
 
-__global__ void __launch_bounds__(256, 3) terma_batch_kernel(const PrologueBeam* __restrict__ recs,
-                                                          int* __restrict__ flags) {
-  __shared__ PrologueBeam R;
-  load_record(recs, R);
-  terma_body(R.rho, R.g, R.b, R.s, R.T, Inter{}, 0, R.aabb + 6, R.list_v, R.aabb, flags, blockIdx.x, gridDim.x);
+// Every beam's listed voxels in one launch, in chunks of 32 (one per lane)
+// that warps claim from one counter: chunk c is entry range [32 c', 32 c' +
+// 32) of the beam whose chunks cover c in beam order.  A warp that finishes
+// early takes the next chunk of any beam, so the SMs end together however
+// unequal the beams' lists and ray lengths are (a static share per CTA left
+// the SMs idle for a sixth of the launch).  Each warp keeps the record of
+// its current beam in its own shared slot and copies the next one when the
+// claimed chunk moves on to another beam; the claims of one warp increase,
+// so the beam search walks forward only.
+constexpr int TERMA_WARPS = 8;   // 256 threads
+
+__global__ void __launch_bounds__(256, 3) terma_batch_kernel(const PrologueBeam* __restrict__ recs, int n_beams,
+                                                          int* __restrict__ flags, int* __restrict__ work) {
+  __shared__ PrologueBeam Rw[TERMA_WARPS];
+  static_assert(sizeof(PrologueBeam) % 4 == 0, "record copy");
+  const int lane = threadIdx.x & 31;
+  PrologueBeam& R = Rw[threadIdx.x >> 5];
+  int cur = -1, beam = 0, base = 0, count = 0;
+  for (;;) {
+    int c = 0;
+    if (lane == 0) c = atomicAdd(work, 1);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    // chunks of beam b: ceil(list count / 32); the counts were written by the cull launch
+    while (beam < n_beams) {
+      count = recs[beam].aabb[6];
+      const int chunks = (count + 31) >> 5;
+      if (c < base + chunks) break;
+      base += chunks;
+      ++beam;
+    }
+    if (beam >= n_beams) break;   // whole warp
+    if (beam != cur) {
+      __syncwarp();
+      const int* src = reinterpret_cast<const int*>(recs + beam);
+      int* dst = reinterpret_cast<int*>(&R);
+      for (int i = lane; i < (int)(sizeof(PrologueBeam) / 4); i += 32) dst[i] = __ldg(src + i);
+      __syncwarp();
+      cur = beam;
+    }
+    terma_entry(R.rho, R.g, R.b, R.s, R.T, Inter{}, 0, count, ((c - base) << 5) + lane, R.list_v, R.aabb, flags);
+  }
 }
 
 // ----------------------------------------------------- beamlet adjoint --
@@ -766,12 +857,14 @@ void launch_prologue(const float* rho, const GridDev& g, const BeamDev& b, const
 // and one TERMA launch in which each beam's list is shared by the same number
 // of CTAs, so all beams run together and no beam leaves a tail.
 void launch_prologue_batch(const PrologueBeam* recs, int n_beams, long long max_voxels, long long max_lines,
-                           int n_sm, int* flags, cudaStream_t st, int ctas_per_sm) {
+                           int n_sm, int* flags, int* work, cudaStream_t st, int ctas_per_sm) {
   const int threads = 256;
   cull_batch_kernel<<<dim3((unsigned)((max_lines + 7) / 8), n_beams), threads, 0, st>>>(recs);
-  const long long per_beam = std::max(1ll, ((long long)n_sm * ctas_per_sm + n_beams - 1) / n_beams);
-  const long long want = (max_voxels + threads - 1) / threads;
-  terma_batch_kernel<<<dim3((unsigned)std::min(per_beam, want), n_beams), threads, 0, st>>>(recs, flags);
+  // persistent: at most the resident CTAs (3 per SM at 80 registers), fewer
+  // for small batches; the warps share all beams' chunks
+  const long long want = ((long long)n_beams * max_voxels + threads - 1) / threads;
+  const long long cap = (long long)n_sm * std::min(ctas_per_sm, 3);
+  terma_batch_kernel<<<(unsigned)std::max(1ll, std::min(cap, want)), threads, 0, st>>>(recs, n_beams, flags, work);
 }
 
 __global__ void init_scratch_kernel(int* aabb, int n_beams, int* counters) {

@@ -300,7 +300,9 @@ ch_status ch_cone_directions(ch_plan* plan, float* out_dev, void* stream);
  * dir_group: unique directions per gather work unit, 1..1024 (default 16);
  * unit_order: 0 = a tile's direction groups are consecutive gather units
  * (default), 1 = a direction group's tiles are;
- * terma_ctas_per_sm: CTAs per SM of the TERMA pass, 1..32 (default 8).
+ * terma_ctas_per_sm: CTAs per SM of the TERMA pass, 1..32 (default 8); the
+ * batched pass is persistent and holds at most 3 CTAs per SM (its register
+ * budget), so values above 3 only change the single-beam pass.
  * Picked per workload by conehead_gb300.autotune. */
 #define CH_CONE_SPECTRAL 0
 #define CH_CONE_GATHER 1
