@@ -422,24 +422,25 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward
   const int l0 = blockIdx.x * L;
   // lines of each beam that may hold TERMA (the others are zero and are not
   // read); a block without any transforms to zero
+  // (both flags fetched together; one barrier publishes them and tells
+  // whether the block holds any)
   __shared__ unsigned char zf[2][SPEC_ELEMS / SPEC_MIN_PERIOD];
-  __shared__ int zany;
-  if (threadIdx.x == 0) zany = 0;
-  __syncthreads();
+  bool mine = false;
   for (int c = threadIdx.x; c < L; c += SPEC_THREADS) {
-    const int l = l0 + c;
-    const bool f1 = l < nl && (!pr.l1 || pr.l1[l]);
-    const bool f2 = l < nl && pr.t2 && (!pr.l2 || pr.l2[l]);
+    const int l = l0 + c, lc = l < nl ? l : nl - 1;
+    const unsigned a1 = pr.l1 ? (unsigned)__ldg(pr.l1 + lc) : 1u;
+    const unsigned a2 = (pr.t2 && pr.l2) ? (unsigned)__ldg(pr.l2 + lc) : 1u;
+    const bool f1 = l < nl && a1 != 0u;
+    const bool f2 = l < nl && pr.t2 && a2 != 0u;
     zf[0][c] = f1;
     zf[1][c] = f2;
-    if (f1 || f2) zany = 1;
+    mine = mine || f1 || f2;
   }
-  __syncthreads();
-  if (!zany) {
-    for (int e = threadIdx.x; e < L * Mz; e += SPEC_THREADS) {
-      const int c = e / Mz, i = e - c * Mz, l = l0 + c;
-      if (l < nl) pr.a[(size_t)l * Mz + i] = make_float2(0.0f, 0.0f);
-    }
+  if (!__syncthreads_or(mine)) {
+    // L Mz float2 of consecutive lines, 16 bytes per store (Mz is even)
+    float4* a4 = reinterpret_cast<float4*>(pr.a + (size_t)l0 * Mz);
+    const int lines = min(L, nl - l0);
+    for (int e = threadIdx.x; e < lines * Mz / 2; e += SPEC_THREADS) a4[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     return;
   }
   if constexpr (MP == 256 && LL == 4) {
