@@ -1,6 +1,7 @@
 """Benchmark: beams/s of the collapsed-cone dose engine on GB300.
 
-Workload (one "step"): a batch of --beams beams on the heterogeneous 128^3
+Workload (one "step"): a batch of --beams beams (default 32: one cull, one
+TERMA and one spectral launch of 16 beam pairs) on the heterogeneous 128^3
 slab phantom (0.25 cm voxels: water, lung slab 0.25 g/cc at depth 5-12 cm,
 bone slab 1.85 g/cc at 14-16 cm, 20 random cuboid inserts of 0.2-2.0
 g/cc), 5 x 5 cm^2 jaw field, gantry uniform in [0, 360), seeded synthetic
@@ -691,7 +692,7 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--beams", type=int, default=16, help="beams per step")
+    ap.add_argument("--beams", type=int, default=32, help="beams per step")
     ap.add_argument("--grid", type=int, default=128)
     ap.add_argument("--spacing", type=float, default=0.25)
     ap.add_argument("--field", type=float, default=5.0)

@@ -232,7 +232,7 @@ constexpr int SPEC_THREADS = 256;
 constexpr int SPEC_CTAS_PER_SM = 3;       // register budget of the passes (85 per thread)
 constexpr int SPEC_ELEMS = 4096;          // complex values per CTA: 4096 / M lines of period M
 constexpr int SPEC_MIN_PERIOD = 16, SPEC_MAX_PERIOD = 4096;
-constexpr int SPEC_MAX_PAIRS = 8;         // beam pairs per launch (their work buffers coexist)
+constexpr int SPEC_MAX_PAIRS = 16;        // beam pairs per launch (their work buffers coexist)
 constexpr int SPEC_SMEM = 2 * SPEC_ELEMS * 8;   // two ping-pong buffers of float2 per CTA
 struct SpecPair {
   const float* t1;   // TERMA of the first beam [nx][ny][zp]
