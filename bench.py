@@ -391,11 +391,15 @@ def spectral_period(n):
     return next(m for m in periods if m >= 2 * n - 1)
 
 
-def spectral_launches(beams, max_pairs=8):
+# beam pairs per spectral launch (SPEC_MAX_PAIRS of the library)
+SPEC_MAX_PAIRS = 16
+
+
+def spectral_launches(beams, max_pairs=SPEC_MAX_PAIRS):
     return ((beams + 1) // 2 + max_pairs - 1) // max_pairs
 
 
-def spectral_bytes(size, beams, max_pairs=8):
+def spectral_bytes(size, beams, max_pairs=SPEC_MAX_PAIRS):
     """HBM bytes the five FFT passes must move for `beams` beams of one grid:
     per pair of beams the two TERMA volumes in and two doses out (16 N), the
     intermediates A [nx][ny][Mz] and B [nx][My][Mz] (complex float32) each
@@ -490,10 +494,12 @@ def run_ours(args):
     method = "spectral" if int(eng.get_tuning().get("cone_method", 0)) == 0 else "gather"
     if method == "spectral":
         alg_bytes = spectral_bytes(ph.size, B)
-        launches_per_step = 1 + 2 * B + 5 * spectral_launches(B)
+        # scratch reset, cull, TERMA (every beam in one launch each), then
+        # five passes per spectral launch
+        launches_per_step = 3 + 5 * spectral_launches(B)
     else:
         alg_bytes = B * 2 * 4 * N                 # TERMA read + dose write per beam
-        launches_per_step = 2 * B + 3
+        launches_per_step = 5                     # reset, cull, TERMA, tap ranges, gather
     peaks = {}
     pk_path = os.path.join(HERE, "MEASURED_PEAKS.json")
     if os.path.exists(pk_path):
