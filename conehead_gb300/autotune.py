@@ -14,7 +14,9 @@ Knobs (see include/conehead_gb300.h):
   dir_group          unique directions per gather work unit (16, 32, 64)
   unit_order         0 = a tile's direction groups run back to back,
                      1 = a direction group's tiles do
-  terma_ctas_per_sm  CTAs per SM of the TERMA pass (4, 8, 16)
+  terma_ctas_per_sm  CTAs per SM of the TERMA pass (2, 3; the batched pass is
+                     persistent and holds at most 3 per SM, its register
+                     budget, so larger values run as 3)
 """
 import json
 import os
@@ -28,9 +30,9 @@ DEFAULT = {"dir_group": 16, "unit_order": 0, "terma_ctas_per_sm": 8, "cone_metho
 # the float32-mirrored oracle at 64^3 the error grows from 5e-7 of Dmax (16
 # or 32 directions) and 9e-7 (64) to 1.6e-6 (128) and 9e-6 (1024).  The tuner
 # stays at 64 or below, where the precision is unchanged.
-CANDIDATES = ([{"dir_group": 16, "unit_order": 0, "terma_ctas_per_sm": t, "cone_method": 0} for t in (4, 8, 16)] +
+CANDIDATES = ([{"dir_group": 16, "unit_order": 0, "terma_ctas_per_sm": t, "cone_method": 0} for t in (2, 3)] +
               [{"dir_group": g, "unit_order": o, "terma_ctas_per_sm": t, "cone_method": 1}
-               for g in (16, 32, 64) for o in (0, 1) for t in (4, 8, 16)])
+               for g in (16, 32, 64) for o in (0, 1) for t in (2, 3)])
 
 
 def cache_path():

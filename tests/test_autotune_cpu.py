@@ -36,7 +36,7 @@ def test_autotune_picks_the_fastest_and_caches(tmp_path):
     jobs = _jobs([64, 96, 128, 160] * 16)
     r = autotune(eng, jobs, path=path, timer=timer, device_name="GB300")
     assert not r["cached"] and eng.calls == len(CANDIDATES)
-    assert r["tuning"] == {"dir_group": 32, "unit_order": 0, "terma_ctas_per_sm": 4, "cone_method": 1} == eng.tuning
+    assert r["tuning"] == {"dir_group": 32, "unit_order": 0, "terma_ctas_per_sm": 3, "cone_method": 1} == eng.tuning
     eng2 = FakeEngine()
     r2 = autotune(eng2, _jobs([160, 128, 96, 64] * 16), path=path, timer=timer, device_name="GB300")
     assert r2["cached"] and eng2.calls == 0 and eng2.tuning == r["tuning"]
