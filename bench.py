@@ -190,13 +190,14 @@ def run_reference(args):
         oracle.calculate(src, blk, ph, SETTINGS, oracle.MODE_F64)
     v, cores, dt = cpu_oracle_beams(ph, beams[args.warmup:])
     sample = (f"{args.steps} whole beams ({args.grid}^3, {args.field:g}x{args.field:g} cm, "
-              f"random gantry), FP64 oracle, OpenMP")
+              f"random gantry), one per step: a bounded sample of the {args.beams}-beam step; FP64 oracle, "
+              f"OpenMP")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": "beams/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": config(args, beams_per_step=1),
+        "config": config(args),
         "cpu_baseline": {"value": v, "unit": "beams/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "beams/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
