@@ -645,7 +645,8 @@ ch_status check_settings(const ch_settings* s) {
 }
 
 // ------------------------------------------------------ beam prep --
-BeamDev make_beam(const ch_beam& in, const ch_grid& g) {
+// samples: sub-samples per axis of the blocking test (fluenceResampling)
+BeamDev make_beam(const ch_beam& in, const ch_grid& g, int samples) {
   BeamDev b{};
   for (int k = 0; k < 3; ++k) {
     b.src[k] = in.src[k];
@@ -684,7 +685,12 @@ BeamDev make_beam(const ch_beam& in, const ch_grid& g) {
   b.cz_lo = (float)std::max(zlo, -20.0);
   b.cz_hi = (float)std::min(zhi, 20.0);
   const float smax = std::max(g.spacing[0], std::max(g.spacing[1], g.spacing[2]));
-  b.cull_margin_k = 1.25f * 0.8660254f * smax;
+  // The sub-samples of a voxel sit at s (2 i + 1 - S) / (2 S) from its
+  // centre per axis, so the farthest lies sqrt(3) smax (S - 1) / (2 S) away;
+  // a lateral offset r at depth d moves the projection by at most
+  // |K| r / (d - r) (1 + lateral ratio), and 1.25 covers d / (d - r) (the
+  // cull tests depths above 0.2 |K|, far beyond r).
+  b.cull_margin_k = (float)(1.25 * std::sqrt(3.0) * (double)smax * (double)(samples - 1) / (2.0 * samples));
   b.cull_enable = (-nS > 0.0 && b.cx_lo <= b.cx_hi && b.cz_lo <= b.cz_hi) ? 1 : 0;
   b.block = in.block;
   b.brows = in.block_rows;
@@ -1044,7 +1050,7 @@ ch_status plan_batch(ch_plan* P, int n, const ch_grid* grids, const float* const
     }
     J.g.zp = round_up(grids[i].n[2], 4);
     J.g.swap_xy = swap_xy ? swap_xy[i] : 0;
-    J.b = make_beam(beams[i], grids[i]);
+    J.b = make_beam(beams[i], grids[i], settings[i].samples);
     J.s = make_settings(settings[i]);
     J.rho = rho[i];
     J.dose = dose[i];
@@ -1515,7 +1521,7 @@ ch_status ch_dose_static(ch_plan* P, const ch_grid* grid, const float* rho, int 
   int* flags = counters + 1;
   unsigned long long* updates = reinterpret_cast<unsigned long long*>(counters + 2);
 
-  const BeamDev b = make_beam(*beam, *grid);
+  const BeamDev b = make_beam(*beam, *grid, settings->samples);
   const SettingsDev sd = make_settings(*settings);
   // aabb and the list count must start from their reset values; TERMA is
   // rewritten in full by the prologue and the range tables by range_kernel
@@ -1757,7 +1763,7 @@ ch_status ch_dose_adjoint(ch_plan* P, const ch_grid* grid, const float* rho, int
   int* box = P->aabb.as<int>();          // [0..7] TERMA box + list count, [8..15] input box
   int* counters = P->counters.as<int>();
   int* flags = counters + 1;
-  const BeamDev b = make_beam(*beam, *grid);
+  const BeamDev b = make_beam(*beam, *grid, settings->samples);
   const SettingsDev sd = make_settings(*settings);
   launch_init_scratch(box, 2, counters, s);
   // forward prologue: TERMA, its box and the list of voxels the beam reaches

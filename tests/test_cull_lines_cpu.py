@@ -13,7 +13,10 @@ library derives (``make_beam_dev`` in conehead_gb300/csrc/capi.cu) and
 checks, on seeded grids, beams (gantry, collimator, asymmetric jaws) and
 grids that reach close to the source plane, that no rejected line holds a
 voxel the per-voxel test keeps, and that the rejection does take out most
-lines of a small field.
+lines of a small field.  It also checks the per-voxel margin itself: a
+voxel any of whose S^3 blocking sub-samples projects into the jaw opening
+is always kept (the margin is the farthest sub-sample's offset,
+sqrt(3) s_max (S - 1) / (2 S), magnified to the blocking plane).
 """
 import numpy as np
 import pytest
@@ -23,10 +26,11 @@ from conehead_gb300.source import Source
 F = np.float32
 
 
-def beam_consts(src, jaws, spacing):
+def beam_consts(src, jaws, spacing, samples=3):
     """Cull constants of one beam, as the library computes them in float64
     and stores in float32.  jaws = (xlo, xhi, zlo, zhi) in cm at the
-    blocking plane (already clipped to the 40 cm map)."""
+    blocking plane (already clipped to the 40 cm map); samples = sub-samples
+    per axis of the blocking test (fluenceResampling)."""
     pos = np.asarray(src.position, dtype=np.float64)
     vy = np.asarray(src.v_y, dtype=np.float64)
     T = np.asarray(src.transform, dtype=np.float64)
@@ -39,7 +43,7 @@ def beam_consts(src, jaws, spacing):
         a_nS=F(nS), a_m0S=F(m0 @ pos), a_m2S=F(m2 @ pos), a_K=F(-vyw),
         a_c0=F(m0 @ w), a_c2=F(m2 @ w),
         cx_lo=F(jaws[0]), cx_hi=F(jaws[1]), cz_lo=F(jaws[2]), cz_hi=F(jaws[3]),
-        k=F(F(1.25) * F(0.8660254) * F(max(spacing))),
+        k=F(1.25 * np.sqrt(3.0) * max(spacing) * (samples - 1) / (2.0 * samples)),
         enable=(-nS > 0.0 and jaws[0] <= jaws[1] and jaws[2] <= jaws[3]),
     )
     return c
@@ -142,3 +146,51 @@ def test_small_field_rejects_most_lines(gantry):
     assert rej.mean() > 0.6, rej.mean()
     # lines the test keeps but that hold no candidate: the price of the bound
     assert (~rej & ~any_cand).mean() < 0.1
+
+
+@pytest.mark.parametrize("samples", [1, 2, 3, 5])
+def test_margin_keeps_every_voxel_with_an_open_sample(samples):
+    rng = np.random.default_rng(20 + samples)
+    n_needed = n_kept = 0
+    for case in range(12):
+        n = tuple(int(v) for v in rng.integers(16, 40, 3))
+        spacing = np.array(rng.uniform(0.15, 0.6, 3))
+        ext = np.array(n) * spacing
+        src = Source()
+        src.gantry = float(rng.uniform(0, 360))
+        src.collimator = float(rng.uniform(0, 90))
+        centre = rng.uniform(-3, 3, 3)
+        if case % 4 == 3:
+            # on the beam axis 25-40 cm from the source: depths from below
+            # 0.2 SAD (always kept) up, magnifications up to 5
+            centre = np.asarray(src.position, float) + np.asarray(src.v_y, float) * rng.uniform(25, 40)
+        origin = centre - ext / 2
+        h = rng.uniform(0.2, 6, 2)
+        off = rng.uniform(-2, 2, 2)
+        jaws = (round(off[0] - h[0], 2), round(off[0] + h[0], 2), round(off[1] - h[1], 2), round(off[1] + h[1], 2))
+        c = beam_consts(src, jaws, tuple(spacing), samples)
+        # voxel centres (float32 as the kernels hold them)
+        idx = np.stack(np.meshgrid(*[np.arange(k) for k in n], indexing="ij"), -1).reshape(-1, 3)
+        cen = (origin[None, :].astype(F) + spacing[None, :].astype(F) * idx.astype(F)).astype(F)
+        keep = voxel_candidates(c, cen[:, 0], cen[:, 1], cen[:, 2])
+        # every sub-sample, projected in float64 through the source onto the
+        # blocking plane (v_y . (p - S) = -v_y . S, i.e. the isocentre plane)
+        S_ = np.asarray(src.position, dtype=np.float64)
+        vy = np.asarray(src.v_y, dtype=np.float64)
+        T = np.asarray(src.transform, dtype=np.float64)
+        o = (2 * np.arange(samples) + 1 - samples) / (2.0 * samples)
+        offs = np.stack(np.meshgrid(o, o, o, indexing="ij"), -1).reshape(-1, 3) * spacing[None, :]
+        pts = cen.astype(np.float64)[:, None, :] + offs[None, :, :]
+        r = pts - S_
+        si = -(vy @ S_) / (r @ vy)
+        hit = S_ + si[..., None] * r
+        xb, zb = hit @ T[0], hit @ T[2]
+        front = (r @ vy) > 0
+        open_ = front & (xb >= jaws[0]) & (xb < jaws[1]) & (zb >= jaws[2]) & (zb < jaws[3])
+        needed = open_.any(axis=1)
+        missed = needed & ~keep
+        assert not missed.any(), (samples, case, int(missed.sum()))
+        n_needed += int(needed.sum())
+        n_kept += int(keep.sum())
+    # the check saw voxels at the field edges, and the margin is not vacuous
+    assert 0 < n_needed <= n_kept
