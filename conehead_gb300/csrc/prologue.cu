@@ -677,8 +677,9 @@ __global__ void __launch_bounds__(256) terma_kernel(const float* __restrict__ rh
 }
 
 // Every beam's listed voxels in one launch, in chunks of 32 (one per lane)
-// that warps claim from one counter: chunk c is entry range [32 c', 32 c' +
-// 32) of the beam whose chunks cover c in beam order.  A warp that finishes
+// that warps claim from one counter: claim c is chunk c - base of the beam
+// whose chunks cover c, where base counts the chunks of the beams before it
+// (entries 32 (c - base) .. 32 (c - base) + 31 of its list).  A warp that finishes
 // early takes the next chunk of any beam, so the SMs end together however
 // unequal the beams' lists and ray lengths are (a static share per CTA left
 // the SMs idle for a sixth of the launch).  Each warp keeps the record of
