@@ -686,12 +686,17 @@ BeamDev make_beam(const ch_beam& in, const ch_grid& g, int samples) {
   b.cz_hi = (float)std::min(zhi, 20.0);
   const float smax = std::max(g.spacing[0], std::max(g.spacing[1], g.spacing[2]));
   // The sub-samples of a voxel sit at s (2 i + 1 - S) / (2 S) from its
-  // centre per axis, so the farthest lies sqrt(3) smax (S - 1) / (2 S) away;
-  // a lateral offset r at depth d moves the projection by at most
-  // |K| r / (d - r) (1 + lateral ratio), and 1.25 covers d / (d - r) (the
-  // cull tests depths above 0.2 |K|, far beyond r).
-  b.cull_margin_k = (float)(1.25 * std::sqrt(3.0) * (double)smax * (double)(samples - 1) / (2.0 * samples));
-  b.cull_enable = (-nS > 0.0 && b.cx_lo <= b.cx_hi && b.cz_lo <= b.cz_hi) ? 1 : 0;
+  // centre per axis, so the farthest lies r = sqrt(3) smax (S - 1) / (2 S)
+  // away.  An offset r at depth d moves the projection by at most
+  // |K| r / (d - r) (1 + lateral ratio at the centre), and the cull tests
+  // centres deeper than dmin = 0.2 |K| (nearer ones are always kept), so
+  // k = r / (1 - r / dmin) bounds r d / (d - r); the margin's 0.01 cm
+  // covers float32 rounding.  Voxels a tenth of dmin across or larger
+  // (never in practice) are not culled.
+  const double r_s = std::sqrt(3.0) * (double)smax * (double)(samples - 1) / (2.0 * samples);
+  const double dmin = 0.2 * std::fabs((double)b.a_K);
+  b.cull_margin_k = r_s < 0.1 * dmin ? (float)(r_s / (1.0 - r_s / dmin)) : 0.0f;
+  b.cull_enable = (-nS > 0.0 && b.cx_lo <= b.cx_hi && b.cz_lo <= b.cz_hi && r_s < 0.1 * dmin) ? 1 : 0;
   b.block = in.block;
   b.brows = in.block_rows;
   b.bcols = in.block_cols;

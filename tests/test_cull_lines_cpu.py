@@ -16,7 +16,9 @@ voxel the per-voxel test keeps, and that the rejection does take out most
 lines of a small field.  It also checks the per-voxel margin itself: a
 voxel any of whose S^3 blocking sub-samples projects into the jaw opening
 is always kept (the margin is the farthest sub-sample's offset,
-sqrt(3) s_max (S - 1) / (2 S), magnified to the blocking plane).
+r = sqrt(3) s_max (S - 1) / (2 S), magnified to the blocking plane, with
+r / (1 - r / dmin) bounding r d / (d - r) over the depths d > dmin = 0.2 |K|
+that the cull tests).
 """
 import numpy as np
 import pytest
@@ -43,9 +45,12 @@ def beam_consts(src, jaws, spacing, samples=3):
         a_nS=F(nS), a_m0S=F(m0 @ pos), a_m2S=F(m2 @ pos), a_K=F(-vyw),
         a_c0=F(m0 @ w), a_c2=F(m2 @ w),
         cx_lo=F(jaws[0]), cx_hi=F(jaws[1]), cz_lo=F(jaws[2]), cz_hi=F(jaws[3]),
-        k=F(1.25 * np.sqrt(3.0) * max(spacing) * (samples - 1) / (2.0 * samples)),
         enable=(-nS > 0.0 and jaws[0] <= jaws[1] and jaws[2] <= jaws[3]),
     )
+    r = np.sqrt(3.0) * max(spacing) * (samples - 1) / (2.0 * samples)
+    dmin = 0.2 * abs(float(c["a_K"]))
+    c["k"] = F(r / (1.0 - r / dmin)) if r < 0.1 * dmin else F(0)
+    c["enable"] = c["enable"] and r < 0.1 * dmin
     return c
 
 
