@@ -543,86 +543,85 @@ def run_ours(args):
     # doses come down (copy-out stream) while step s computes.  The timed
     # region runs from the first copy in to the last copy out, the L2 flush
     # of each step included.
-    e2e = None
-    if rank == 0 or True:
-        from conehead_gb300.engine import DeviceBlock
-        h_rho = torch.from_numpy(np.ascontiguousarray(ph.densities)).pin_memory()
-        # block maps that exist (MLC or drawn maps) are inputs copied every
-        # step; a jaw rectangle travels in the beam record
-        crops = [i for i in range(B) if dblocks[i].crop is not None]
-        h_blocks = {i: torch.from_numpy(np.ascontiguousarray(dblocks[i].crop.cpu().numpy())).pin_memory()
-                    for i in crops}
-        sets = 2
-        h_doses = [[torch.empty(ph.size, dtype=torch.float32).pin_memory() for _ in range(B)] for _ in range(sets)]
-        d_rho = [torch.empty_like(rho) for _ in range(sets)]
-        d_blocks = [{i: torch.empty_like(dblocks[i].crop) for i in crops} for _ in range(sets)]
-        d_doses = [[torch.empty(ph.size, dtype=torch.float32, device=dev) for _ in range(B)] for _ in range(sets)]
-        in_st, out_st = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
-        computed, uploaded, copied = [None] * sets, [None] * sets, [None] * sets
-        # the job descriptors of a buffer set point at its device buffers and
-        # do not change between steps (the data they point at does): built once
-        set_jobs = [[eng.job(ph, d_rho[k], beams[i][0],
-                             DeviceBlock(d_blocks[k][i], dblocks[i].r0, dblocks[i].c0, dblocks[i].full_shape,
-                                         dblocks[i].uniform) if i in d_blocks[k] else dblocks[i],
-                             SETTINGS, dose=d_doses[k][i]) for i in range(B)] for k in range(sets)]
+    # every rank runs it (the window is a max over ranks)
+    from conehead_gb300.engine import DeviceBlock
+    h_rho = torch.from_numpy(np.ascontiguousarray(ph.densities)).pin_memory()
+    # block maps that exist (MLC or drawn maps) are inputs copied every
+    # step; a jaw rectangle travels in the beam record
+    crops = [i for i in range(B) if dblocks[i].crop is not None]
+    h_blocks = {i: torch.from_numpy(np.ascontiguousarray(dblocks[i].crop.cpu().numpy())).pin_memory()
+                for i in crops}
+    sets = 2
+    h_doses = [[torch.empty(ph.size, dtype=torch.float32).pin_memory() for _ in range(B)] for _ in range(sets)]
+    d_rho = [torch.empty_like(rho) for _ in range(sets)]
+    d_blocks = [{i: torch.empty_like(dblocks[i].crop) for i in crops} for _ in range(sets)]
+    d_doses = [[torch.empty(ph.size, dtype=torch.float32, device=dev) for _ in range(B)] for _ in range(sets)]
+    in_st, out_st = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    computed, uploaded, copied = [None] * sets, [None] * sets, [None] * sets
+    # the job descriptors of a buffer set point at its device buffers and
+    # do not change between steps (the data they point at does): built once
+    set_jobs = [[eng.job(ph, d_rho[k], beams[i][0],
+                         DeviceBlock(d_blocks[k][i], dblocks[i].r0, dblocks[i].c0, dblocks[i].full_shape,
+                                     dblocks[i].uniform) if i in d_blocks[k] else dblocks[i],
+                         SETTINGS, dose=d_doses[k][i]) for i in range(B)] for k in range(sets)]
 
-        def upload(s):
-            k = s % sets
-            if computed[k] is not None:
-                in_st.wait_event(computed[k])     # step s - 2 no longer reads set k's inputs
-            with torch.cuda.stream(in_st):
-                d_rho[k].copy_(h_rho, non_blocking=True)
-                for i in crops:
-                    d_blocks[k][i].copy_(h_blocks[i], non_blocking=True)
-            ev = torch.cuda.Event()
-            ev.record(in_st)
-            uploaded[k] = ev
+    def upload(s):
+        k = s % sets
+        if computed[k] is not None:
+            in_st.wait_event(computed[k])     # step s - 2 no longer reads set k's inputs
+        with torch.cuda.stream(in_st):
+            d_rho[k].copy_(h_rho, non_blocking=True)
+            for i in crops:
+                d_blocks[k][i].copy_(h_blocks[i], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(in_st)
+        uploaded[k] = ev
 
-        def compute(s):
-            k = s % sets
-            flush.fill_(float(s))
-            st.wait_event(uploaded[k])
-            if copied[k] is not None:
-                st.wait_event(copied[k])          # set k's doses of step s - 2 are on the host
-            eng.run_batch(set_jobs[k])
-            done = torch.cuda.Event()
-            done.record(st)
-            computed[k] = done
-            out_st.wait_event(done)
-            with torch.cuda.stream(out_st):
-                for i in range(B):
-                    h_doses[k][i].copy_(d_doses[k][i], non_blocking=True)
-            ev = torch.cuda.Event()
-            ev.record(out_st)
-            copied[k] = ev
+    def compute(s):
+        k = s % sets
+        flush.fill_(float(s))
+        st.wait_event(uploaded[k])
+        if copied[k] is not None:
+            st.wait_event(copied[k])          # set k's doses of step s - 2 are on the host
+        eng.run_batch(set_jobs[k])
+        done = torch.cuda.Event()
+        done.record(st)
+        computed[k] = done
+        out_st.wait_event(done)
+        with torch.cuda.stream(out_st):
+            for i in range(B):
+                h_doses[k][i].copy_(d_doses[k][i], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(out_st)
+        copied[k] = ev
 
-        def run_steps(first, count):
-            upload(first)
-            for s in range(first, first + count):
-                if s + 1 < first + count:
-                    upload(s + 1)
-                compute(s)
+    def run_steps(first, count):
+        upload(first)
+        for s in range(first, first + count):
+            if s + 1 < first + count:
+                upload(s + 1)
+            compute(s)
 
-        run_steps(0, args.warmup)
-        torch.cuda.synchronize(dev)
-        barrier()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        # e0 is recorded on the compute stream before the first upload is issued
-        e0.record(st)
-        in_st.wait_event(e0)
-        run_steps(args.warmup, args.steps)
-        for ev in copied:
-            if ev is not None:
-                st.wait_event(ev)
-        e1.record(st)
-        e1.synchronize()
-        eng.sync()
-        e2e_s = max_over_ranks(e0.elapsed_time(e1) / 1000.0, dev)
-        h2d = h_rho.numel() * 4 + sum(h.numel() * 4 for h in h_blocks.values())
-        e2e = {"value": world * args.steps * B / e2e_s, "unit": "beams/s",
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(B * N * 4),
-               "pipelined": "two buffer sets, copy-in / compute / copy-out streams: step s+1's inputs and "
-                            "step s-1's doses move while step s computes; each set's job descriptors built once"}
+    run_steps(0, args.warmup)
+    torch.cuda.synchronize(dev)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # e0 is recorded on the compute stream before the first upload is issued
+    e0.record(st)
+    in_st.wait_event(e0)
+    run_steps(args.warmup, args.steps)
+    for ev in copied:
+        if ev is not None:
+            st.wait_event(ev)
+    e1.record(st)
+    e1.synchronize()
+    eng.sync()
+    e2e_s = max_over_ranks(e0.elapsed_time(e1) / 1000.0, dev)
+    h2d = h_rho.numel() * 4 + sum(h.numel() * 4 for h in h_blocks.values())
+    e2e = {"value": world * args.steps * B / e2e_s, "unit": "beams/s",
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(B * N * 4),
+           "pipelined": "two buffer sets, copy-in / compute / copy-out streams: step s+1's inputs and "
+                        "step s-1's doses move while step s computes; each set's job descriptors built once"}
 
     # ---- reference-equivalent voxel·direction updates/s (untimed, a few beams)
     updates_line = None
