@@ -18,12 +18,15 @@ fluence -> TERMA -> collapsed-cone dose (float32 dose and accumulation).
               timed region
   roofline    the cone stage of the schedule in use, from the library's stage
               events on the launching stream, against the measured HBM peak:
-              spectral (default) = the five FFT passes, achieved = the bytes
-              those passes must move (TERMA pair in, A and B intermediates
-              written and read, dose pair out, S^ once per launch) over their
-              time; gather = algorithmic 8 N bytes per beam over the gather
-              launch, with "onchip" its updates/s against the shared-memory
-              lane ceiling
+              achieved = the stage's algorithmic bytes, 8 N per beam (TERMA
+              read, dose write), over its time; traffic = the DRAM bytes of
+              the committed ncu capture, and their ratio to the algorithmic
+              bytes; pass_traffic_frac (spectral) = the bytes the five FFT
+              passes' structure must move (A and B intermediates written and
+              read twice, S^ once per launch) over the same time.  "onchip"
+              (gather) gives its updates/s against the shared-memory lane
+              ceiling; "updates" gives the reference-equivalent updates/s of
+              the cone stage against an FP32 FMA ceiling
   cpu_baseline / --impl reference
               the CPU oracle (C++ FP64 restatement of the reference path,
               OpenMP over every host core) on whole beams of the workload
@@ -156,6 +159,29 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------- workload --
+def host_cpu():
+    """The host CPU model (lscpu, else /proc/cpuinfo) and its online cores."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if model is None:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.lower().startswith("model name"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    import platform
+    return {"model": model, "machine": platform.machine(), "online_cores": os.cpu_count()}
+
+
 def workload(n, spacing, seed=0):
     from conehead_gb300.phantoms import slab_phantom
     return slab_phantom(n, spacing, seed=seed)
@@ -198,7 +224,8 @@ def run_reference(args):
         "ms_per_step": 1000.0 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config(args),
-        "cpu_baseline": {"value": v, "unit": "beams/s", "cores": cores, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": v, "unit": "beams/s", "cores": cores, "kind": "port", "sample": sample,
+                         "cpu": host_cpu()},
         "e2e": {"value": v, "unit": "beams/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
     return 0
@@ -503,13 +530,16 @@ def run_ours(args):
     cone_ms = statistics.mean(x["ms_cone"] for x in stats)
     updates = statistics.mean(x["updates"] for x in stats)
     method = "spectral" if int(eng.get_tuning().get("cone_method", 0)) == 0 else "gather"
+    # algorithmic bytes of the cone stage: TERMA read + dose write, 8 N per
+    # beam, whatever the method (the per-beam figure of the path's roofline)
+    alg_bytes = B * 2 * 4 * N
     if method == "spectral":
-        alg_bytes = spectral_bytes(ph.size, B)
+        pass_bytes = spectral_bytes(ph.size, B)
         # scratch reset, cull, TERMA (every beam in one launch each), then
         # five passes per spectral launch
         launches_per_step = 3 + 5 * spectral_launches(B)
     else:
-        alg_bytes = B * 2 * 4 * N                 # TERMA read + dose write per beam
+        pass_bytes = alg_bytes
         launches_per_step = 5                     # reset, cull, TERMA, tap ranges, gather
     peaks = {}
     pk_path = os.path.join(HERE, "MEASURED_PEAKS.json")
@@ -527,14 +557,16 @@ def run_ours(args):
             tr = json.load(f)
         if tr.get("dram_bytes_per_beam"):
             traffic = tr["dram_bytes_per_beam"] * B
+    props = torch.cuda.get_device_properties(dev)
+    sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     onchip = None
     if method == "gather":
-        props = torch.cuda.get_device_properties(dev)
-        sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
         lds_ceiling = props.multi_processor_count * 32 * sm_mhz * 1e6     # one 4-byte LDS lane per update
         onchip = {"metric": "voxel-direction updates/s", "achieved": updates / (cone_ms * 1e-3),
                   "peak": lds_ceiling, "frac": updates / (cone_ms * 1e-3) / lds_ceiling,
                   "peak_basis": "SMs x 32 shared-memory lanes/clk x median SM clock"}
+    # a direct sum of the reference's updates costs one FP32 FMA each
+    fma_ceiling = props.multi_processor_count * 128 * sm_mhz * 1e6
 
     # ---- e2e through the C ABI with pinned host buffers.  Every step copies
     # its density and block crops host -> device, runs the batch and copies
@@ -628,8 +660,14 @@ def run_ours(args):
     if rank == 0 and args.update_beams > 0:
         w = reference_updates(eng, ph, [eng.job(ph, rho, beams[i][0], dblocks[i], SETTINGS)
                                         for i in range(min(args.update_beams, B))])
+        cone_rate = w * B / (cone_ms * 1e-3)
         updates_line = {"metric": "reference-equivalent voxel·direction updates/s", "per_beam": w,
                         "value": w * value, "e2e_value": w * e2e["value"] if e2e else None,
+                        "cone_stage_value": cone_rate,
+                        "fp32_fma_ceiling": fma_ceiling,
+                        "frac_of_fma_ceiling": cone_rate / fma_ceiling,
+                        "ceiling_basis": "a direct sum costs one FP32 FMA per update: SMs x 128 lanes x "
+                                         "median SM clock",
                         "basis": "updates the reference's per-voxel cone scatter does per beam (every "
                                  "TERMA voxel, 576 directions, every in-grid walk voxel), mean of "
                                  f"{min(args.update_beams, B)} beams of the workload, times beams/s"}
@@ -658,6 +696,12 @@ def run_ours(args):
             pl.append(time.perf_counter() - t0)
         extras["plain_gpu_beams_per_s"] = len(pl) / sum(pl)
         extras["plain_gpu_path"] = "prologue + per-voxel scatter with float32 atomics, one beam per launch"
+        extras["batching_ratios"] = {
+            "batched_over_single_beam": value / extras["single_beam_beams_per_s"],
+            "batched_over_plain_scatter": value / extras["plain_gpu_beams_per_s"],
+            "target_read_against": "plain_gpu_beams_per_s: the reference's own structure (one beam per "
+                                   "launch, per-voxel float32-atomic scatter) on the GPU; "
+                                   "single_beam_beams_per_s is this engine's spectral path one beam per call"}
         if args.serve_requests > 0:
             extras["serving"] = serving_extras(args, dev)
         if args.adjoint_iters > 0:
@@ -667,7 +711,7 @@ def run_ours(args):
         if not args.no_cpu:
             cv, cores, dt = cpu_oracle_beams(ph, beams[:args.cpu_beams])
             extras["cpu_baseline"] = {
-                "value": cv, "unit": "beams/s", "cores": cores, "kind": "port",
+                "value": cv, "unit": "beams/s", "cores": cores, "kind": "port", "cpu": host_cpu(),
                 "sample": f"{args.cpu_beams} whole beam(s) of the workload, FP64 oracle "
                           f"(C++ restatement of conehead's GPU path), OpenMP, {dt:.1f} s"}
     if rank == 0:
@@ -682,6 +726,15 @@ def run_ours(args):
                          "kernel": ("spectral cone stage (spec_z_forward, spec_y, spec_x, spec_y, "
                                     "spec_z_inverse)" if method == "spectral" else "cone_gather_kernel"),
                          "algorithmic_bytes_per_step": alg_bytes,
+                         "algorithmic_basis": "8 N bytes per beam (TERMA read, dose write), N = grid voxels",
+                         "traffic_over_algorithmic": traffic / alg_bytes if traffic else None,
+                         "pass_bytes_per_step": pass_bytes,
+                         "pass_traffic_frac": pass_bytes / (cone_ms * 1e-3) / 1e9 / hbm_peak,
+                         "pass_basis": ("bytes the FFT pass structure must move (TERMA pair in, A and B "
+                                        "intermediates written and read twice, dose pair out, S^ once per "
+                                        "launch) over the stage time: how well the passes stream, not how "
+                                        "close the stage is to its bound") if method == "spectral" else
+                                       "as achieved",
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"},
             "onchip": onchip,
             "cone_ms_per_step": cone_ms,

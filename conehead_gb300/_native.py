@@ -124,6 +124,7 @@ SIGNATURES = {
                                               P(ctypes.c_size_t)]),
     "ch_plan_trim": (ctypes.c_int, [VP]),
     "ch_plan_sync": (ctypes.c_int, [VP, VP]),
+    "ch_plan_set_wait_limit": (ctypes.c_int, [VP, ctypes.c_longlong, ctypes.c_int]),
     "ch_plan_stats": (ctypes.c_int, [VP, P(Stats)]),
     "ch_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "ch_last_error": (ctypes.c_char_p, []),

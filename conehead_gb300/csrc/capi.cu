@@ -126,6 +126,8 @@ struct ch_plan {
   int n_sm = 0;
   ch_tuning tuning{DIR_GROUP, 0, 8, CH_CONE_SPECTRAL};
   int live_batches = 0;      // captured batches reading this plan's stencils
+  long long wait_limit = 0;  // gather pipeline waits (try_wait iterations); 0 = MBAR_LIMIT
+  int withhold = 0;          // test hook of the expired-wait path (ch_plan_set_wait_limit)
   int reweights = 0;         // spectrum switches served by reweighting the stencils
   std::vector<std::unique_ptr<FrameStencils>> frames;   // beam-frame cone stencils by orientation
   uint64_t use_clock = 0;
@@ -477,8 +479,11 @@ ch_status frame_stencils(ch_plan* P, const float* spacing, const int* dims, cons
   return CH_OK;
 }
 
-ConeDirs cone_dirs(const StencilSet& S, const ch_tuning& t) {
+ConeDirs cone_dirs(const StencilSet& S, const ch_plan* P) {
+  const ch_tuning& t = P->tuning;
   ConeDirs D;
+  D.wait_limit = P->wait_limit > 0 ? P->wait_limit : MBAR_LIMIT;
+  D.withhold = P->withhold;
   D.group = t.dir_group;
   D.order = t.unit_order;
   D.n_dirs = S.n_dirs;
@@ -1223,7 +1228,7 @@ ch_status enqueue_batch(ch_plan* P, const BatchPlan& B, const Scratch& S, const 
   for (int i = 0; i < n; ++i)
     CH_CUDA(cudaMemsetAsync(B.jobs[i].dose, 0, (size_t)B.jobs[i].g.n[0] * B.jobs[i].g.n[1] * B.jobs[i].g.n[2] * 4,
                             s));
-  const ConeDirs D = cone_dirs(*B.set, P->tuning);
+  const ConeDirs D = cone_dirs(*B.set, P);
   launch_range(S.range_beams, n, B.max_tiles, D, s);
   CH_CUDA(cudaGetLastError());
   if (ev) CH_CUDA(cudaEventRecord(ev[2], s));
@@ -1267,7 +1272,7 @@ ch_status run_group(ch_plan* P, int n, const ch_grid* grids, const float* const*
       CH_CUDA(cudaGetLastError());
     }
     CH_CUDA(cudaEventRecord(P->ev[1], s));
-    const ConeDirs D = cone_dirs(*B.set, P->tuning);
+    const ConeDirs D = cone_dirs(*B.set, P);
     for (int i = 0; i < n; ++i) {
       const BeamJob& J = B.jobs[i];
       CH_CUDA(cudaMemsetAsync(J.dose, 0, (size_t)J.g.n[0] * J.g.n[1] * J.g.n[2] * 4, s));
@@ -1366,6 +1371,24 @@ ch_status static_scratch(int device, unsigned char** out) {
 }
 
 inline size_t align_up(size_t a, size_t b) { return (a + b - 1) / b * b; }
+
+// The launch records of ch_dose_static travel as one kernel parameter (the
+// launch copies it), so the call reads no host memory after it returns and
+// needs neither a copy engine nor a pinned buffer.
+struct StaticRecordWords {
+  unsigned int w[(sizeof(ConeBeam) + sizeof(RangeBeam)) / 4];
+};
+static_assert(sizeof(ConeBeam) % 4 == 0 && sizeof(RangeBeam) % 4 == 0, "records are whole words");
+static_assert(sizeof(StaticRecordWords) <= 16384, "the records fit the kernel parameter space");
+
+__global__ void write_static_records(const __grid_constant__ StaticRecordWords rec, unsigned int* cone_dst,
+                                     unsigned int* range_dst) {
+  constexpr int NC = (int)(sizeof(ConeBeam) / 4), NR = (int)(sizeof(RangeBeam) / 4);
+  for (int i = threadIdx.x; i < NC + NR; i += blockDim.x) {
+    if (i < NC) cone_dst[i] = rec.w[i];
+    else range_dst[i - NC] = rec.w[i];
+  }
+}
 
 }  // namespace
 
@@ -1528,6 +1551,10 @@ ch_status ch_dose_static(ch_plan* P, const ch_grid* grid, const float* rho, int 
 
   const BeamDev b = make_beam(*beam, *grid, settings->samples);
   const SettingsDev sd = make_settings(*settings);
+  // this call records no stage events: ch_plan_stats reports zeros for it
+  // rather than an earlier call's timings
+  P->stats_pending = false;
+  P->stats = ch_stats{};
   // aabb and the list count must start from their reset values; TERMA is
   // rewritten in full by the prologue and the range tables by range_kernel
   launch_init_scratch(aabb, 1, counters, s);
@@ -1540,18 +1567,7 @@ ch_status ch_dose_static(ch_plan* P, const ch_grid* grid, const float* rho, int 
   if (!enc) return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled is not available from the driver");
   ConeBeam C;
   std::memset(&C, 0, sizeof(C));
-  cuuint64_t gdim[3] = {(cuuint64_t)g.n[2], (cuuint64_t)g.n[1], (cuuint64_t)g.n[0]};
-  cuuint64_t gstride[2] = {(cuuint64_t)g.zp * 4, (cuuint64_t)g.zp * g.n[1] * 4};
-  cuuint32_t estr[3] = {1, 1, 1};
-  for (int v = 0; v < N_VARIANTS; ++v) {
-    for (int ex = TX; ex <= var_max_ex(v); ++ex) {
-      cuuint32_t box[3] = {(cuuint32_t)var_p(v), (cuuint32_t)var_rows(v), (cuuint32_t)ex};
-      CUresult r = enc(&C.tmap[tmap_index(v, ex)], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)T, gdim, gstride, box,
-                       estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-      if (r != CUDA_SUCCESS) return fail(CH_ERR_DEVICE, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
-    }
-  }
+  if ((st = encode_windows(enc, C, T, g)) != CH_OK) return st;
   C.dose = dose;
   C.ranges = reinterpret_cast<uint32_t*>(base + o_r);
   C.cranges = reinterpret_cast<uint32_t*>(base + o_cr);
@@ -1575,9 +1591,13 @@ ch_status ch_dose_static(ch_plan* P, const ch_grid* grid, const float* rho, int 
   R.aabb = aabb;
   R.ranges = reinterpret_cast<uint32_t*>(base + o_r);
   R.cranges = reinterpret_cast<uint32_t*>(base + o_cr);
-  CH_CUDA(cudaMemcpyAsync(base + o_cb, &C, sizeof(C), cudaMemcpyHostToDevice, s));
-  CH_CUDA(cudaMemcpyAsync(base + o_rb, &R, sizeof(R), cudaMemcpyHostToDevice, s));
-  const ConeDirs D = cone_dirs(P->st, P->tuning);
+  StaticRecordWords rec;
+  std::memcpy(rec.w, &C, sizeof(C));
+  std::memcpy(reinterpret_cast<unsigned char*>(rec.w) + sizeof(C), &R, sizeof(R));
+  write_static_records<<<1, 256, 0, s>>>(rec, reinterpret_cast<unsigned int*>(base + o_cb),
+                                         reinterpret_cast<unsigned int*>(base + o_rb));
+  CH_CUDA(cudaGetLastError());
+  const ConeDirs D = cone_dirs(P->st, P);
   launch_range(reinterpret_cast<const RangeBeam*>(base + o_rb), 1, n_tiles, D, s);
   CH_CUDA(cudaGetLastError());
   launch_gather(reinterpret_cast<const ConeBeam*>(base + o_cb), 1, D, n_units, P->n_sm, counters, updates, flags, s);
@@ -1688,7 +1708,7 @@ ch_status cone_operator(ch_plan* P, const ch_grid& grid, const float* in_dense, 
   launch_nonzero_box(in_dense, g.n[0], g.n[1], g.n[2], box, s);
   CH_CUDA(cudaGetLastError());
   CH_CUDA(cudaMemsetAsync(out, 0, (size_t)g.n[0] * g.n[1] * g.n[2] * sizeof(float), s));
-  const ConeDirs D = cone_dirs(S, P->tuning);
+  const ConeDirs D = cone_dirs(S, P);
   launch_range(P->range_beams.as<RangeBeam>(), 1, n_tiles, D, s);
   CH_CUDA(cudaGetLastError());
   launch_gather(P->cone_beams.as<ConeBeam>(), 1, D, n_units, P->n_sm, counters, updates, flags, s);
@@ -2023,6 +2043,16 @@ ch_status ch_plan_trim(ch_plan* P) {
                     &P->list_v, &P->spec_work, &P->pro_beams, &P->adj_in, &P->adj_out, &P->adj_w})
     b->release();
   P->stats_pending = false;
+  return CH_OK;
+}
+
+ch_status ch_plan_set_wait_limit(ch_plan* P, long long iterations, int withhold) {
+  if (!P) return fail(CH_ERR_INVALID_ARG, "plan is NULL");
+  if (P->live_batches > 0) return fail(CH_ERR_INVALID_ARG, "the wait limit cannot change while captured batches exist");
+  if (withhold != 0 && withhold != CH_WITHHOLD_WINDOWS && withhold != CH_WITHHOLD_SLOTS)
+    return fail(CH_ERR_INVALID_ARG, "withhold must be 0, CH_WITHHOLD_WINDOWS or CH_WITHHOLD_SLOTS");
+  P->wait_limit = iterations > 0 ? iterations : 0;
+  P->withhold = withhold;
   return CH_OK;
 }
 

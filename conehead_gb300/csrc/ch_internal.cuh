@@ -73,8 +73,11 @@ constexpr int CONE_THREADS = (CONE_CONSUMER_WARPS + 1) * 32;
 constexpr int DIR_GROUP = 16;         // unique directions per work unit (default; ch_tuning.dir_group)
 constexpr int MAX_DIR_GROUP = 1024;   // the producer walks a unit's directions 32 at a time
 
-// Bounded device-side waits (iterations of try_wait / spin).
-constexpr long long WAIT_LIMIT = 1ll << 26;
+// Bounded device-side waits: try_wait iterations of an mbarrier wait before
+// the gather gives up (its pipeline waits may be given a smaller bound per
+// plan, ch_plan_set_wait_limit; the wait for its own copies in flight always
+// has this one).
+constexpr long long MBAR_LIMIT = 1ll << 22;
 
 // device error flags (bit mask in Plan::d_flags[0])
 constexpr int FLAG_TIMEOUT = 1;
@@ -196,6 +199,9 @@ struct ConeDirs {
   const float* dirs;       // unit direction (x, y, z)
   int group;               // unique directions per work unit (1..MAX_DIR_GROUP)
   int order;               // units: 0 = tile outer, group inner; 1 = group outer, tile inner
+  long long wait_limit;    // try_wait iterations of a pipeline wait before the gather gives up
+  int withhold;            // test hook: 0 = off; CH_WITHHOLD_WINDOWS / CH_WITHHOLD_SLOTS (the
+                           // producer issues no window / the consumers free no slot)
 };
 
 struct RangeBeam {

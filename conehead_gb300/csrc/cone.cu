@@ -27,7 +27,9 @@
 //     tap's offsets and weight prefetched; on the unit's last chunk the
 //     accumulators are added to the dose with red.global.add.f32.
 // Every mbarrier wait is bounded; on expiry the kernel records
-// FLAG_TIMEOUT and returns.
+// FLAG_TIMEOUT, lets the producer's copies in flight land (a wait bounded by
+// MBAR_LIMIT) and returns.  The pipeline waits take their bound from the
+// launch (ConeDirs::wait_limit, MBAR_LIMIT unless the plan sets another).
 
 #include <cuda.h>
 
@@ -35,7 +37,6 @@
 
 namespace ch {
 
-constexpr long long MBAR_LIMIT = 1ll << 22;
 constexpr int DESC_LAST = 1, DESC_DONE = 2;
 
 // one chunk as the producer hands it to the consumers: runs a..b of walk u
@@ -76,8 +77,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (long long i = 0; i < MBAR_LIMIT; ++i)
+// `limit` try_wait iterations at most; false when the wait gave up
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit) {
+  for (long long i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -221,6 +223,8 @@ __device__ __forceinline__ void producer(const ConeBeam* __restrict__ beams, int
                                          int* flags, float* win, int4* slot_runs, ChunkDesc* desc,
                                          uint64_t* full, uint64_t* empty) {
   const int lane = threadIdx.x & 31;
+  // test hook: no window is issued, so every consumer's wait for one expires
+  if (D.withhold == CH_WITHHOLD_WINDOWS) return;
   const int n_groups = (D.n_dirs + D.group - 1) / D.group;
   int k = 0;
   bool ok = true;
@@ -229,7 +233,7 @@ __device__ __forceinline__ void producer(const ConeBeam* __restrict__ beams, int
   auto emit = [&](const ChunkDesc& d) -> bool {
     const int s = k % N_SLOTS;
     const uint32_t ph = (uint32_t)(k / N_SLOTS) & 1u;
-    if (!mbar_wait(&empty[s], ph ^ 1u)) return false;
+    if (!mbar_wait(&empty[s], ph ^ 1u, D.wait_limit)) return false;
     const bool done = (d.flags & DESC_DONE) != 0;
     const uint32_t run_bytes = done ? 0u : (uint32_t)(d.b - d.a + 1) * (uint32_t)(RUN_REC_INT4 * sizeof(int4));
     const uint32_t win_bytes = done ? 0u : (uint32_t)(var_p(d.var) * var_rows(d.var) * d.ex * 4);
@@ -364,7 +368,10 @@ __device__ __forceinline__ void producer(const ConeBeam* __restrict__ beams, int
   if (!ok) {
     if (lane == 0) atomicOr(flags, FLAG_TIMEOUT);
     // let this CTA's own copies land before its shared memory goes away
-    for (int j = max(0, k - N_SLOTS); j < k; ++j) mbar_wait(&full[j % N_SLOTS], (uint32_t)(j / N_SLOTS) & 1u);
+    // (always the full MBAR_LIMIT: a copy in flight completes in
+    // microseconds, whatever limit the pipeline waits were given)
+    for (int j = max(0, k - N_SLOTS); j < k; ++j)
+      mbar_wait(&full[j % N_SLOTS], (uint32_t)(j / N_SLOTS) & 1u, MBAR_LIMIT);
   }
 }
 
@@ -422,7 +429,7 @@ __device__ __forceinline__ void consumer(const ConeBeam* __restrict__ beams, con
   for (int i = 0; i < OUT_PER_THREAD; ++i) acc[i] = 0.0f;
   for (int k = 0;; ++k) {
     const int s = k % N_SLOTS;
-    if (!mbar_wait(&full[s], (uint32_t)(k / N_SLOTS) & 1u)) {
+    if (!mbar_wait(&full[s], (uint32_t)(k / N_SLOTS) & 1u, D.wait_limit)) {
       if (lane == 0) atomicOr(flags, FLAG_TIMEOUT);
       return;
     }
@@ -444,7 +451,9 @@ __device__ __forceinline__ void consumer(const ConeBeam* __restrict__ beams, con
       else consume_chunk<2, 1>(w, rp, nr, base0, acc);
     }
     __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[s]);
+    // (test hook: a slot is never freed, so the producer's wait for one
+    // expires with two windows in flight)
+    if (lane == 0 && D.withhold != CH_WITHHOLD_SLOTS) mbar_arrive(&empty[s]);
     if (d.flags & DESC_LAST) {
       const ConeBeam& B = beams[d.beam];
       const int x = d.tx0 + xl, y = d.ty0 + yl, z = d.tz0 + zl;

@@ -215,6 +215,13 @@ class DoseEngine:
         N.check(self.L.ch_plan_get_tuning(self.plan, ctypes.byref(t)), "ch_plan_get_tuning")
         return {k: getattr(t, k) for k, _ in N.Tuning._fields_}
 
+    def set_wait_limit(self, iterations=0, withhold=0):
+        """Bound of the gather's pipeline waits (try_wait iterations; 0 = the
+        default) and the test hook of their expiry (``withhold`` 1: no window
+        is issued; 2: no slot is freed; 0: off)."""
+        N.check(self.L.ch_plan_set_wait_limit(self.plan, int(iterations), int(withhold)),
+                "ch_plan_set_wait_limit")
+
     def prepare(self, size, spacing):
         """Build the stencils for grids up to ``size`` at ``spacing`` now."""
         g = N.grid_struct(size, (0.0, 0.0, 0.0), spacing)

@@ -184,7 +184,10 @@ ch_status ch_dose_scatter(ch_plan* plan, const ch_grid* grid, const float* rho_d
  * at least this large: run one ch_dose on it first.  The first call on a
  * device looks up the array's device address, so make that call before any
  * stream capture.  Every call shares the one array: calls whose work
- * overlaps on the GPU race, so serialise them (one stream, or events). */
+ * overlaps on the GPU race, so serialise them (one stream, or events).  It
+ * also uses the plan's own counters, so it must not overlap on the GPU with
+ * any other call on the same plan either.  It records no stage timings:
+ * ch_plan_stats reports zeros after it. */
 ch_status ch_dose_static(ch_plan* plan, const ch_grid* grid, const float* rho_dev, int swap_xy,
                          const ch_beam* beam, const ch_settings* settings, float* dose_dev,
                          void* stream);
@@ -358,6 +361,21 @@ ch_status ch_batch_scratch_bytes(ch_plan* plan, int n, const ch_grid* grids, siz
 /* Free the plan's scratch arena (kernel tables and stencils stay).  Waits
  * for all work on the device first. */
 ch_status ch_plan_trim(ch_plan* plan);
+
+/* Bound of the gather cone stage's pipeline waits, in mbarrier try_wait
+ * iterations (iterations <= 0 restores the default, 2^22).  When a wait
+ * gives up, the kernel records the failure, lets its own copies in flight
+ * land and returns; ch_plan_sync then reports CH_ERR_TIMEOUT and the plan
+ * stays usable.
+ * withhold is the test hook of that failure path (0 in normal use): with
+ * CH_WITHHOLD_WINDOWS the gather's producer issues no window, so the
+ * consumers' waits for one expire; with CH_WITHHOLD_SLOTS the consumers never
+ * free a window slot, so the producer's wait for one expires while its last
+ * two window copies are in flight.  No counterpart in the reference (its
+ * kernels have no device-side waits). */
+#define CH_WITHHOLD_WINDOWS 1
+#define CH_WITHHOLD_SLOTS 2
+ch_status ch_plan_set_wait_limit(ch_plan* plan, long long iterations, int withhold);
 
 /* Wait for the plan's work on `stream` and report device-side failures
  * (CH_ERR_TIMEOUT, CH_ERR_PARALLEL_RAY) of the last dose call. */

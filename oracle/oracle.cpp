@@ -511,9 +511,12 @@ void cone(const or_grid& g, const double* terma, const double* K, int n_r,
 // walk from s of dK_j[m] * r[v_m] -- the same walks as the scatter, reading
 // where it writes.  It is the dL/dTERMA of the beamlet adjoint (no
 // counterpart in the reference).  float64 sums in both modes.
+// With `support` set, only voxels whose support value is nonzero are
+// computed (the others are 0): the beamlet gradient needs dL/dTERMA only
+// where TERMA is nonzero, and that bounds the walks to the forward's.
 template <typename F>
 void cone_transpose(const or_grid& g, const double* r, const double* K, int n_r, const float* thetas,
-                    int n_theta, const float* phis, int n_phi, double* out) {
+                    int n_theta, const float* phis, int n_phi, double* out, const double* support = nullptr) {
   const int* n = g.n;
   std::vector<F> dirs((size_t)n_theta * n_phi * 3);
   for (int i = 0; i < n_theta; ++i)
@@ -524,6 +527,10 @@ void cone_transpose(const or_grid& g, const double* r, const double* K, int n_r,
     for (int y = 0; y < n[1]; ++y)
       for (int z = 0; z < n[2]; ++z) {
         const int start[3] = {x, y, z};
+        if (support && support[idx3(n, x, y, z)] == 0.0) {
+          out[idx3(n, x, y, z)] = 0.0;
+          continue;
+        }
         double acc = 0.0;
         for (int i = 0; i < n_theta; ++i)
           for (int j = 0; j < n_phi; ++j) {
@@ -541,9 +548,95 @@ void cone_transpose(const or_grid& g, const double* r, const double* K, int n_r,
       }
 }
 
+// Transposed blocking in float64 onto a beamlet grid (no counterpart in the
+// reference; the test oracle of the beamlet-weight gradient).  blocked(v) is
+// the mean over the voxel's S^3 sub-samples of the block map value of the
+// cell each projects to (conehead.py:71-120); on a beamlet map that value is
+// the weight of the beamlet holding the cell, so
+//   d blocked(v) / d w_b = (sub-samples of v in beamlet b) / S^3,
+// and grad[b] = sum_v coef[v] * d blocked(v) / d w_b for the caller's coef
+// (dL/dTERMA * dTERMA/dblocked).  Sample positions, projection and cell rule
+// are those of prologue_f64.  Beamlet (i, j) covers map rows
+// r0 + i cell_rows .. and columns c0 + j cell_cols ..
+int blocked_adjoint_f64(const or_grid& g, const or_beam& b, int S, const double* coef, int rows, int cols,
+                        int cell_rows, int cell_cols, int r0, int c0, double* grad) {
+  const int* n = g.n;
+  const int nb = rows * cols;
+  int bad = 0;
+  int nthr = 1;
+#ifdef _OPENMP
+  nthr = omp_get_max_threads();
+#endif
+  std::vector<std::vector<double>> priv((size_t)nthr, std::vector<double>((size_t)nb, 0.0));
+#pragma omp parallel for collapse(2) schedule(dynamic, 1) reduction(| : bad)
+  for (int x = 0; x < n[0]; ++x)
+    for (int y = 0; y < n[1]; ++y) {
+      int tid = 0;
+#ifdef _OPENMP
+      tid = omp_get_thread_num();
+#endif
+      std::vector<double>& acc = priv[(size_t)tid];
+      for (int z = 0; z < n[2]; ++z) {
+        const double cv = coef[idx3(n, x, y, z)];
+        if (cv == 0.0) continue;
+        const int id[3] = {x, y, z};
+        double pos[3], off[3];
+        for (int k = 0; k < 3; ++k) {
+          pos[k] = (double)g.origin[k] + (double)g.spacing[k] * id[k];
+          off[k] = (double)g.spacing[k] / S;
+        }
+        for (int ix = 0; ix < S; ++ix)
+          for (int iy = 0; iy < S; ++iy)
+            for (int iz = 0; iz < S; ++iz) {
+              const int ii[3] = {ix, iy, iz};
+              double rd[3];
+              for (int k = 0; k < 3; ++k)
+                rd[k] = b.src[k] - (pos[k] - (double)g.spacing[k] / 2.0 + off[k] / 2.0 + off[k] * ii[k]);
+              double px, pz;
+              if (!project_d(b, rd, &px, &pz)) {
+                bad = 1;
+                continue;
+              }
+              const double cr = (double)floor_clamped(px * 100.0) + 2000.0;
+              const double cc = (double)floor_clamped(pz * 100.0) + 2000.0;
+              if (cr < 0 || cr > 3999 || cc < 0 || cc > 3999) continue;
+              int64_t r = (int64_t)cr - 1, c = (int64_t)cc - 1;
+              if (r < 0) r += b.block_rows;
+              if (c < 0) c += b.block_cols;
+              const int64_t i = r - r0, j = c - c0;
+              if (i < 0 || j < 0 || i >= (int64_t)rows * cell_rows || j >= (int64_t)cols * cell_cols) continue;
+              acc[(size_t)((i / cell_rows) * cols + j / cell_cols)] += cv / (double)(S * S * S);
+            }
+      }
+    }
+  for (int k = 0; k < nb; ++k) {
+    double s = 0.0;
+    for (int t = 0; t < nthr; ++t) s += priv[(size_t)t][(size_t)k];
+    grad[k] = s;
+  }
+  return bad ? 1 : 0;
+}
+
 }  // namespace
 
 extern "C" {
+
+// Transposed cone computed only where support != 0 (0 elsewhere); see
+// cone_transpose.
+void or_cone_transpose_on(const or_grid* g, const double* r, const double* K, int n_r, const float* thetas,
+                          int n_theta, const float* phis, int n_phi, int mode, const double* support,
+                          double* out) {
+  if (mode == 0) cone_transpose<float>(*g, r, K, n_r, thetas, n_theta, phis, n_phi, out, support);
+  else cone_transpose<double>(*g, r, K, n_r, thetas, n_theta, phis, n_phi, out, support);
+}
+
+// Float64 transposed blocking onto a beamlet grid (see blocked_adjoint_f64);
+// `grad` (rows * cols float64) is overwritten.  Returns 0, or 1 if a ray was
+// parallel to the blocking plane.
+int or_blocked_adjoint(const or_grid* g, const or_beam* b, int samples, const double* coef, int rows, int cols,
+                       int cell_rows, int cell_cols, int r0, int c0, double* grad) {
+  return blocked_adjoint_f64(*g, *b, samples, coef, rows, cols, cell_rows, cell_cols, r0, c0, grad);
+}
 
 // Cone stage with the physics extensions (see ConeExt): rho (float32, the
 // phantom's densities, read with swap_xy like the TERMA pass) for the

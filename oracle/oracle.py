@@ -75,6 +75,10 @@ def lib():
         L.or_cone_ext.restype = None
         L.or_cone_transpose.argtypes = L.or_cone.argtypes
         L.or_cone_transpose.restype = None
+        L.or_cone_transpose_on.argtypes = L.or_cone.argtypes[:-1] + [dp, dp]
+        L.or_cone_transpose_on.restype = None
+        L.or_blocked_adjoint.argtypes = [P(_Grid), P(_Beam), ctypes.c_int, dp] + [ctypes.c_int] * 6 + [dp]
+        L.or_blocked_adjoint.restype = ctypes.c_int
         L.or_dda.argtypes = [P(ctypes.c_int), P(ctypes.c_float), P(ctypes.c_int), dp,
                              ctypes.c_int, ctypes.c_int, P(ctypes.c_int), dp]
         L.or_dda.restype = ctypes.c_int
@@ -209,6 +213,69 @@ def cone_transpose(r, size, spacing, K, thetas, phis, mode=MODE_F64):
                             K.shape[1], _ptr(th, ctypes.c_float), len(th), _ptr(ph, ctypes.c_float),
                             len(ph), int(mode), _ptr(out, ctypes.c_double))
     return out
+
+
+def cone_transpose_on(r, support, size, spacing, K, thetas, phis, mode=MODE_F64):
+    """Transposed cone of ``r`` computed only where ``support`` != 0 (0
+    elsewhere); float64."""
+    size = [int(n) for n in size]
+    R = np.ascontiguousarray(r, dtype=np.float64)
+    sup = np.ascontiguousarray(support, dtype=np.float64)
+    K = np.ascontiguousarray(K, dtype=np.float64)
+    th = np.ascontiguousarray(thetas, dtype=np.float32)
+    ph = np.ascontiguousarray(phis, dtype=np.float32)
+    g = grid_struct(size, (0, 0, 0), spacing)
+    out = np.zeros(size, dtype=np.float64)
+    lib().or_cone_transpose_on(ctypes.byref(g), _ptr(R, ctypes.c_double), _ptr(K, ctypes.c_double),
+                               K.shape[1], _ptr(th, ctypes.c_float), len(th), _ptr(ph, ctypes.c_float),
+                               len(ph), int(mode), _ptr(sup, ctypes.c_double), _ptr(out, ctypes.c_double))
+    return out
+
+
+def blocked_adjoint(source, block, phantom, settings, coef, beamlets):
+    """Float64 transposed blocking onto a beamlet grid: grad[i, j] = sum over
+    voxels v of coef[v] * (sub-samples of v whose block map cell lies in
+    beamlet (i, j)) / S^3.  ``beamlets`` has rows, cols, cell_rows,
+    cell_cols, r0 and c0 (map cells); ``block.block_values`` gives the map
+    shape (the cell rule wraps index -1 to its last row / column)."""
+    size = [int(n) for n in phantom.size]
+    block_values = np.ascontiguousarray(block.block_values, dtype=np.float32)
+    g = grid_struct(size, phantom.origin, phantom.spacing)
+    b = beam_struct(source, block_values)
+    c = np.ascontiguousarray(coef, dtype=np.float64)
+    grad = np.zeros((beamlets.rows, beamlets.cols), dtype=np.float64)
+    rc = lib().or_blocked_adjoint(ctypes.byref(g), ctypes.byref(b), int(settings["fluenceResampling"]),
+                                  _ptr(c, ctypes.c_double), beamlets.rows, beamlets.cols, beamlets.cell_rows,
+                                  beamlets.cell_cols, beamlets.r0, beamlets.c0, _ptr(grad, ctypes.c_double))
+    if rc != 0:
+        raise RuntimeError("no intersection or line is within plane")
+    return grad
+
+
+def beamlet_gradient_f64(source, beamlets, weights, phantom, settings, target, kernel_dir=None):
+    """FP64 gradient of L = sum (dose - target)^2 with respect to beamlet
+    weights, by the chain rule through the FP64 re-run of the reference path:
+    the forward (prologue and cone), dL/dTERMA = C^T 2 (dose - target) on the
+    TERMA support, and, since fluence and TERMA each carry one factor of the
+    blocked fraction (conehead.py:360, :377), dTERMA/dblocked = 2 TERMA /
+    blocked, pushed onto the beamlets by the transposed blocking.  Returns
+    (grad [rows, cols], dose)."""
+    from conehead_gb300.kernel import poly_kernel_tables
+
+    class _Map:
+        block_values = beamlets.host_map(weights)
+
+    blk = _Map()
+    out = prologue(source, blk, phantom, settings, MODE_F64)
+    K, thetas, phis = poly_kernel_tables(settings["energy_weights"], kernel_dir)
+    T, bl = out["terma"], out["blocked"]
+    dose = cone(T, phantom.size, phantom.spacing, K, thetas, phis, MODE_F64)
+    g_t = cone_transpose_on(2.0 * (dose - np.asarray(target, dtype=np.float64)), T, phantom.size, phantom.spacing,
+                            K, thetas, phis, MODE_F64)
+    coef = np.zeros_like(T)
+    nz = bl > 0
+    coef[nz] = 2.0 * g_t[nz] * T[nz] / bl[nz]
+    return blocked_adjoint(source, blk, phantom, settings, coef, beamlets), dose
 
 
 def calculate(source, block, phantom, settings, mode=MODE_F32, kernel_dir=None):

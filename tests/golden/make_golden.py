@@ -1,9 +1,9 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Run once in a container that has the conehead sources (read-only) at
-``--ref`` (default /root/reference)::
+Run once in a container that has the conehead sources (read-only), named
+by ``--ref`` or by the environment variable ``CONEHEAD_REFERENCE``::
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref /path/to/conehead
 
 Three fixture families:
 
@@ -430,9 +430,12 @@ def make_plans(ref):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("CONEHEAD_REFERENCE"),
+                    help="conehead checkout (default: $CONEHEAD_REFERENCE)")
     ap.add_argument("--only", default=None, help="pipeline|dda|tables|plans")
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("name the conehead checkout with --ref or CONEHEAD_REFERENCE")
     if a.only in (None, "tables"):
         make_tables(a.ref)
         print("tables done")

@@ -77,3 +77,39 @@ def test_beamlet_grid_geometry():
     assert (s.rows, s.cols, s.cell_rows, s.cell_cols, s.r0, s.c0) == (40, 40, 50, 50, 1000, 1000)
     with pytest.raises(ValueError):
         BeamletGrid.square(90, 0.5)           # 45 cm does not fit the 40 cm map
+
+
+def test_fp64_chain_rule_gradient_equals_oracle_differences(oracle_lib, settings):
+    """The FP64 beamlet gradient by the chain rule (forward, C^T on the TERMA
+    support, dTERMA/dblocked = 2 T / blocked, transposed blocking onto the
+    beamlets) equals central differences of the FP64 oracle's own objective.
+    This pins the checker that the full-size GPU gradient is compared with."""
+    from conehead_gb300 import Source
+    from conehead_gb300.adjoint import BeamletGrid, MapBlock, sphere_target
+    from conehead_gb300.phantoms import slab_phantom
+    ph = slab_phantom(20, 0.5, seed=6, n_inserts=3)
+    src = Source()
+    src.gantry = 35.0
+    src.collimator = 0.0
+    bl = BeamletGrid.square(6, 1.0)
+    rng = np.random.default_rng(12)
+    w = rng.uniform(0.0, 1.0, bl.shape).astype(np.float32)
+    target = sphere_target(ph, (0.5, 0.0, -0.5), 2.0)
+    grad, dose = oracle_lib.beamlet_gradient_f64(src, bl, w, ph, settings, target)
+    assert dose.max() > 0 and np.abs(grad).max() > 0
+
+    def loss(weights):
+        d = oracle_lib.calculate(src, MapBlock(bl.host_map(weights)), ph, settings, oracle_lib.MODE_F64)["dose"]
+        return float(((d - target) ** 2).sum())
+
+    h = 1e-4
+    flat = [(i, j) for i in range(bl.rows) for j in range(bl.cols)]
+    picks = [flat[k] for k in rng.choice(len(flat), 8, replace=False)]
+    for i, j in picks:
+        wp, wm = w.copy(), w.copy()
+        wp[i, j] = np.float32(w[i, j] + h)
+        wm[i, j] = np.float32(w[i, j] - h)
+        fd = (loss(wp) - loss(wm)) / (float(wp[i, j]) - float(wm[i, j]))
+        # L is quartic in w (the dose is quadratic), so the central difference
+        # is off by O(h^2) terms, far below this bound
+        assert abs(grad[i, j] - fd) <= 1e-6 * np.abs(grad).max(), (i, j, grad[i, j], fd)

@@ -9,7 +9,10 @@
   the FP64 oracle on 50 random beamlets (40^3 heterogeneous phantom,
   10 x 10 beamlets of 1 cm).
 * At the full configuration (128^3 heterogeneous phantom, 40 x 40 beamlets
-  of 0.5 cm, weights U[0, 1], 4 cm target sphere) the gradient agrees with a
+  of 0.5 cm, weights U[0, 1], 4 cm target sphere) the gradient agrees on all
+  1600 beamlets with the exact FP64 gradient of the FP64 oracle (its forward,
+  its transposed cone of 2 (dose - target) on the TERMA support, and the
+  chain through blocked^2, conehead/conehead.py:360 and :377), and with a
   central difference of the plain forward along a random direction.
 * The autograd path returns the adjoint's gradient and a descent step
   lowers the objective.
@@ -171,6 +174,42 @@ def test_full_size_directional_derivative(eng, settings):
     ad = float((g * delta).sum())
     print(f"128^3, 40x40 beamlets: <grad, d> = {ad:.6e}, central difference {fd:.6e}, rel {abs(ad - fd) / abs(fd):.2e}")
     assert abs(ad - fd) <= 5e-4 * abs(fd)
+
+
+def test_full_size_gradient_matches_the_fp64_gradient(eng, settings, oracle_lib):
+    """128^3 slab phantom, 40 x 40 beamlets of 0.5 cm, weights U[0, 1], target
+    2 inside a seeded 4 cm sphere: the GPU's float32 adjoint against the FP64
+    chain-rule gradient of the oracle (one FP64 forward and one FP64
+    transposed cone for all beamlets; about a minute of host time)."""
+    import time
+
+    import torch
+    from conehead_gb300.adjoint import BeamletDose, BeamletGrid, beamlet_dose, sphere_target
+    from conehead_gb300.phantoms import slab_phantom
+    ph = slab_phantom(128, 0.25, seed=0)
+    rng = np.random.default_rng(5)
+    centre = tuple(rng.uniform(-3.0, 3.0, 3))
+    target = sphere_target(ph, centre, 2.0)
+    src = _beam(float(rng.uniform(0, 360)), 0.0)
+    bl = BeamletGrid.square(40, 0.5)
+    w = rng.uniform(0, 1, bl.shape).astype(np.float32)
+    op = BeamletDose(eng, ph, src, bl, settings)
+    wt = torch.tensor(w, device="cuda", requires_grad=True)
+    loss = ((beamlet_dose(wt, op).double() - torch.from_numpy(target).cuda().double()) ** 2).sum()
+    loss.backward()
+    g_gpu = wt.grad.cpu().numpy().astype(np.float64)
+    t0 = time.perf_counter()
+    g64, _ = oracle_lib.beamlet_gradient_f64(src, bl, w, ph, settings, target)
+    t_cpu = time.perf_counter() - t0
+    scale = np.abs(g64).max()
+    err = np.abs(g_gpu - g64) / scale
+    rel = np.linalg.norm(g_gpu - g64) / np.linalg.norm(g64)
+    picks = rng.choice(g64.size, 50, replace=False)
+    print(f"128^3, 40x40 beamlets of 0.5 cm: GPU gradient vs FP64 chain-rule gradient: max |diff| "
+          f"{err.max():.2e} of max |grad| over all 1600 beamlets ({err.reshape(-1)[picks].max():.2e} on 50 "
+          f"random ones), relative L2 {rel:.2e}; FP64 oracle {t_cpu:.0f} s on {oracle_lib.num_threads()} threads")
+    assert scale > 0
+    assert err.max() <= 1e-3 and rel <= 1e-3
 
 
 def test_autograd_matches_backward_and_descends(eng, settings):

@@ -78,6 +78,39 @@ def test_static_matches_ch_dose_on_consecutive_calls(setup):
         assert np.abs(d - ref).max() <= TOL * ref.max()
 
 
+@pytest.mark.parametrize("size", [(48, 40, 37), (44, 44, 30)], ids=["ragged-swap0", "square-xy-swap1"])
+def test_static_matches_ch_dose_on_smaller_grids(setup, size):
+    """A plan prepared for 64^3 serves smaller, non-cubic grids: its tile
+    count, z padding and scratch layout follow the grid of each call.  A grid
+    with unequal x and y reads the densities as they are (swap_xy = 0); a
+    square x/y grid reads them transposed, as the reference's resampling
+    does (swap_xy = 1)."""
+    import torch
+    from conehead_gb300 import GridPhantom
+    from conehead_gb300.phantoms import random_beam
+    eng, settings = setup
+    eng.prepare((64, 64, 64), (0.25, 0.25, 0.25))
+    rng = np.random.default_rng(sum(size))
+    rho_h = rng.uniform(0.3, 1.8, size).astype(np.float32)
+    s = np.float32(0.25)
+    ph = GridPhantom(rho_h, tuple(-(k - 1) * s / 2 for k in size), (s, s, s))
+    rho = eng.upload_densities(ph.densities)
+    src, blk = random_beam(rng, rect=(3.0, 7.0), collimator=True)
+    db = eng.upload_block(blk.block_values)
+    ref_job = eng.job(ph, rho, src, db, settings)
+    assert ref_job.swap_xy == int(size[0] == size[1])
+    ref = eng.run(ref_job).clone()
+    eng.sync()
+    ref = ref.cpu().numpy()
+    assert ref.max() > 0
+    outs = [torch.full(size, -1.0, dtype=torch.float32, device=eng.device) for _ in range(2)]
+    for out in outs:                                   # two calls in a row
+        call_static(eng, eng.job(ph, rho, src, db, settings, dose=out))
+    eng.sync()
+    for out in outs:
+        assert np.abs(out.cpu().numpy() - ref).max() <= TOL * ref.max()
+
+
 def test_static_refuses_grids_beyond_its_scratch(setup):
     from conehead_gb300 import _native as N
     from conehead_gb300.phantoms import random_beam, slab_phantom
