@@ -126,7 +126,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (OSError, ValueError):
             self.proc = None
@@ -261,7 +261,8 @@ def serving_extras(args, dev):
         st = server.stats()
         rows.append({"rate_req_s": rate, "requests": st["requests"], "beams": st["beams"],
                      "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "beams_per_s": st["beams_per_s"],
-                     "mean_batch_beams": st["mean_batch_beams"], "peak_gb": st["peak_bytes"] / 1e9})
+                     "mean_batch_beams": st["mean_batch_beams"], "peak_gb": st["peak_bytes"] / 1e9,
+                     "slowest": st["slowest"]})
     ex.close()
     return {"workload": "Poisson arrivals, 1-8 beams per request (5x5 cm, gantry U[0,360)), phantoms "
                         "64^3/96^3/128^3/192^3 @ 0.25 cm resident, 2 slots, latency = arrival to dose "
@@ -429,15 +430,24 @@ def spectral_launches(beams, max_pairs=SPEC_MAX_PAIRS):
     return ((beams + 1) // 2 + max_pairs - 1) // max_pairs
 
 
+def plane_path(size):
+    """The library's plane path: FFT periods of 256 on every axis (grids of
+    97-128 voxels per axis): z forward, one fused plane kernel (y and x
+    transforms, the S^ product and their inverses on chip), z inverse."""
+    return all(spectral_period(int(k)) == 256 for k in size)
+
+
 def spectral_bytes(size, beams, max_pairs=SPEC_MAX_PAIRS):
-    """HBM bytes the five FFT passes must move for `beams` beams of one grid:
-    per pair of beams the two TERMA volumes in and two doses out (16 N), the
-    intermediates A [nx][ny][Mz] and B [nx][My][Mz] (complex float32) each
-    written and read twice, and S^ [Mx][My][Mz] read once per launch."""
+    """HBM bytes the FFT passes must move for `beams` beams of one grid: per
+    pair of beams the two TERMA volumes in and two doses out (16 N), the
+    intermediate A [nx][ny][Mz] (complex float32) written and read twice,
+    B [nx][My][Mz] likewise on the five-pass path (the plane path keeps it on
+    chip), and S^ [Mx][My][Mz] read once per launch."""
     nx, ny, nz = (int(k) for k in size)
     Mx, My, Mz = (spectral_period(k) for k in (nx, ny, nz))
     pairs = (beams + 1) // 2
-    a, b = nx * ny * Mz * 8, nx * My * Mz * 8
+    a = nx * ny * Mz * 8
+    b = 0 if plane_path(size) else nx * My * Mz * 8
     return pairs * (16 * nx * ny * nz + 4 * a + 4 * b) + spectral_launches(beams, max_pairs) * Mx * My * Mz * 8
 
 
@@ -536,8 +546,9 @@ def run_ours(args):
     if method == "spectral":
         pass_bytes = spectral_bytes(ph.size, B)
         # scratch reset, cull, TERMA (every beam in one launch each), then
-        # five passes per spectral launch
-        launches_per_step = 3 + 5 * spectral_launches(B)
+        # per spectral launch three kernels (plane path: z forward, plane
+        # kernel, z inverse) or five passes
+        launches_per_step = 3 + (3 if plane_path(ph.size) else 5) * spectral_launches(B)
     else:
         pass_bytes = alg_bytes
         launches_per_step = 5                     # reset, cull, TERMA, tap ranges, gather
@@ -718,22 +729,26 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": "beams/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * job_s / args.steps,
+            "step_ms_spread": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)},
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded slab phantom and beams; no dataset)",
             "config": config(args),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic,
-                         "kernel": ("spectral cone stage (spec_z_forward, spec_y, spec_x, spec_y, "
-                                    "spec_z_inverse)" if method == "spectral" else "cone_gather_kernel"),
+                         "kernel": (("spectral cone stage, plane path (spec_z_forward_plane, spec_plane, "
+                                     "spec_z_inverse_plane)" if plane_path(ph.size) else
+                                     "spectral cone stage (spec_z_forward, spec_y, spec_x, spec_y, spec_z_inverse)")
+                                    if method == "spectral" else "cone_gather_kernel"),
                          "algorithmic_bytes_per_step": alg_bytes,
                          "algorithmic_basis": "8 N bytes per beam (TERMA read, dose write), N = grid voxels",
                          "traffic_over_algorithmic": traffic / alg_bytes if traffic else None,
                          "pass_bytes_per_step": pass_bytes,
                          "pass_traffic_frac": pass_bytes / (cone_ms * 1e-3) / 1e9 / hbm_peak,
-                         "pass_basis": ("bytes the FFT pass structure must move (TERMA pair in, A and B "
-                                        "intermediates written and read twice, dose pair out, S^ once per "
-                                        "launch) over the stage time: how well the passes stream, not how "
-                                        "close the stage is to its bound") if method == "spectral" else
+                         "pass_basis": ("bytes the FFT pass structure must move (TERMA pair in, the A "
+                                        "intermediate (and B on the five-pass path) written and read twice, "
+                                        "dose pair out, S^ once per launch) over the stage time: how well the "
+                                        "passes stream, not how close the stage is to its bound")
+                                       if method == "spectral" else
                                        "as achieved",
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"},
             "onchip": onchip,

@@ -517,6 +517,8 @@ SpecGrid spec_grid(const ch_plan* P, const int* n, const int* M, int zp, int con
   g.zp = zp;
   g.conj = conj;
   g.shat = shat;
+  g.plane = spec_plane_path(M) && n[0] <= SPEC_PLANE_M / 2 && n[1] <= SPEC_PLANE_M / 2 && n[2] <= SPEC_PLANE_M / 2;
+  g.lp = g.plane ? spec_plane_pitch(n) : 0;
   return g;
 }
 
@@ -604,6 +606,13 @@ ch_status spec_shat(ch_plan* P, const StencilSet& S, const int* n, cudaStream_t 
   L.p[0] = SpecPair{s_real.as<float>(), nullptr, nullptr, nullptr, work.as<float2>(), E->shat.as<float2>(),
                     nullptr, nullptr};
   launch_spec_build(L, d_idx.as<long long>(), d_val.as<float>(), (int)idx.size(), s_real.as<float>(), s);
+  if (spec_plane_path(M)) {
+    // the plane path reads S^ plane by plane: [Mz][My][Mx], transposed into
+    // the work buffer, which then becomes the cached S^ (the untransposed
+    // copy is released with the other build buffers)
+    launch_spec_transpose(E->shat.as<float2>(), work.as<float2>(), M[0], M[1], M[2], s);
+    std::swap(E->shat, work);
+  }
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   cleanup();
@@ -904,7 +913,10 @@ SpecLayout spec_layout(int n, const ch_grid* grids) {
       }
     const int* d = grids[i].n;
     const int M[3] = {spec_period(d[0]), spec_period(d[1]), spec_period(d[2])};
-    const size_t a_sz = (size_t)d[0] * d[1] * M[2], b_sz = (size_t)d[0] * M[1] * M[2];
+    // the plane path keeps A plane-major (pitch spec_plane_pitch) and needs no B
+    const bool plane = spec_plane_path(M);
+    const size_t a_sz = plane ? (size_t)M[2] * spec_plane_pitch(d) : (size_t)d[0] * d[1] * M[2];
+    const size_t b_sz = plane ? 0 : (size_t)d[0] * M[1] * M[2];
     for (size_t p = 0; p < group.size(); p += 2 * SPEC_MAX_PAIRS) {
       SpecPlanLaunch l;
       for (int k = 0; k < 3; ++k) {

@@ -256,7 +256,9 @@ struct SpecGrid {
   int zp;                  // z pitch of the TERMA volumes
   int conj;                // multiply by conj(S^): the transposed cone
   const float2* tw[3];     // twiddles exp(-2 pi i k / M_axis)
-  const float2* shat;      // S^ [Mx][My][Mz], 1/(Mx My Mz) folded in
+  const float2* shat;      // S^ [Mx][My][Mz], 1/(Mx My Mz) folded in; [Mz][My][Mx] on the plane path
+  int plane;               // the plane path (spec_plane_path): A = [Mz][lp] plane-major, no B
+  int lp;                  // plane pitch of A on the plane path (nx ny rounded up to 32)
 };
 struct SpecLaunch {
   SpecGrid g;
@@ -270,6 +272,20 @@ std::vector<float2> spec_twiddles();      // every period (ascending), back to b
 size_t spec_twiddle_offset(int M);
 cudaError_t setup_spec_kernels();        // allow SPEC_SMEM of dynamic shared memory
 void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st);
+// The plane path: periods of 256 on every axis (grids of 97 to 128 voxels
+// per axis).  z forward into plane-major A[kz][x y], one cluster of two CTAs
+// per (pair, kz) plane for the y and x transforms, the S^ product and their
+// inverses (the plane's spectrum held in the pair's shared memory), z
+// inverse from A.  S^ is then kept as [Mz][My][Mx].
+constexpr int SPEC_PLANE_M = 256;
+// half the plane spectrum, an exchange buffer per warp, the twiddle table
+constexpr int SPEC_PLANE_SMEM = (128 * 128 + 16 * 2 * 256 + 256) * 8;
+inline bool spec_plane_path(const int* M) {
+  return M[0] == SPEC_PLANE_M && M[1] == SPEC_PLANE_M && M[2] == SPEC_PLANE_M;
+}
+inline int spec_plane_pitch(const int* n) { return (n[0] * n[1] + 31) / 32 * 32; }
+// S^ [Mx][My][Mz] -> [Mz][My][Mx]
+void launch_spec_transpose(const float2* in, float2* out, int Mx, int My, int Mz, cudaStream_t st);
 // S^ of one grid shape: scatter the stencil values into the real volume
 // s_real (zeroed, [Mx][My][Mz] = L.p[0].t1), then three forward passes
 // (L.g.n = M, L.p[0].a = work, L.p[0].b = S^)

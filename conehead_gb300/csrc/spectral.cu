@@ -32,6 +32,8 @@
 #include <cmath>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "ch_internal.cuh"
 
 namespace ch {
@@ -711,6 +713,379 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_inverse
   }
 }
 
+// ------------------------------------------------------------ plane path --
+// Periods of 256 on all three axes.  The y and x transforms of one kz plane
+// (with the S^ product and both inverses) run in one kernel on the plane's
+// spectrum held on chip, so the intermediate B [nx][My][Mz] of the five-pass
+// path never reaches memory; A is laid out plane-major, A[kz][l] with
+// l = x ny + y and plane pitch lp, so a plane is one contiguous block.
+//
+// z forward into plane-major A: stage 1 with lanes along z (the TERMA rows
+// are read coalesced), stage 2 with lanes across the CTA's 16 lines (one kz
+// of 16 consecutive lines is one 128-byte store).  Both stages address the
+// exchange buffer with the z layout swz16<true>; either lane mapping reads
+// or writes 16 distinct banks per half warp there.
+__global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward_plane_kernel(SpecLaunch P) {
+  extern __shared__ float2 spec_sm[];
+  float2* sm = spec_sm;
+  const SpecPair& pr = P.p[blockIdx.y];
+  const int nl = P.g.n[0] * P.g.n[1], nz = P.g.n[2], lp = P.g.lp;
+  const int l0 = blockIdx.x * R16_LINES;
+  __shared__ unsigned char zf[2][R16_LINES];
+  bool mine = false;
+  if (threadIdx.x < R16_LINES) {
+    const int c = threadIdx.x, l = l0 + c, lc = l < nl ? l : nl - 1;
+    const unsigned a1 = pr.l1 ? (unsigned)__ldg(pr.l1 + lc) : 1u;
+    const unsigned a2 = (pr.t2 && pr.l2) ? (unsigned)__ldg(pr.l2 + lc) : 1u;
+    zf[0][c] = l < nl && a1 != 0u;
+    zf[1][c] = l < nl && pr.t2 && a2 != 0u;
+    mine = zf[0][c] || zf[1][c];
+  }
+  if (!__syncthreads_or(mine)) {
+    // no TERMA on these 16 lines: zeros in every plane, two lines per
+    // aligned 16-byte store (lp is a multiple of 32, l0 of 16)
+    for (int e = threadIdx.x; e < SPEC_PLANE_M * (R16_LINES / 2); e += SPEC_THREADS) {
+      const int kz = e >> 3, c2 = (e & 7) * 2;
+      *reinterpret_cast<float4*>(pr.a + (size_t)kz * lp + l0 + c2) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    return;
+  }
+  {
+    const int j = threadIdx.x & 15, c = threadIdx.x >> 4, l = l0 + c;
+    const bool f1 = zf[0][c], f2 = zf[1][c];
+    const size_t o = (size_t)(l < nl ? l : 0) * P.g.zp;
+    float2 v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const int i = j + 16 * r;
+      v[r] = make_float2(0.0f, 0.0f);
+      if (r < 8 && i < nz) {
+        if (f1) v[r].x = __ldg(pr.t1 + o + i);
+        if (f2) v[r].y = __ldg(pr.t2 + o + i);
+      }
+    }
+    r16_first<false, true>(v, true, sm, j, c);
+  }
+  __syncthreads();
+  const int c = threadIdx.x & 15, j = threadIdx.x >> 4, l = l0 + c;
+  float2 v[16];
+  r16_second<false, true>(sm, v, j, c, P.g.tw[2]);
+  if (l < nl) {
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+      for (int k2 = 0; k2 < 4; ++k2) pr.a[(size_t)(j + 16 * (k1 + 4 * k2)) * lp + l] = v[4 * k1 + k2];
+  }
+}
+
+// z inverse from plane-major A: stage 1 with lanes across the 16 lines
+// (coalesced loads of one kz), stage 2 with lanes along z (coalesced dose
+// rows).
+__global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_inverse_plane_kernel(SpecLaunch P) {
+  extern __shared__ float2 spec_sm[];
+  float2* sm = spec_sm;
+  const SpecPair& pr = P.p[blockIdx.y];
+  const int nl = P.g.n[0] * P.g.n[1], nz = P.g.n[2], lp = P.g.lp;
+  const int l0 = blockIdx.x * R16_LINES;
+  {
+    const int c = threadIdx.x & 15, j = threadIdx.x >> 4, l = l0 + c;
+    float2 v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[r] = l < nl ? __ldg(pr.a + (size_t)(j + 16 * r) * lp + l) : make_float2(0.0f, 0.0f);
+    r16_first<true, true>(v, false, sm, j, c);
+  }
+  __syncthreads();
+  const int j = threadIdx.x & 15, c = threadIdx.x >> 4, l = l0 + c;
+  float2 v[16];
+  r16_second<true, true>(sm, v, j, c, P.g.tw[2]);
+  if (l < nl) {
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+      for (int k2 = 0; k2 < 2; ++k2) {
+        const int i = j + 16 * (k1 + 4 * k2);
+        if (i < nz) {
+          pr.d1[(size_t)l * nz + i] = v[4 * k1 + k2].x;
+          if (pr.d2) pr.d2[(size_t)l * nz + i] = v[4 * k1 + k2].y;
+        }
+      }
+  }
+}
+
+// ---- plane kernel helpers: one warp transforms two lines of 256 (lanes
+// 0-15 the first, 16-31 the second; lane j of a line holds butterfly j) with
+// an exchange buffer of its own, so only __syncwarp orders the two stages.
+// A 64-bit shared access is served per half warp, i.e. per line here: each
+// line has its own 256 elements, element i at i ^ ((i / 16) mod 16), so that
+// the stage-1 writes (rows 16 j + q) and the stage-2 reads (rows j + 16 r)
+// of a line's 16 lanes fall in 16 different banks.
+__device__ __forceinline__ int wx(int i, int c) { return c * 256 + (i ^ ((i >> 4) & 15)); }
+
+template <bool INV>
+__device__ __forceinline__ void w16_first(float2 (&v)[16], bool hin, float2* wb, int j, int c) {
+  if (hin)
+    dft16_half_in<INV>(v);
+  else
+    dft16<INV>(v);
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) wb[wx(16 * j + k1 + 4 * k2, c)] = v[4 * k1 + k2];
+}
+
+// stage 2 with the twiddles exp(-2 pi i r j / 256), r = 1..15, of butterfly
+// j from a shared table twj = tws + 16 j holding twiddle r at r ^ j (the 16
+// lanes of a line read 16 banks; every transform of the plane kernel has
+// period 256)
+template <bool INV>
+__device__ __forceinline__ void w16_second(const float2* wb, float2 (&v)[16], int j, int c, const float2* twj) {
+#pragma unroll
+  for (int r = 0; r < 16; ++r) v[r] = wb[wx(j + 16 * r, c)];
+#pragma unroll
+  for (int r = 1; r < 16; ++r) {
+    float2 w = twj[r ^ j];
+    if (INV) w.y = -w.y;
+    v[r] = cmul(v[r], w);
+  }
+  dft16<INV>(v);
+}
+
+// distributed shared memory: the partner CTA's copy of a shared address
+__device__ __forceinline__ uint32_t cluster_addr(const void* p, uint32_t rank) {
+  uint32_t out;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(out) : "r"((uint32_t)__cvta_generic_to_shared(p)),
+               "r"(rank));
+  return out;
+}
+__device__ __forceinline__ void st_cluster(uint32_t a, float2 v) {
+  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(a), "f"(v.x), "f"(v.y) : "memory");
+}
+__device__ __forceinline__ float2 ld_cluster(uint32_t a) {
+  float2 v;
+  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
+  return v;
+}
+// split cluster barrier: release/acquire where one CTA reads what the other
+// wrote, relaxed where it only orders running and exiting
+__device__ __forceinline__ void cluster_arrive_release() {
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// One kz plane of one beam pair per cluster of two CTAs.  CTA r of the
+// cluster holds the ky in [128 r, 128 r + 128) of the plane's spectrum,
+// Y[x][ky - 128 r] (x < nx <= 128; 128 KB), in its shared memory, element
+// (x, k) at x * 128 + (k ^ (x mod 16)) so that a row (lanes along ky) and a
+// column (lanes along x) are both conflict-free:
+//   1. y forward: CTA r transforms rows x in [64 r, 64 r + 64) of A (y < ny,
+//      the upper half zero) and stores each output ky into the CTA that
+//      holds it (its own shared memory or its partner's);
+//   2. per ky column of its half: x forward (x < nx), times S^[kz][ky][kx]
+//      (or its conjugate), x inverse (x < nx kept), in place;
+//   3. y inverse of its rows: the 256 ky of a row come half from each CTA;
+//      rows y < ny go back to A.
+// Every warp owns two lines at a time (rows in 1 and 3, columns in 2) with
+// its own exchange buffer, so warps never wait for each other inside a
+// phase.  The next pair's rows of A (phase 1) are loaded while the current
+// pair transforms, the S^ values of a column pair while its forward
+// transform runs.  Cluster barriers start the kernel (the partner is
+// running before its shared memory is written; waited on just before the
+// first stores), separate the phases (release/acquire) and end it (the
+// partner has read this CTA's half before it exits); every thread reaches
+// each of them once.  Consecutive clusters take the same kz of consecutive
+// pairs, so that plane of S^ comes from L2 after the first.
+constexpr int PLANE_THREADS = 512;
+constexpr int PLANE_WARPS = PLANE_THREADS / 32;
+static_assert(SPEC_PLANE_SMEM >= (128 * 128 + PLANE_WARPS * 2 * 256 + 256) * 8, "plane kernel shared memory");
+
+template <int R>
+__device__ __forceinline__ void plane_store_rows(float2* Y, uint32_t peer, int x, int jx, const float2 (&v)[16]) {
+  // outputs ky = j + 16 q, q = k1 + 4 k2: q < 8 in CTA 0, q >= 8 in CTA 1
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) {
+      const int off = x * 128 + jx + 16 * (k1 + 4 * (k2 & 1));
+      if ((k2 >> 1) == R)
+        Y[off] = v[4 * k1 + k2];
+      else
+        st_cluster(peer + 8u * (uint32_t)off, v[4 * k1 + k2]);
+    }
+}
+
+template <int R>
+__device__ __forceinline__ void plane_load_row(const float2* Y, uint32_t peer, int x, int jx, float2 (&v)[16]) {
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int off = x * 128 + jx + 16 * (q & 7);
+    v[q] = (q >> 3) == R ? Y[off] : ld_cluster(peer + 8u * (uint32_t)off);
+  }
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PLANE_THREADS, 1) spec_plane_kernel(SpecLaunch P) {
+  extern __shared__ float2 spec_sm[];
+  constexpr int H = SPEC_PLANE_M / 2;              // ky per CTA, and the largest nx
+  float2* const Y = spec_sm;                         // [H][H], swizzled
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = lane & 15, c = lane >> 4;            // butterfly, line of the warp
+  float2* const wb = spec_sm + H * H + warp * 2 * SPEC_PLANE_M;
+  const int r = (int)cluster_rank();
+  const uint32_t peer = cluster_addr(Y, (uint32_t)(r ^ 1));
+  const int nx = P.g.n[0], ny = P.g.n[1];
+  const float cs = P.g.conj ? -1.0f : 1.0f;
+  // stage-2 twiddles of every butterfly (period 256): [j][r ^ j]
+  float2* const tws = spec_sm + H * H + PLANE_WARPS * 2 * SPEC_PLANE_M;
+  if (threadIdx.x < 256) {
+    const int tj = threadIdx.x >> 4, tr = threadIdx.x & 15;
+    tws[16 * tj + (tr ^ tj)] = __ldg(P.g.tw[0] + tr * tj);
+  }
+  __syncthreads();
+  const float2* const tw = tws + 16 * j;
+  constexpr int ROWS = H / 2 / (2 * PLANE_WARPS);    // row pairs per warp in phases 1 and 3
+  constexpr int COLS = H / (2 * PLANE_WARPS);        // column pairs per warp in phase 2
+  const int pair = blockIdx.x >> 1, kz = blockIdx.y;
+  float2* const plane = P.p[pair].a + (size_t)kz * P.g.lp;
+  const float2* const sh = P.g.shat + (size_t)kz * SPEC_PLANE_M * SPEC_PLANE_M + (size_t)H * r * SPEC_PLANE_M;
+  auto row_of = [&](int it) { return (H / 2) * r + 2 * (PLANE_WARPS * it + warp) + c; };
+  auto load_a = [&](int it, float2 (&v)[8]) {        // rows of A: y < ny, the upper half zero
+    const int x = row_of(it);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int y = j + 16 * q;
+      v[q] = (x < nx && y < ny) ? __ldg(plane + (size_t)x * ny + y) : make_float2(0.0f, 0.0f);
+    }
+  };
+  auto col_of = [&](int it) { return 2 * (PLANE_WARPS * it + warp) + c; };
+
+  cluster_arrive_relaxed();
+  float2 pa[8];
+  load_a(0, pa);
+
+  // ---- 1. y forward
+  for (int it = 0; it < ROWS; ++it) {
+    const int x = row_of(it);
+    float2 v[16];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      v[q] = pa[q];
+      v[q + 8] = make_float2(0.0f, 0.0f);
+    }
+    if (it + 1 < ROWS) load_a(it + 1, pa);
+    w16_first<false>(v, true, wb, j, c);
+    __syncwarp();
+    w16_second<false>(wb, v, j, c, tw);
+    __syncwarp();
+    if (it == 0) cluster_wait();                      // the partner runs: its half may be written
+    if (x < nx) {
+      if (r == 0)
+        plane_store_rows<0>(Y, peer, x, j ^ (x & 15), v);
+      else
+        plane_store_rows<1>(Y, peer, x, j ^ (x & 15), v);
+    }
+  }
+  cluster_arrive_release();
+  cluster_wait();
+
+  // ---- 2. x forward, times S^, x inverse, on the CTA's ky columns
+  for (int it = 0; it < COLS; ++it) {
+    const int k = col_of(it);
+    float2 v[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int x = j + 16 * q;
+      v[q] = (q < 8 && x < nx) ? Y[x * H + (k ^ j)] : make_float2(0.0f, 0.0f);
+    }
+    float2 sv[16];                        // S^[kz][ky][kx = j + 16 q], in flight during the forward transform
+    {
+      const float2* row = sh + (size_t)k * SPEC_PLANE_M + j;
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        sv[q] = __ldg(row + 16 * q);
+        sv[q].y *= cs;
+      }
+    }
+    w16_first<false>(v, true, wb, j, c);
+    __syncwarp();
+    w16_second<false>(wb, v, j, c, tw);
+    __syncwarp();
+    float2 u[16];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+      for (int k2 = 0; k2 < 4; ++k2) u[k1 + 4 * k2] = cmul(v[4 * k1 + k2], sv[k1 + 4 * k2]);
+    w16_first<true>(u, false, wb, j, c);
+    __syncwarp();
+    w16_second<true>(wb, u, j, c, tw);
+    __syncwarp();
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+      for (int k2 = 0; k2 < 2; ++k2) {
+        const int x = j + 16 * (k1 + 4 * k2);
+        if (x < nx) Y[x * H + (k ^ j)] = u[4 * k1 + k2];
+      }
+  }
+  cluster_arrive_release();
+  cluster_wait();
+
+  // ---- 3. y inverse: the 256 ky of a row, half from each CTA
+  for (int it = 0; it < ROWS; ++it) {
+    const int x = row_of(it);
+    float2 v[16];
+    if (x < nx) {
+      if (r == 0)
+        plane_load_row<0>(Y, peer, x, j ^ (x & 15), v);
+      else
+        plane_load_row<1>(Y, peer, x, j ^ (x & 15), v);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 16; ++q) v[q] = make_float2(0.0f, 0.0f);
+    }
+    w16_first<true>(v, false, wb, j, c);
+    __syncwarp();
+    w16_second<true>(wb, v, j, c, tw);
+    __syncwarp();
+    if (x < nx) {
+#pragma unroll
+      for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+        for (int k2 = 0; k2 < 2; ++k2) {
+          const int y = j + 16 * (k1 + 4 * k2);
+          if (y < ny) plane[(size_t)x * ny + y] = v[4 * k1 + k2];
+        }
+    }
+  }
+  // the partner's loads of this CTA's half have all returned (their values
+  // were used above) before it arrives: relaxed suffices
+  cluster_arrive_relaxed();
+  cluster_wait();
+}
+
+// S^ [Mx][My][Mz] -> [Mz][My][Mx]: 32 x 32 (kx, kz) tiles through shared
+// memory, one ky per blockIdx.z
+__global__ void spec_transpose_kernel(const float2* __restrict__ in, float2* __restrict__ out, int Mx, int My,
+                                      int Mz) {
+  __shared__ float2 t[32][33];
+  const int ky = blockIdx.z, kx0 = blockIdx.y * 32, kz0 = blockIdx.x * 32;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int kx = kx0 + i, kz = kz0 + threadIdx.x;
+    if (kx < Mx && kz < Mz) t[i][threadIdx.x] = in[((size_t)kx * My + ky) * Mz + kz];
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int kz = kz0 + i, kx = kx0 + threadIdx.x;
+    if (kx < Mx && kz < Mz) out[((size_t)kz * My + ky) * Mx + kx] = t[threadIdx.x][i];
+  }
+}
+
 __global__ void spec_scatter_kernel(const long long* __restrict__ idx, const float* __restrict__ val, int n,
                                     float* __restrict__ S) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -783,6 +1158,12 @@ cudaError_t set_smem() {
 
 cudaError_t setup_spec_kernels() {
   cudaError_t e = set_smem<-1, -1>();
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(spec_z_forward_plane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(spec_z_inverse_plane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(spec_plane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_PLANE_SMEM);
 #define SPEC_SET(mp, ll) \
   if (e == cudaSuccess) e = set_smem<mp, ll>();
   SPEC_FOR_PERIODS(SPEC_SET)
@@ -792,9 +1173,22 @@ cudaError_t setup_spec_kernels() {
 
 // Each pass is launched specialised when (period, lines) is one of
 // SPEC_FOR_PERIODS, generic otherwise.
+void launch_spec_transpose(const float2* in, float2* out, int Mx, int My, int Mz, cudaStream_t st) {
+  spec_transpose_kernel<<<dim3((Mz + 31) / 32, (Mx + 31) / 32, My), dim3(32, 8), 0, st>>>(in, out, Mx, My, Mz);
+}
+
 void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
   const SpecGrid& g = L.g;
   const int nl = g.n[0] * g.n[1];
+  if (g.plane) {
+    const dim3 gz((nl + R16_LINES - 1) / R16_LINES, L.n_pairs);
+    spec_z_forward_plane_kernel<<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
+    // clusters of two along x: consecutive clusters take the same kz plane of
+    // consecutive pairs
+    spec_plane_kernel<<<dim3(2 * L.n_pairs, SPEC_PLANE_M), PLANE_THREADS, SPEC_PLANE_SMEM, st>>>(L);
+    spec_z_inverse_plane_kernel<<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
+    return;
+  }
   const int Lz = 1 << g.logL[2], Ly = 1 << g.logL[1], Lx = 1 << g.logL[0];
   const dim3 gz((nl + Lz - 1) / Lz, L.n_pairs), gy(g.n[0] * (g.M[2] / Ly), L.n_pairs);
   const unsigned gx = g.M[1] * (g.M[2] / Lx) * L.n_pairs;

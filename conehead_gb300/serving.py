@@ -51,7 +51,7 @@ class Request:
         self.beams = list(beams)
         self.settings = settings
         self.doses = [None] * len(self.beams)
-        self.t_submit = self.t_admit = self.t_done = None
+        self.t_submit = self.t_admit = self.t_launch = self.t_done = None
         self.error = None
         self.remaining = len(self.beams)
         self.reserved = 0
@@ -203,6 +203,10 @@ class DoseServer:
             if not self._fits(slot, wave):
                 self.ex.trim(slot)
             self.ex.launch(slot, wave)
+            now = self.clock()
+            for req, _ in wave:
+                if req.t_launch is None:
+                    req.t_launch = now
             self.busy[slot] = wave
             self.waves.append(len(wave))
 
@@ -225,11 +229,20 @@ class DoseServer:
             span = max(r.t_done for r in reqs) - min(r.t_submit for r in reqs)
         else:
             span = 0.0
+        # the slowest requests, split into waiting for memory (submit ->
+        # admit), waiting for a slot (admit -> first launch) and on the GPU
+        # (first launch -> done, the dose copy to the host included)
+        slow = sorted(reqs, key=lambda r: r.latency, reverse=True)[:3]
+        tail = [{"ms": 1e3 * r.latency, "phantom": r.phantom, "beams": len(r.beams),
+                 "admit_ms": 1e3 * (r.t_admit - r.t_submit),
+                 "to_launch_ms": 1e3 * (r.t_launch - r.t_admit) if r.t_launch is not None else None,
+                 "on_gpu_ms": 1e3 * (r.t_done - r.t_launch) if r.t_launch is not None else None}
+                for r in slow]
         return {"requests": len(reqs), "beams": beams,
                 "p50_ms": _percentile(lat, 50), "p99_ms": _percentile(lat, 99),
                 "beams_per_s": beams / span if span > 0 else None,
                 "mean_batch_beams": float(np.mean(self.waves)) if self.waves else None,
-                "peak_bytes": self.peak_used, "budget_bytes": self.budget}
+                "peak_bytes": self.peak_used, "budget_bytes": self.budget, "slowest": tail}
 
 
 class GpuExecutor:
