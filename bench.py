@@ -47,6 +47,7 @@ batches (weak scaling, no data-path collective); the step time is the
 maximum over ranks.
 """
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -242,6 +243,10 @@ def serving_extras(args, dev):
     for n in sizes:
         ex.add_phantom(f"p{n}", workload(n, args.spacing, seed=n))
     ex.prepare(SETTINGS, (args.spacing,) * 3, (max(sizes),) * 3)
+    # every slot's arena at its full pool, every shape's kernels and pinned
+    # host buffers allocated: no request pays a first-use cost
+    if not args.serve_no_warm:
+        ex.warm(SETTINGS, args.serve_batch)
     budget = int(0.8 * torch.cuda.mem_get_info(dev)[1])
     names = [f"p{n}" for n in sizes]
 
@@ -252,18 +257,32 @@ def serving_extras(args, dev):
     # warm-up (pinned host buffers, lazy CUDA state), not reported
     arr, specs = poisson_workload(np.random.default_rng(99), names, 400.0, 24)
     drive(DoseServer(ex, budget, max_wave_beams=args.serve_batch), arr, specs, SETTINGS, on_done=drop)
+    # a long-running server collects once after start-up and freezes what it
+    # holds: otherwise a cyclic-GC pass over the objects of this process
+    # (every earlier section's beams and jobs) stalls the scheduler loop for
+    # tens of milliseconds in the middle of the timed rates
+    gc.collect()
+    gc.freeze()
     rows = []
     for rate in args.serve_rates:
         rng = np.random.default_rng(int(rate))
         arr, specs = poisson_workload(rng, names, float(rate), args.serve_requests)
         server = DoseServer(ex, budget, max_wave_beams=args.serve_batch)
+        ex.batch_log.clear()
         drive(server, arr, specs, SETTINGS, on_done=drop)
         st = server.stats()
+        blog = ex.batch_log
+        batches = {"n": len(blog),
+                   "host_ms_median": statistics.median(b["host_ms"] for b in blog) if blog else None,
+                   "device_ms_median": statistics.median(b["device_ms"] for b in blog) if blog else None,
+                   "copy_ms_median": statistics.median(b["copy_ms"] for b in blog) if blog else None,
+                   "slowest": sorted(blog, key=lambda b: -(b["device_ms"] + b["copy_ms"]))[:3]}
         rows.append({"rate_req_s": rate, "requests": st["requests"], "beams": st["beams"],
                      "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "beams_per_s": st["beams_per_s"],
                      "mean_batch_beams": st["mean_batch_beams"], "peak_gb": st["peak_bytes"] / 1e9,
-                     "slowest": st["slowest"]})
+                     "slowest": st["slowest"], "batches": batches})
     ex.close()
+    gc.unfreeze()
     return {"workload": "Poisson arrivals, 1-8 beams per request (5x5 cm, gantry U[0,360)), phantoms "
                         "64^3/96^3/128^3/192^3 @ 0.25 cm resident, 2 slots, latency = arrival to dose "
                         "in pinned host memory",
@@ -786,6 +805,7 @@ def main(argv=None):
     ap.add_argument("--serve-requests", type=int, default=100, help="requests per serving rate (0: skip)")
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 200.0, 2000.0])
     ap.add_argument("--serve-batch", type=int, default=32, help="beams per serving batch at most")
+    ap.add_argument("--serve-no-warm", action="store_true", help="skip the serving executor's warm-up")
     ap.add_argument("--adjoint-iters", type=int, default=5, help="timed gradient evaluations (0: skip)")
     ap.add_argument("--batch-beams", type=int, default=64, help="beams of the captured mixed batch (0: skip)")
     ap.add_argument("--batch-iters", type=int, default=5)

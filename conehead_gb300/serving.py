@@ -31,6 +31,13 @@ mix, up to the float rounding of the dose accumulation order.
 ``DoseServer`` talks to an executor through a small interface, so its
 admission and batching logic runs on the CPU in tests with a simulated
 executor; ``GpuExecutor`` is the real one.
+
+Latency in practice: call ``GpuExecutor.warm`` once after ``prepare`` (no
+request then pays for growing a slot's scratch arena -- cudaFree waits for
+the whole device -- or for a first pinned host allocation), and have a
+long-running server process ``gc.collect(); gc.freeze()`` after start-up,
+so that the cyclic garbage collector does not walk every object the process
+holds while requests are in flight.
 """
 import time
 import types
@@ -264,6 +271,7 @@ class GpuExecutor:
                 e.set_tuning(**tuning)      # the cone/TERMA schedule (conehead_gb300.autotune)
         self.streams = [torch.cuda.Stream(self.device) for _ in range(n_slots)]
         self.events = [None] * n_slots
+        self.batch_log = []
         self.n_slots = n_slots
         self.copy_to_host = copy_to_host
         self.phantoms = {}
@@ -291,6 +299,41 @@ class GpuExecutor:
                     g = N.grid_struct(shape, (0.0, 0.0, 0.0), spacing)
                     N.check(eng.L.ch_plan_prepare(eng.plan, ctypes.byref(g), eng.stream()), "ch_plan_prepare")
         self.torch.cuda.synchronize(self.device)
+
+    def warm(self, settings, max_wave_beams, pinned_per_shape=None):
+        """Take every first-use cost out of serving: each slot runs one full
+        batch of ``max_wave_beams`` beams on the largest registered phantom
+        (its scratch arena grows to the pool a server with that batch cap
+        charges, so no later batch allocates -- a growth frees the old arena,
+        and cudaFree waits for the whole device) and one beam on every other
+        phantom (every grid shape's kernels), and the pinned host buffers the
+        doses are copied into are allocated once for every phantom shape and
+        returned to torch's host cache (a first cudaHostAlloc of tens of MB
+        takes milliseconds)."""
+        from .block import Block
+        from .source import Source
+        torch = self.torch
+        src = Source()
+        src.gantry = 0.0
+        src.collimator = 0.0
+        blk = Block()
+        blk.set_square(5.0)
+        names = sorted(self.phantoms, key=lambda k: -int(np.prod(self.phantoms[k][0].size)))
+        for slot, eng in enumerate(self.engines):
+            with torch.cuda.stream(self.streams[slot]):
+                eng.set_kernel(settings["energy_weights"])
+                for i, name in enumerate(names):
+                    ph, rho = self.phantoms[name]
+                    n = max_wave_beams if i == 0 else 1
+                    jobs = [eng.job(ph, rho, src, eng.block_for(blk), settings) for _ in range(n)]
+                    eng.run_batch(jobs)
+                    eng.sync()
+        k = pinned_per_shape if pinned_per_shape is not None else self.n_slots * max_wave_beams
+        for name in names:
+            shape = tuple(int(n) for n in self.phantoms[name][0].size)
+            bufs = [torch.empty(shape, dtype=torch.float32, pin_memory=True) for _ in range(k)]
+            del bufs
+        torch.cuda.synchronize(self.device)
 
     # ------------------------------------------------------- accounting --
     def _plan_memory(self, eng):
@@ -346,7 +389,10 @@ class GpuExecutor:
     def launch(self, slot, items):
         torch = self.torch
         eng, st = self.engines[slot], self.streams[slot]
+        t0 = time.perf_counter()
         with torch.cuda.stream(st):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
             eng.set_kernel(items[0][0].settings["energy_weights"])
             jobs = []
             for req, b in items:
@@ -355,6 +401,8 @@ class GpuExecutor:
                 dose = torch.empty(tuple(int(n) for n in ph.size), dtype=torch.float32, device=self.device)
                 jobs.append(eng.job(ph, rho, src, eng.block_for(blk), req.settings, dose=dose))
             eng.run_batch(jobs)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e1.record(st)
             for (req, b), job in zip(items, jobs):
                 if self.copy_to_host:
                     host = torch.empty(job.dose.shape, dtype=torch.float32, pin_memory=True)
@@ -362,9 +410,10 @@ class GpuExecutor:
                     req.doses[b] = host
                 else:
                     req.doses[b] = job.dose
-            ev = torch.cuda.Event()
+            ev = torch.cuda.Event(enable_timing=True)
             ev.record(st)
-        self.events[slot] = (ev, jobs)
+        self.events[slot] = (ev, jobs, e0, e1, time.perf_counter() - t0,
+                             sorted({self.phantoms[r.phantom][0].size[0] for r, _ in items}), len(items))
 
     def done(self, slot):
         ev = self.events[slot]
@@ -372,6 +421,12 @@ class GpuExecutor:
 
     def collect(self, slot):
         eng = self.engines[slot]
+        ev, _, e0, e1, host_s, sizes, n = self.events[slot]
+        # per batch: host time of the launch call, device time of the dose
+        # calculation and of the copies to the host (stream-ordered events, so
+        # the time includes waiting for the other slot's work on the GPU)
+        self.batch_log.append({"slot": slot, "beams": n, "grids": sizes, "host_ms": 1e3 * host_s,
+                               "device_ms": e0.elapsed_time(e1), "copy_ms": e1.elapsed_time(ev)})
         self.events[slot] = None
         with self.torch.cuda.stream(self.streams[slot]):
             eng.sync()                      # the stream is idle: reads the device error flags
