@@ -886,8 +886,9 @@ __device__ __forceinline__ uint32_t cluster_rank() {
 // (x, k) at x * 128 + (k ^ (x mod 16)) so that a row (lanes along ky) and a
 // column (lanes along x) are both conflict-free:
 //   1. y forward: CTA r transforms rows x in [64 r, 64 r + 64) of A (y < ny,
-//      the upper half zero) and stores each output ky into the CTA that
-//      holds it (its own shared memory or its partner's);
+//      the upper half zero; rows without TERMA in either beam skip the
+//      transform) and stores each output ky into the CTA that holds it (its
+//      own shared memory or its partner's);
 //   2. per ky column of its half: x forward (x < nx), times S^[kz][ky][kx]
 //      (or its conjugate), x inverse (x < nx kept), in place;
 //   3. y inverse of its rows: the 256 ky of a row come half from each CTA;
@@ -979,10 +980,17 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PLANE_THREADS, 1) sp
       v[q + 8] = make_float2(0.0f, 0.0f);
     }
     if (it + 1 < ROWS) load_a(it + 1, pa);
-    w16_first<false>(v, true, wb, j, c);
-    __syncwarp();
-    w16_second<false>(wb, v, j, c, tw);
-    __syncwarp();
+    // two rows without TERMA in either beam (a beam lights a band of the
+    // plane): their spectra are zero, the transform is skipped
+    bool nz = false;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) nz = nz || v[q].x != 0.0f || v[q].y != 0.0f;
+    if (__any_sync(0xffffffffu, nz)) {
+      w16_first<false>(v, true, wb, j, c);
+      __syncwarp();
+      w16_second<false>(wb, v, j, c, tw);
+      __syncwarp();
+    }
     if (it == 0) cluster_wait();                      // the partner runs: its half may be written
     if (x < nx) {
       if (r == 0)
