@@ -279,7 +279,7 @@ void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st);
 // inverse from A.  S^ is then kept as [Mz][My][Mx].
 constexpr int SPEC_PLANE_M = 256;
 // half the plane spectrum, an exchange buffer per warp, the twiddle table
-constexpr int SPEC_PLANE_SMEM = (128 * 128 + 16 * 2 * 256 + 256) * 8;
+constexpr int SPEC_PLANE_SMEM = (128 * 128 + 16 * 2 * 256 + 16 * 18) * 8;
 inline bool spec_plane_path(const int* M) {
   return M[0] == SPEC_PLANE_M && M[1] == SPEC_PLANE_M && M[2] == SPEC_PLANE_M;
 }

@@ -833,19 +833,22 @@ __device__ __forceinline__ void w16_first(float2 (&v)[16], bool hin, float2* wb,
     for (int k2 = 0; k2 < 4; ++k2) wb[wx(16 * j + k1 + 4 * k2, c)] = v[4 * k1 + k2];
 }
 
-// stage 2 with the twiddles exp(-2 pi i r j / 256), r = 1..15, of butterfly
-// j from a shared table twj = tws + 16 j holding twiddle r at r ^ j (the 16
-// lanes of a line read 16 banks; every transform of the plane kernel has
-// period 256)
+// stage 2 with the twiddles exp(-2 pi i r j / 256), r = 0..15, of butterfly
+// j from a shared table row twj = tws + 18 j (rows padded to 144 bytes), two
+// twiddles per 16-byte load: the 16 lanes of a line then read 8 distinct
+// 16-byte bank groups, two wavefronts, the minimum for 256 bytes (every
+// transform of the plane kernel has period 256)
+constexpr int PLANE_TW_ROW = 18;
 template <bool INV>
 __device__ __forceinline__ void w16_second(const float2* wb, float2 (&v)[16], int j, int c, const float2* twj) {
 #pragma unroll
   for (int r = 0; r < 16; ++r) v[r] = wb[wx(j + 16 * r, c)];
+  const float4* tw4 = reinterpret_cast<const float4*>(twj);
 #pragma unroll
-  for (int r = 1; r < 16; ++r) {
-    float2 w = twj[r ^ j];
-    if (INV) w.y = -w.y;
-    v[r] = cmul(v[r], w);
+  for (int m = 0; m < 8; ++m) {
+    const float4 t = tw4[m];
+    if (m > 0) v[2 * m] = cmul(v[2 * m], make_float2(t.x, INV ? -t.y : t.y));
+    v[2 * m + 1] = cmul(v[2 * m + 1], make_float2(t.z, INV ? -t.w : t.w));
   }
   dft16<INV>(v);
 }
@@ -905,7 +908,8 @@ __device__ __forceinline__ uint32_t cluster_rank() {
 // pairs, so that plane of S^ comes from L2 after the first.
 constexpr int PLANE_THREADS = 512;
 constexpr int PLANE_WARPS = PLANE_THREADS / 32;
-static_assert(SPEC_PLANE_SMEM >= (128 * 128 + PLANE_WARPS * 2 * 256 + 256) * 8, "plane kernel shared memory");
+static_assert(SPEC_PLANE_SMEM >= (128 * 128 + PLANE_WARPS * 2 * 256 + 16 * PLANE_TW_ROW) * 8,
+              "plane kernel shared memory");
 
 template <int R>
 __device__ __forceinline__ void plane_store_rows(float2* Y, uint32_t peer, int x, int jx, const float2 (&v)[16]) {
@@ -942,14 +946,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PLANE_THREADS, 1) sp
   const uint32_t peer = cluster_addr(Y, (uint32_t)(r ^ 1));
   const int nx = P.g.n[0], ny = P.g.n[1];
   const float cs = P.g.conj ? -1.0f : 1.0f;
-  // stage-2 twiddles of every butterfly (period 256): [j][r ^ j]
+  // stage-2 twiddles of every butterfly (period 256): [j][r], rows of 18
   float2* const tws = spec_sm + H * H + PLANE_WARPS * 2 * SPEC_PLANE_M;
   if (threadIdx.x < 256) {
     const int tj = threadIdx.x >> 4, tr = threadIdx.x & 15;
-    tws[16 * tj + (tr ^ tj)] = __ldg(P.g.tw[0] + tr * tj);
+    tws[PLANE_TW_ROW * tj + tr] = __ldg(P.g.tw[0] + tr * tj);
   }
   __syncthreads();
-  const float2* const tw = tws + 16 * j;
+  const float2* const tw = tws + PLANE_TW_ROW * j;
   constexpr int ROWS = H / 2 / (2 * PLANE_WARPS);    // row pairs per warp in phases 1 and 3
   constexpr int COLS = H / (2 * PLANE_WARPS);        // column pairs per warp in phase 2
   const int pair = blockIdx.x >> 1, kz = blockIdx.y;
