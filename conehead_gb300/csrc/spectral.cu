@@ -714,6 +714,14 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_inverse
 }
 
 // ------------------------------------------------------------ plane path --
+// The z passes of the plane path use one exchange buffer (16 lines of 256)
+// and run more CTAs per SM than the five-pass kernels: more loads and
+// stores in flight in passes that stream A (measured per 16 pairs at 128^3:
+// z forward 137 / 117 / 104 / 102 us at 3 / 4 / 5 / 6 CTAs per SM, z
+// inverse 155 / 149 / 153 / 187 us).
+constexpr int SPEC_ZFWD_CTAS_PER_SM = 5;
+constexpr int SPEC_ZINV_CTAS_PER_SM = 4;
+constexpr int SPEC_ZPLANE_SMEM = R16_LINES * 256 * 8;
 // Periods of 256 on all three axes.  The y and x transforms of one kz plane
 // (with the S^ product and both inverses) run in one kernel on the plane's
 // spectrum held on chip, so the intermediate B [nx][My][Mz] of the five-pass
@@ -725,7 +733,7 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_inverse
 // of 16 consecutive lines is one 128-byte store).  Both stages address the
 // exchange buffer with the z layout swz16<true>; either lane mapping reads
 // or writes 16 distinct banks per half warp there.
-__global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward_plane_kernel(SpecLaunch P) {
+__global__ void __launch_bounds__(SPEC_THREADS, SPEC_ZFWD_CTAS_PER_SM) spec_z_forward_plane_kernel(SpecLaunch P) {
   extern __shared__ float2 spec_sm[];
   float2* sm = spec_sm;
   const SpecPair& pr = P.p[blockIdx.y];
@@ -781,7 +789,7 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward
 // z inverse from plane-major A: stage 1 with lanes across the 16 lines
 // (coalesced loads of one kz), stage 2 with lanes along z (coalesced dose
 // rows).
-__global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_inverse_plane_kernel(SpecLaunch P) {
+__global__ void __launch_bounds__(SPEC_THREADS, SPEC_ZINV_CTAS_PER_SM) spec_z_inverse_plane_kernel(SpecLaunch P) {
   extern __shared__ float2 spec_sm[];
   float2* sm = spec_sm;
   const SpecPair& pr = P.p[blockIdx.y];
@@ -1171,9 +1179,9 @@ cudaError_t set_smem() {
 cudaError_t setup_spec_kernels() {
   cudaError_t e = set_smem<-1, -1>();
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(spec_z_forward_plane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_SMEM);
+    e = cudaFuncSetAttribute(spec_z_forward_plane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_ZPLANE_SMEM);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(spec_z_inverse_plane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_SMEM);
+    e = cudaFuncSetAttribute(spec_z_inverse_plane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_ZPLANE_SMEM);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(spec_plane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_PLANE_SMEM);
 #define SPEC_SET(mp, ll) \
@@ -1194,11 +1202,11 @@ void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
   const int nl = g.n[0] * g.n[1];
   if (g.plane) {
     const dim3 gz((nl + R16_LINES - 1) / R16_LINES, L.n_pairs);
-    spec_z_forward_plane_kernel<<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
+    spec_z_forward_plane_kernel<<<gz, SPEC_THREADS, SPEC_ZPLANE_SMEM, st>>>(L);
     // clusters of two along x: consecutive clusters take the same kz plane of
     // consecutive pairs
     spec_plane_kernel<<<dim3(2 * L.n_pairs, SPEC_PLANE_M), PLANE_THREADS, SPEC_PLANE_SMEM, st>>>(L);
-    spec_z_inverse_plane_kernel<<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
+    spec_z_inverse_plane_kernel<<<gz, SPEC_THREADS, SPEC_ZPLANE_SMEM, st>>>(L);
     return;
   }
   const int Lz = 1 << g.logL[2], Ly = 1 << g.logL[1], Lx = 1 << g.logL[0];
