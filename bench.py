@@ -47,6 +47,7 @@ batches (weak scaling, no data-path collective); the step time is the
 maximum over ranks.
 """
 import argparse
+import contextlib
 import gc
 import json
 import os
@@ -74,7 +75,23 @@ SETTINGS = {
 }
 
 
+@contextlib.contextmanager
+def quiet_gc():
+    """Collect once, then keep Python's cyclic collector out of a timed loop
+    whose window includes the host enqueueing the steps: a pass over this
+    process's objects can stall that thread for tens of milliseconds."""
+    gc.collect()
+    gc.freeze()
+    gc.disable()
+    try:
+        yield
+    finally:
+        gc.enable()
+        gc.unfreeze()
+
+
 # ----------------------------------------------------------- distribution --
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -668,15 +685,17 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    # e0 is recorded on the compute stream before the first upload is issued
-    e0.record(st)
-    in_st.wait_event(e0)
-    run_steps(args.warmup, args.steps)
-    for ev in copied:
-        if ev is not None:
-            st.wait_event(ev)
-    e1.record(st)
-    e1.synchronize()
+    # the window spans host enqueueing: the cyclic collector stays out of it
+    with quiet_gc():
+        # e0 is recorded on the compute stream before the first upload is issued
+        e0.record(st)
+        in_st.wait_event(e0)
+        run_steps(args.warmup, args.steps)
+        for ev in copied:
+            if ev is not None:
+                st.wait_event(ev)
+        e1.record(st)
+        e1.synchronize()
     eng.sync()
     e2e_s = max_over_ranks(e0.elapsed_time(e1) / 1000.0, dev)
     h2d = h_rho.numel() * 4 + sum(h.numel() * 4 for h in h_blocks.values())
