@@ -130,17 +130,24 @@ def beam_seed(rank, index):
 
 # ------------------------------------------------------------------ clocks --
 class ClockSampler:
+    """nvidia-smi samples (every 20 ms) of the SM clock, its maximum, power and
+    the throttle reasons.  Started before the timed loops and waited on until
+    its first sample arrives (nvidia-smi takes a while to start); the timed
+    loops mark their windows with begin() / end(), and stop() summarises the
+    samples that arrived inside a window."""
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index):
         self.index = index
-        self.samples = []
+        self.samples = []      # (arrival time, fields)
+        self.windows = []
         self.proc = None
         self.thread = None
+        self.first = threading.Event()
 
-    def start(self):
+    def start(self, wait_s=5.0):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
@@ -151,14 +158,23 @@ class ClockSampler:
             return
         self.thread = threading.Thread(target=self._read, daemon=True)
         self.thread.start()
+        self.first.wait(wait_s)
 
     def _read(self):
         for line in self.proc.stdout:
-            self.samples.append([p.strip() for p in line.split(",")])
+            self.samples.append((time.monotonic(), [p.strip() for p in line.split(",")]))
+            self.first.set()
+
+    def begin(self):
+        self.windows.append([time.monotonic(), None])
+
+    def end(self):
+        if self.windows and self.windows[-1][1] is None:
+            self.windows[-1][1] = time.monotonic()
 
     def stop(self):
         if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+            return self.summary()
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -166,14 +182,26 @@ class ClockSampler:
             self.proc.kill()
         if self.thread:
             self.thread.join(timeout=2)
-        sm = [float(s[0]) for s in self.samples if s and s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if len(s) > 1 and s[1].replace(".", "").isdigit()]
+        return self.summary()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        samples = list(self.samples)
+        inside = [f for t, f in samples
+                  if any(a <= t <= (b if b is not None else float("inf")) for a, b in self.windows)]
+        rows = inside or [f for _, f in samples]
+        sm = [float(r[0]) for r in rows if r and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if len(r) > 1 and r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4)
-                          if len(s) > 3 + i and s[3 + i].lower() == "active"})
+        reasons = sorted({names[i] for r in rows for i in range(4)
+                          if len(r) > 3 + i and r[3 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(inside),
+                "windows_ms": [round((b - a) * 1e3, 1) for a, b in self.windows if b is not None],
+                "basis": "samples inside the timed windows (device-timed loop and e2e loop)"
+                         if inside else "no sample inside the timed windows: every sample of the run"}
 
 
 # --------------------------------------------------------------- workload --
@@ -543,8 +571,7 @@ def run_ours(args):
     # The host enqueues step s + 1 (building its jobs and launch records)
     # while the device runs step s, as a batch loop does; each step's window
     # runs from after its L2 flush to the end of its batch, so the flushes are
-    # outside and no host preparation leaves the device idle inside.  The
-    # library's stage events are those of the last timed step.
+    # outside and no host preparation leaves the device idle inside.
     # (job descriptors are host objects, built before the timed loop as the
     # e2e loop builds its sets' once; each call still stages its own launch
     # records)
@@ -554,20 +581,30 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     clocks.start()
     marks = []
-    for s in range(args.warmup, args.warmup + args.steps):
-        jobs = timed_jobs[s]
-        flush.fill_(float(s))
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        eng.run_batch(jobs)
-        e1.record(st)
-        marks.append((e0, e1))
-    torch.cuda.synchronize(dev)
+    with quiet_gc():
+        clocks.begin()
+        for s in range(args.warmup, args.warmup + args.steps):
+            jobs = timed_jobs[s]
+            flush.fill_(float(s))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            eng.run_batch(jobs)
+            e1.record(st)
+            marks.append((e0, e1))
+        torch.cuda.synchronize(dev)
+        clocks.end()
     barrier()
-    clk = clocks.stop()
     eng.sync()
     step_ms = [a.elapsed_time(b) for a, b in marks]
-    stats = [eng.stats()]
+    # Stage times (prologue, cone stage) from the library's events, which
+    # hold one call's: the timed steps replayed one at a time after the timed
+    # loop, same jobs and flushes, each call's events read before the next.
+    stats = []
+    for s in range(args.warmup, args.warmup + args.steps):
+        flush.fill_(float(s))
+        eng.run_batch(timed_jobs[s])
+        eng.sync()
+        stats.append(eng.stats())
     local_s = sum(step_ms) / 1000.0
     job_s = max_over_ranks(local_s, dev)
     value = world * args.steps * B / job_s
@@ -605,7 +642,7 @@ def run_ours(args):
         if tr.get("dram_bytes_per_beam"):
             traffic = tr["dram_bytes_per_beam"] * B
     props = torch.cuda.get_device_properties(dev)
-    sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    sm_mhz = clocks.summary().get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     onchip = None
     if method == "gather":
         lds_ceiling = props.multi_processor_count * 32 * sm_mhz * 1e6     # one 4-byte LDS lane per update
@@ -687,6 +724,7 @@ def run_ours(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     # the window spans host enqueueing: the cyclic collector stays out of it
     with quiet_gc():
+        clocks.begin()
         # e0 is recorded on the compute stream before the first upload is issued
         e0.record(st)
         in_st.wait_event(e0)
@@ -696,6 +734,8 @@ def run_ours(args):
                 st.wait_event(ev)
         e1.record(st)
         e1.synchronize()
+        clocks.end()
+    clk = clocks.stop()
     eng.sync()
     e2e_s = max_over_ranks(e0.elapsed_time(e1) / 1000.0, dev)
     h2d = h_rho.numel() * 4 + sum(h.numel() * 4 for h in h_blocks.values())
