@@ -412,11 +412,25 @@ __device__ __forceinline__ void store_lines(const float2* res, float2* __restric
 // L M <= 4096 for lines along z; lines along y and x are taken in blocks of L
 // consecutive kz, so L also divides Mz.
 // z forward: lines (x, y), TERMA pair in, A out.  One CTA per L lines and pair.
+// Shared memory of a five-pass kernel: two buffers of its CTA's lines.  A
+// compile-time period and line count take only what they use, so periods
+// 96, 192 and 384 (3072 values per CTA, 48 KB) run four CTAs per SM, the
+// others (4096 values, 64 KB) three.
 template <int MP, int LL>
-__global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward_kernel(SpecLaunch P) {
+constexpr int spec_elems() {
+  static_assert(MP <= 0 || (MP << LL) <= SPEC_ELEMS, "lines of a CTA");
+  return MP > 0 ? (MP << LL) : SPEC_ELEMS;
+}
+template <int MP, int LL>
+constexpr int spec_smem() { return 2 * spec_elems<MP, LL>() * 8; }
+template <int MP, int LL>
+constexpr int spec_ctas() { return spec_smem<MP, LL>() <= 48 * 1024 ? 4 : SPEC_CTAS_PER_SM; }
+
+template <int MP, int LL>
+__global__ void __launch_bounds__(SPEC_THREADS, spec_ctas<MP, LL>()) spec_z_forward_kernel(SpecLaunch P) {
   extern __shared__ float2 spec_sm[];
   float2* sm = spec_sm;
-  float2* sm2 = spec_sm + SPEC_ELEMS;
+  float2* sm2 = spec_sm + spec_elems<MP, LL>();
   const SpecPair& pr = P.p[blockIdx.y];
   const int Mz = MP > 0 ? MP : P.g.M[2];
   const int logL = MP > 0 ? LL : P.g.logL[2], L = 1 << logL;
@@ -503,10 +517,10 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_forward
 
 // y forward (A -> B) or inverse (B -> A): lines (x, kz) in blocks of L kz.
 template <bool INV, int MP, int LL>
-__global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_y_kernel(SpecLaunch P) {
+__global__ void __launch_bounds__(SPEC_THREADS, spec_ctas<MP, LL>()) spec_y_kernel(SpecLaunch P) {
   extern __shared__ float2 spec_sm[];
   float2* sm = spec_sm;
-  float2* sm2 = spec_sm + SPEC_ELEMS;
+  float2* sm2 = spec_sm + spec_elems<MP, LL>();
   const SpecPair& pr = P.p[blockIdx.y];
   const int My = MP > 0 ? MP : P.g.M[1], Mz = P.g.M[2];
   const int logL = MP > 0 ? LL : P.g.logL[1], L = 1 << logL;
@@ -556,10 +570,10 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_y_kernel(
 // CONV: forward, times S^ (or its conjugate), inverse, x < nx kept;
 // otherwise forward only over the full period (building S^).
 template <bool CONV, int MP, int LL>
-__global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(SpecLaunch P) {
+__global__ void __launch_bounds__(SPEC_THREADS, spec_ctas<MP, LL>()) spec_x_kernel(SpecLaunch P) {
   extern __shared__ float2 spec_sm[];
   float2* sm = spec_sm;
-  float2* sm2 = spec_sm + SPEC_ELEMS;
+  float2* sm2 = spec_sm + spec_elems<MP, LL>();
   const int pair = blockIdx.x % P.n_pairs, blk = blockIdx.x / P.n_pairs;
   const SpecPair& pr = P.p[pair];
   const int Mx = MP > 0 ? MP : P.g.M[0], My = P.g.M[1], Mz = P.g.M[2];
@@ -652,10 +666,10 @@ __global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_x_kernel(
 
 // z inverse: lines (x, y), A in, dose pair out (real part, imaginary part).
 template <int MP, int LL>
-__global__ void __launch_bounds__(SPEC_THREADS, SPEC_CTAS_PER_SM) spec_z_inverse_kernel(SpecLaunch P) {
+__global__ void __launch_bounds__(SPEC_THREADS, spec_ctas<MP, LL>()) spec_z_inverse_kernel(SpecLaunch P) {
   extern __shared__ float2 spec_sm[];
   float2* sm = spec_sm;
-  float2* sm2 = spec_sm + SPEC_ELEMS;
+  float2* sm2 = spec_sm + spec_elems<MP, LL>();
   const SpecPair& pr = P.p[blockIdx.y];
   const int Mz = MP > 0 ? MP : P.g.M[2];
   const int logL = MP > 0 ? LL : P.g.logL[2], L = 1 << logL;
@@ -1172,7 +1186,7 @@ cudaError_t set_smem() {
   for (const void* f : {(const void*)spec_z_forward_kernel<MP, LL>, (const void*)spec_y_kernel<false, MP, LL>,
                         (const void*)spec_y_kernel<true, MP, LL>, (const void*)spec_x_kernel<false, MP, LL>,
                         (const void*)spec_x_kernel<true, MP, LL>, (const void*)spec_z_inverse_kernel<MP, LL>})
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_SMEM);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, spec_smem<MP, LL>());
   return e;
 }
 
@@ -1214,11 +1228,11 @@ void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
   const unsigned gx = g.M[1] * (g.M[2] / Lx) * L.n_pairs;
   bool z_done = false, y_done = false, x_done = false;
 #define SPEC_Z(mp, ll) \
-  if (!z_done && g.M[2] == mp && g.logL[2] == ll) { spec_z_forward_kernel<mp, ll><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L); z_done = true; }
+  if (!z_done && g.M[2] == mp && g.logL[2] == ll) { spec_z_forward_kernel<mp, ll><<<gz, SPEC_THREADS, (spec_smem<mp, ll>()), st>>>(L); z_done = true; }
 #define SPEC_Y(mp, ll) \
-  if (!y_done && g.M[1] == mp && g.logL[1] == ll) { spec_y_kernel<false, mp, ll><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L); y_done = true; }
+  if (!y_done && g.M[1] == mp && g.logL[1] == ll) { spec_y_kernel<false, mp, ll><<<gy, SPEC_THREADS, (spec_smem<mp, ll>()), st>>>(L); y_done = true; }
 #define SPEC_X(mp, ll) \
-  if (!x_done && g.M[0] == mp && g.logL[0] == ll) { spec_x_kernel<true, mp, ll><<<gx, SPEC_THREADS, SPEC_SMEM, st>>>(L); x_done = true; }
+  if (!x_done && g.M[0] == mp && g.logL[0] == ll) { spec_x_kernel<true, mp, ll><<<gx, SPEC_THREADS, (spec_smem<mp, ll>()), st>>>(L); x_done = true; }
   SPEC_FOR_PERIODS(SPEC_Z)
   if (!z_done) spec_z_forward_kernel<-1, -1><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
   SPEC_FOR_PERIODS(SPEC_Y)
@@ -1230,9 +1244,9 @@ void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
 #undef SPEC_X
   y_done = z_done = false;
 #define SPEC_YI(mp, ll) \
-  if (!y_done && g.M[1] == mp && g.logL[1] == ll) { spec_y_kernel<true, mp, ll><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L); y_done = true; }
+  if (!y_done && g.M[1] == mp && g.logL[1] == ll) { spec_y_kernel<true, mp, ll><<<gy, SPEC_THREADS, (spec_smem<mp, ll>()), st>>>(L); y_done = true; }
 #define SPEC_ZI(mp, ll) \
-  if (!z_done && g.M[2] == mp && g.logL[2] == ll) { spec_z_inverse_kernel<mp, ll><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L); z_done = true; }
+  if (!z_done && g.M[2] == mp && g.logL[2] == ll) { spec_z_inverse_kernel<mp, ll><<<gz, SPEC_THREADS, (spec_smem<mp, ll>()), st>>>(L); z_done = true; }
   SPEC_FOR_PERIODS(SPEC_YI)
   if (!y_done) spec_y_kernel<true, -1, -1><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L);
   SPEC_FOR_PERIODS(SPEC_ZI)
