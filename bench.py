@@ -391,11 +391,12 @@ def batched_extras(args, dev):
     phantoms = {n: workload(n, args.spacing, seed=n) for n in sizes}
     rhos = {n: eng.upload_densities(ph.densities) for n, ph in phantoms.items()}
     rng = np.random.default_rng(64)
-    jobs = []
+    jobs, grid_of = [], []
     for i in range(args.batch_beams):
         n = sizes[int(rng.integers(0, len(sizes)))]
         src, blk = random_beam(rng, rect=(2.0, 20.0), collimator=True)
         jobs.append(eng.job(phantoms[n], rhos[n], src, eng.block_for(blk), SETTINGS))
+        grid_of.append(n)
     eng.prepare((max(sizes),) * 3, (args.spacing,) * 3)
     eng.set_tuning()
     default_ms = time_batch(eng, jobs, iters=2)
@@ -417,12 +418,20 @@ def batched_extras(args, dev):
     batch.close()
     eng.close()
     med = statistics.median(ms)
+    # kernels in the graph: scratch reset, cull, TERMA, then per grid shape
+    # its spectral launches (three kernels on the plane path, five on the
+    # five-pass one), or the tap ranges and the gather
+    if int(tuned["tuning"].get("cone_method", 0)) == 0:
+        per_shape = {n: grid_of.count(n) for n in set(grid_of)}
+        kernels = 3 + sum(spectral_launches(k) * (3 if plane_path((n, n, n)) else 5) for n, k in per_shape.items())
+    else:
+        kernels = 5
     return {"workload": f"{args.batch_beams} beams, slab phantoms 64^3/96^3/128^3/160^3 @ {args.spacing:g} cm, "
                         "jaws U[2,20] cm, gantry U[0,360), collimator U[0,90), one captured CUDA graph",
             "beams_per_s": args.batch_beams * 1000.0 / med, "ms_per_batch": med,
             "uncaptured_default_schedule_ms": default_ms, "tuning": tuned["tuning"],
             "tuned_uncaptured_ms": tuned["ms"], "autotune_cached": tuned["cached"],
-            "kernels_per_batch": 2 * args.batch_beams + 3, "graph_launches_per_batch": 1}
+            "kernels_per_batch": kernels, "graph_launches_per_batch": 1}
 
 
 def reference_updates(eng, ph, jobs):
