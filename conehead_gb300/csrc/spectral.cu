@@ -664,6 +664,175 @@ __global__ void __launch_bounds__(SPEC_THREADS, spec_ctas<MP, LL>()) spec_x_kern
   store_lines(res, b, xs, nx, L, logL);
 }
 
+// ----------------------------------------------- period 384 along x --
+// 8-point DFT in place, natural order in and out (radix 2 over two DFT4s).
+template <bool INV>
+__device__ __forceinline__ void dft8(float2 (&a)[8]) {
+  constexpr float R2 = 0.70710678118654752f;
+  float2 e0 = a[0], e1 = a[2], e2 = a[4], e3 = a[6], o0 = a[1], o1 = a[3], o2 = a[5], o3 = a[7];
+  dft4<INV>(e0, e1, e2, e3);
+  dft4<INV>(o0, o1, o2, o3);
+  o1 = rot<INV>(o1, R2, R2);
+  o2 = INV ? make_float2(-o2.y, o2.x) : make_float2(o2.y, -o2.x);   // times -+i
+  o3 = rot<INV>(o3, -R2, R2);
+  a[0] = make_float2(e0.x + o0.x, e0.y + o0.y);
+  a[4] = make_float2(e0.x - o0.x, e0.y - o0.y);
+  a[1] = make_float2(e1.x + o1.x, e1.y + o1.y);
+  a[5] = make_float2(e1.x - o1.x, e1.y - o1.y);
+  a[2] = make_float2(e2.x + o2.x, e2.y + o2.y);
+  a[6] = make_float2(e2.x - o2.x, e2.y - o2.y);
+  a[3] = make_float2(e3.x + o3.x, e3.y + o3.y);
+  a[7] = make_float2(e3.x - o3.x, e3.y - o3.y);
+}
+
+// 24-point DFT, natural order in (a) and out (x): n = 3 n8 + n3, three DFT8s
+// over n8, twiddles exp(-+2 pi i n3 k8 / 24), eight DFT3s over n3, output
+// k8 + 8 k3.
+template <bool INV>
+__device__ __forceinline__ void dft24(const float2 (&a)[24], float2 (&x)[24]) {
+  // cos and sin of 15 m degrees, m = 0..14
+  constexpr float C[15] = {1.0f,  0.96592582628906829f,  0.86602540378443865f,  0.70710678118654752f,
+                           0.5f,  0.25881904510252076f,  0.0f,                 -0.25881904510252076f,
+                           -0.5f, -0.70710678118654752f, -0.86602540378443865f, -0.96592582628906829f,
+                           -1.0f, -0.96592582628906829f, -0.86602540378443865f};
+  constexpr float S[15] = {0.0f, 0.25881904510252076f, 0.5f, 0.70710678118654752f, 0.86602540378443865f,
+                           0.96592582628906829f, 1.0f, 0.96592582628906829f, 0.86602540378443865f,
+                           0.70710678118654752f, 0.5f, 0.25881904510252076f, 0.0f,
+                           -0.25881904510252076f, -0.5f};
+  float2 b[3][8];
+#pragma unroll
+  for (int n3 = 0; n3 < 3; ++n3) {
+#pragma unroll
+    for (int n8 = 0; n8 < 8; ++n8) b[n3][n8] = a[3 * n8 + n3];
+    dft8<INV>(b[n3]);
+  }
+#pragma unroll
+  for (int k8 = 0; k8 < 8; ++k8) {
+    float2 t0 = b[0][k8], t1 = b[1][k8], t2 = b[2][k8];
+    if (k8 > 0) {
+      t1 = rot<INV>(t1, C[k8], S[k8]);
+      t2 = rot<INV>(t2, C[2 * k8], S[2 * k8]);
+    }
+    dft3<INV>(t0, t1, t2);
+    x[k8] = t0;
+    x[k8 + 8] = t1;
+    x[k8 + 16] = t2;
+  }
+}
+
+// The x pass at period 384 (grids of 129-192 voxels along x): forward
+// transform of rows x < nx <= 192, times S^, inverse, rows x < nx kept, for
+// 16 lines (consecutive kz, 128-byte rows in B) per CTA.  384 = 16 x 24:
+//   forward, n = 24 n1 + n2, k = k1 + 16 k2:
+//     stage 1, thread (c, n2): 16-point DFT over n1 (n1 < 8 nonzero: the
+//       upper half of the padded input) of row 24 n1 + n2, times
+//       exp(-2 pi i n2 k1 / 384), out to shared memory;
+//     stage 2, thread (c, k1): 24-point DFT over n2 -> X[k1 + 16 k2] in
+//       registers;
+//   times S^[k1 + 16 k2] (staged in shared memory by cp.async during stage 1);
+//   inverse, k = k1 + 16 k2, n = n2 + 24 n1:
+//     stage A, the same thread: 24-point DFT over k2 -> n2, times
+//       exp(+2 pi i n2 k1 / 384), out to shared memory;
+//     stage B, thread (c, n2): 16-point DFT over k1 -> rows n2 + 24 n1,
+//       n1 < 8 (rows < 192) written where < nx.
+// Two shared-memory exchanges per transform pair instead of the generic
+// kernel's eight stages; rows of 16 lines are 128 bytes, so every shared
+// access of a half warp (16 lanes, one row) is conflict-free.
+constexpr int X384_THREADS = 384;
+constexpr int X384_SMEM = (2 * 384 * 16 + 384) * 8;   // exchange, S^ block, twiddles
+__global__ void __launch_bounds__(X384_THREADS, 2) spec_x384_kernel(SpecLaunch P) {
+  extern __shared__ float2 spec_sm[];
+  float2* const xb = spec_sm;                 // exchange, row r at 16 r
+  float2* const sb = spec_sm + 384 * 16;      // S^ block, row kx at 16 kx
+  float2* const twb = spec_sm + 2 * 384 * 16; // exp(-2 pi i k / 384)
+  const int pair = blockIdx.x % P.n_pairs, blk = blockIdx.x / P.n_pairs;
+  const SpecPair& pr = P.p[pair];
+  const int My = P.g.M[1], Mz = P.g.M[2];
+  const int nkb = Mz >> 4;
+  const int ky = blk / nkb, kz0 = (blk - ky * nkb) << 4;
+  const size_t xs = (size_t)My * Mz, off = (size_t)ky * Mz + kz0;
+  float2* const b = pr.b + off;
+  const int nx = P.g.n[0];
+  const int c = threadIdx.x & 15;
+  {
+    // S^ rows of the CTA's 16 lines: 384 x 128 bytes, 16 bytes per copy
+    const float2* sh = P.g.shat + off;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int e = threadIdx.x + q * X384_THREADS, i = e >> 3, cp = (e & 7) * 2;
+      const unsigned d = (unsigned)__cvta_generic_to_shared(sb + i * 16 + cp);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(sh + (size_t)i * xs + cp));
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+    twb[threadIdx.x] = __ldg(P.g.tw[0] + threadIdx.x);
+  }
+  __syncthreads();   // twiddle table
+  {
+    // forward stage 1, thread (c, n2): rows 24 n1 + n2, n1 < 8
+    const int n2 = threadIdx.x >> 4;
+    float2 v[16];
+#pragma unroll
+    for (int n1 = 0; n1 < 16; ++n1) {
+      const int x = 24 * n1 + n2;
+      v[n1] = (n1 < 8 && x < nx) ? __ldg(b + (size_t)x * xs + c) : make_float2(0.0f, 0.0f);
+    }
+    dft16_half_in<false>(v);
+    // X[m] of the DFT16 sits in v[4 (m mod 4) + m / 4]; out to row m 24 + n2
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      float2 y = v[4 * (m & 3) + (m >> 2)];
+      if (m > 0) y = cmul(y, twb[n2 * m]);
+      xb[(m * 24 + n2) * 16 + c] = y;
+    }
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  __syncthreads();   // exchange written, S^ landed
+  float2 z[24];
+  const int k1 = threadIdx.x >> 4;
+  if (threadIdx.x < 256) {
+    // forward stage 2, thread (c, k1): rows k1 24 + n2
+    float2 a[24];
+#pragma unroll
+    for (int n2 = 0; n2 < 24; ++n2) a[n2] = xb[(k1 * 24 + n2) * 16 + c];
+    dft24<false>(a, z);
+    const float cs = P.g.conj ? -1.0f : 1.0f;
+#pragma unroll
+    for (int k2 = 0; k2 < 24; ++k2) {
+      const float2 sv = sb[(k1 + 16 * k2) * 16 + c];
+      a[k2] = cmul(z[k2], make_float2(sv.x, cs * sv.y));
+    }
+    // inverse stage A: 24-point DFT over k2 -> n2
+    dft24<true>(a, z);
+  }
+  __syncthreads();   // every read of the exchange done
+  if (threadIdx.x < 256) {
+#pragma unroll
+    for (int n2 = 0; n2 < 24; ++n2) {
+      float2 y = z[n2];
+      if (n2 > 0) {
+        float2 w = twb[n2 * k1];
+        w.y = -w.y;
+        y = cmul(y, w);
+      }
+      xb[(n2 * 16 + k1) * 16 + c] = y;
+    }
+  }
+  __syncthreads();
+  {
+    // inverse stage B, thread (c, n2): 16-point DFT over k1 -> rows n2 + 24 n1
+    const int n2 = threadIdx.x >> 4;
+    float2 v[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = xb[(n2 * 16 + q) * 16 + c];
+    dft16<true>(v);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const int x = n2 + 24 * m;
+      if (x < nx) b[(size_t)x * xs + c] = v[4 * (m & 3) + (m >> 2)];
+    }
+  }
+}
+
 // z inverse: lines (x, y), A in, dose pair out (real part, imaginary part).
 template <int MP, int LL>
 __global__ void __launch_bounds__(SPEC_THREADS, spec_ctas<MP, LL>()) spec_z_inverse_kernel(SpecLaunch P) {
@@ -1198,6 +1367,8 @@ cudaError_t setup_spec_kernels() {
     e = cudaFuncSetAttribute(spec_z_inverse_plane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_ZPLANE_SMEM);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(spec_plane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_PLANE_SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(spec_x384_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, X384_SMEM);
 #define SPEC_SET(mp, ll) \
   if (e == cudaSuccess) e = set_smem<mp, ll>();
   SPEC_FOR_PERIODS(SPEC_SET)
@@ -1237,6 +1408,10 @@ void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
   if (!z_done) spec_z_forward_kernel<-1, -1><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
   SPEC_FOR_PERIODS(SPEC_Y)
   if (!y_done) spec_y_kernel<false, -1, -1><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  if (g.M[0] == 384 && g.n[0] <= 192 && g.M[2] % 16 == 0) {
+    spec_x384_kernel<<<g.M[1] * (g.M[2] / 16) * L.n_pairs, X384_THREADS, X384_SMEM, st>>>(L);
+    x_done = true;
+  }
   SPEC_FOR_PERIODS(SPEC_X)
   if (!x_done) spec_x_kernel<true, -1, -1><<<gx, SPEC_THREADS, SPEC_SMEM, st>>>(L);
 #undef SPEC_Z
