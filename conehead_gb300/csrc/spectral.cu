@@ -833,6 +833,89 @@ __global__ void __launch_bounds__(X384_THREADS, 2) spec_x384_kernel(SpecLaunch P
   }
 }
 
+// The y passes at period 384 (grids of 129-192 voxels along y), 16 lines
+// (consecutive kz, 128-byte rows) per CTA, with the decomposition of the x
+// pass:
+//   forward (A rows y < ny <= 192 -> B, all 384 ky): stage 1, thread
+//     (c, n2): 16-point DFT over n1 of rows 24 n1 + n2 (n1 < 8), twiddled,
+//     out to shared memory; stage 2, thread (c, k1): 24-point DFT over n2,
+//     rows k1 + 16 k2 of B written;
+//   inverse (B -> A rows y < ny): stage A, thread (c, k1): 24-point DFT
+//     over k2 of rows k1 + 16 k2 of B, twiddled, out to shared memory;
+//     stage B, thread (c, n2): 16-point DFT over k1, rows n2 + 24 n1 < ny
+//     of A written.
+constexpr int Y384_SMEM = (384 * 16 + 384) * 8;   // exchange, twiddles
+template <bool INV>
+__global__ void __launch_bounds__(X384_THREADS, 2) spec_y384_kernel(SpecLaunch P) {
+  extern __shared__ float2 spec_sm[];
+  float2* const xb = spec_sm;                 // exchange, row r at 16 r
+  float2* const twb = spec_sm + 384 * 16;     // exp(-2 pi i k / 384)
+  const SpecPair& pr = P.p[blockIdx.y];
+  const int Mz = P.g.M[2], ny = P.g.n[1];
+  const int nkb = Mz >> 4;
+  const int x = blockIdx.x / nkb, kz0 = (blockIdx.x - x * nkb) << 4;
+  const float2* const src = (INV ? pr.b + (size_t)x * 384 * Mz : pr.a + (size_t)x * ny * Mz) + kz0;
+  float2* const dst = (INV ? pr.a + (size_t)x * ny * Mz : pr.b + (size_t)x * 384 * Mz) + kz0;
+  const int c = threadIdx.x & 15, h = threadIdx.x >> 4;   // h: n2 (stages 1, B) or k1 (stages 2, A)
+  twb[threadIdx.x] = __ldg(P.g.tw[1] + threadIdx.x);
+  __syncthreads();   // twiddle table
+  if (!INV) {
+    // stage 1, thread (c, n2 = h)
+    float2 v[16];
+#pragma unroll
+    for (int n1 = 0; n1 < 16; ++n1) {
+      const int y = 24 * n1 + h;
+      v[n1] = (n1 < 8 && y < ny) ? __ldg(src + (size_t)y * Mz + c) : make_float2(0.0f, 0.0f);
+    }
+    dft16_half_in<false>(v);
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      float2 t = v[4 * (m & 3) + (m >> 2)];
+      if (m > 0) t = cmul(t, twb[h * m]);
+      xb[(m * 24 + h) * 16 + c] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < 256) {
+      // stage 2, thread (c, k1 = h)
+      float2 a[24], z[24];
+#pragma unroll
+      for (int n2 = 0; n2 < 24; ++n2) a[n2] = xb[(h * 24 + n2) * 16 + c];
+      dft24<false>(a, z);
+#pragma unroll
+      for (int k2 = 0; k2 < 24; ++k2) dst[(size_t)(h + 16 * k2) * Mz + c] = z[k2];
+    }
+  } else {
+    if (threadIdx.x < 256) {
+      // stage A, thread (c, k1 = h)
+      float2 a[24], z[24];
+#pragma unroll
+      for (int k2 = 0; k2 < 24; ++k2) a[k2] = __ldg(src + (size_t)(h + 16 * k2) * Mz + c);
+      dft24<true>(a, z);
+#pragma unroll
+      for (int n2 = 0; n2 < 24; ++n2) {
+        float2 t = z[n2];
+        if (n2 > 0) {
+          float2 w = twb[n2 * h];
+          w.y = -w.y;
+          t = cmul(t, w);
+        }
+        xb[(n2 * 16 + h) * 16 + c] = t;
+      }
+    }
+    __syncthreads();
+    // stage B, thread (c, n2 = h)
+    float2 v[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = xb[(h * 16 + q) * 16 + c];
+    dft16<true>(v);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const int y = h + 24 * m;
+      if (y < ny) dst[(size_t)y * Mz + c] = v[4 * (m & 3) + (m >> 2)];
+    }
+  }
+}
+
 // z inverse: lines (x, y), A in, dose pair out (real part, imaginary part).
 template <int MP, int LL>
 __global__ void __launch_bounds__(SPEC_THREADS, spec_ctas<MP, LL>()) spec_z_inverse_kernel(SpecLaunch P) {
@@ -1369,6 +1452,10 @@ cudaError_t setup_spec_kernels() {
     e = cudaFuncSetAttribute(spec_plane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_PLANE_SMEM);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(spec_x384_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, X384_SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(spec_y384_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, Y384_SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(spec_y384_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, Y384_SMEM);
 #define SPEC_SET(mp, ll) \
   if (e == cudaSuccess) e = set_smem<mp, ll>();
   SPEC_FOR_PERIODS(SPEC_SET)
@@ -1406,6 +1493,12 @@ void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
   if (!x_done && g.M[0] == mp && g.logL[0] == ll) { spec_x_kernel<true, mp, ll><<<gx, SPEC_THREADS, (spec_smem<mp, ll>()), st>>>(L); x_done = true; }
   SPEC_FOR_PERIODS(SPEC_Z)
   if (!z_done) spec_z_forward_kernel<-1, -1><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  const bool y384 = g.M[1] == 384 && g.n[1] <= 192 && g.M[2] % 16 == 0;
+  const dim3 gy384(g.n[0] * (g.M[2] / 16), L.n_pairs);
+  if (y384) {
+    spec_y384_kernel<false><<<gy384, X384_THREADS, Y384_SMEM, st>>>(L);
+    y_done = true;
+  }
   SPEC_FOR_PERIODS(SPEC_Y)
   if (!y_done) spec_y_kernel<false, -1, -1><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L);
   if (g.M[0] == 384 && g.n[0] <= 192 && g.M[2] % 16 == 0) {
@@ -1422,6 +1515,10 @@ void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
   if (!y_done && g.M[1] == mp && g.logL[1] == ll) { spec_y_kernel<true, mp, ll><<<gy, SPEC_THREADS, (spec_smem<mp, ll>()), st>>>(L); y_done = true; }
 #define SPEC_ZI(mp, ll) \
   if (!z_done && g.M[2] == mp && g.logL[2] == ll) { spec_z_inverse_kernel<mp, ll><<<gz, SPEC_THREADS, (spec_smem<mp, ll>()), st>>>(L); z_done = true; }
+  if (y384) {
+    spec_y384_kernel<true><<<gy384, X384_THREADS, Y384_SMEM, st>>>(L);
+    y_done = true;
+  }
   SPEC_FOR_PERIODS(SPEC_YI)
   if (!y_done) spec_y_kernel<true, -1, -1><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L);
   SPEC_FOR_PERIODS(SPEC_ZI)
