@@ -720,31 +720,78 @@ __device__ __forceinline__ void dft24(const float2 (&a)[24], float2 (&x)[24]) {
   }
 }
 
-// The x pass at period 384 (grids of 129-192 voxels along x): forward
-// transform of rows x < nx <= 192, times S^, inverse, rows x < nx kept, for
-// 16 lines (consecutive kz, 128-byte rows in B) per CTA.  384 = 16 x 24:
-//   forward, n = 24 n1 + n2, k = k1 + 16 k2:
+// 12-point DFT, natural order in (a) and out (x): n = 3 n4 + n3, three DFT4s
+// over n4, twiddles exp(-+2 pi i n3 k4 / 12), four DFT3s over n3, output
+// k4 + 4 k3.
+template <bool INV>
+__device__ __forceinline__ void dft12(const float2 (&a)[12], float2 (&x)[12]) {
+  constexpr float C[7] = {1.0f, 0.86602540378443865f, 0.5f, 0.0f, -0.5f, -0.86602540378443865f, -1.0f};
+  constexpr float S[7] = {0.0f, 0.5f, 0.86602540378443865f, 1.0f, 0.86602540378443865f, 0.5f, 0.0f};
+  float2 b[3][4];
+#pragma unroll
+  for (int n3 = 0; n3 < 3; ++n3) {
+#pragma unroll
+    for (int n4 = 0; n4 < 4; ++n4) b[n3][n4] = a[3 * n4 + n3];
+    dft4<INV>(b[n3][0], b[n3][1], b[n3][2], b[n3][3]);
+  }
+#pragma unroll
+  for (int k4 = 0; k4 < 4; ++k4) {
+    float2 t0 = b[0][k4], t1 = b[1][k4], t2 = b[2][k4];
+    if (k4 > 0) {
+      t1 = rot<INV>(t1, C[k4], S[k4]);
+      t2 = rot<INV>(t2, C[2 * k4], S[2 * k4]);
+    }
+    dft3<INV>(t0, t1, t2);
+    x[k4] = t0;
+    x[k4 + 4] = t1;
+    x[k4 + 8] = t2;
+  }
+}
+
+template <bool INV, int N2>
+__device__ __forceinline__ void dft_n2(const float2 (&a)[N2], float2 (&x)[N2]) {
+  if constexpr (N2 == 24)
+    dft24<INV>(a, x);
+  else
+    dft12<INV>(a, x);
+}
+
+// The x and y passes at periods 16 N2 = 384 (N2 = 24, grids of 129-192
+// voxels along the axis) and 192 (N2 = 12, 65-96 voxels), 16 lines
+// (consecutive kz, 128-byte rows) per CTA:
+//   forward, n = N2 n1 + n2, k = k1 + 16 k2:
 //     stage 1, thread (c, n2): 16-point DFT over n1 (n1 < 8 nonzero: the
-//       upper half of the padded input) of row 24 n1 + n2, times
-//       exp(-2 pi i n2 k1 / 384), out to shared memory;
-//     stage 2, thread (c, k1): 24-point DFT over n2 -> X[k1 + 16 k2] in
+//       upper half of the padded input) of row N2 n1 + n2, times
+//       exp(-2 pi i n2 k1 / (16 N2)), out to shared memory row N2 k1 + n2;
+//     stage 2, thread (c, k1): N2-point DFT over n2 -> X[k1 + 16 k2] in
 //       registers;
-//   times S^[k1 + 16 k2] (staged in shared memory by cp.async during stage 1);
-//   inverse, k = k1 + 16 k2, n = n2 + 24 n1:
-//     stage A, the same thread: 24-point DFT over k2 -> n2, times
-//       exp(+2 pi i n2 k1 / 384), out to shared memory;
-//     stage B, thread (c, n2): 16-point DFT over k1 -> rows n2 + 24 n1,
-//       n1 < 8 (rows < 192) written where < nx.
-// Two shared-memory exchanges per transform pair instead of the generic
-// kernel's eight stages; rows of 16 lines are 128 bytes, so every shared
-// access of a half warp (16 lanes, one row) is conflict-free.
-constexpr int X384_THREADS = 384;
-constexpr int X384_SMEM = (2 * 384 * 16 + 384) * 8;   // exchange, S^ block, twiddles
-__global__ void __launch_bounds__(X384_THREADS, 2) spec_x384_kernel(SpecLaunch P) {
+//   inverse, k = k1 + 16 k2, n = n2 + N2 n1:
+//     stage A, thread (c, k1): N2-point DFT over k2 -> n2, times
+//       exp(+2 pi i n2 k1 / (16 N2)), out to shared memory row 16 n2 + k1;
+//     stage B, thread (c, n2): 16-point DFT over k1 -> rows n2 + N2 n1,
+//       n1 < 8, written where < n.
+// The x pass chains forward, the product with S^ (the CTA's 16 N2 x 16
+// block staged in shared memory by cp.async during stage 1) and inverse:
+// stage 2, the product and stage A in the same thread's registers, two
+// exchanges for the transform pair instead of the generic kernel's six to
+// eight stages.  The forward y pass writes all 16 N2 rows of B from stage 2;
+// the inverse starts with stage A on rows k1 + 16 k2 of B.  A row of 16
+// lines is 128 bytes, one half-warp access: no swizzle is needed.  Stages
+// 1 and B use 16 N2 threads, stages 2 and A 256.
+template <int N2>
+constexpr int r16n_threads() { return 16 * N2 > 256 ? 16 * N2 : 256; }
+template <int N2>
+constexpr int r16n_ctas() { return N2 == 24 ? 2 : 4; }
+template <int N2>
+constexpr int r16n_smem(bool conv) { return ((conv ? 2 : 1) * 16 * N2 * 16 + 16 * N2) * 8; }
+
+template <int N2>
+__global__ void __launch_bounds__(r16n_threads<N2>(), r16n_ctas<N2>()) spec_x16n_kernel(SpecLaunch P) {
+  constexpr int M = 16 * N2, T = r16n_threads<N2>();
   extern __shared__ float2 spec_sm[];
   float2* const xb = spec_sm;                 // exchange, row r at 16 r
-  float2* const sb = spec_sm + 384 * 16;      // S^ block, row kx at 16 kx
-  float2* const twb = spec_sm + 2 * 384 * 16; // exp(-2 pi i k / 384)
+  float2* const sb = spec_sm + M * 16;        // S^ block, row kx at 16 kx
+  float2* const twb = spec_sm + 2 * M * 16;   // exp(-2 pi i k / M)
   const int pair = blockIdx.x % P.n_pairs, blk = blockIdx.x / P.n_pairs;
   const SpecPair& pr = P.p[pair];
   const int My = P.g.M[1], Mz = P.g.M[2];
@@ -753,146 +800,133 @@ __global__ void __launch_bounds__(X384_THREADS, 2) spec_x384_kernel(SpecLaunch P
   const size_t xs = (size_t)My * Mz, off = (size_t)ky * Mz + kz0;
   float2* const b = pr.b + off;
   const int nx = P.g.n[0];
-  const int c = threadIdx.x & 15;
+  const int c = threadIdx.x & 15, h = threadIdx.x >> 4;   // h: n2 (stages 1, B) or k1 (stages 2, A)
   {
-    // S^ rows of the CTA's 16 lines: 384 x 128 bytes, 16 bytes per copy
+    // S^ rows of the CTA's 16 lines: M x 128 bytes, 16 bytes per copy
     const float2* sh = P.g.shat + off;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int e = threadIdx.x + q * X384_THREADS, i = e >> 3, cp = (e & 7) * 2;
+    for (int q = 0; q < 8 * M / T; ++q) {
+      const int e = threadIdx.x + q * T, i = e >> 3, cp = (e & 7) * 2;
       const unsigned d = (unsigned)__cvta_generic_to_shared(sb + i * 16 + cp);
       asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(sh + (size_t)i * xs + cp));
     }
     asm volatile("cp.async.commit_group;\n" ::);
-    twb[threadIdx.x] = __ldg(P.g.tw[0] + threadIdx.x);
+    if (threadIdx.x < M) twb[threadIdx.x] = __ldg(P.g.tw[0] + threadIdx.x);
   }
   __syncthreads();   // twiddle table
-  {
-    // forward stage 1, thread (c, n2): rows 24 n1 + n2, n1 < 8
-    const int n2 = threadIdx.x >> 4;
+  if (threadIdx.x < 16 * N2) {
+    // forward stage 1, thread (c, n2 = h): rows N2 n1 + n2, n1 < 8
     float2 v[16];
 #pragma unroll
     for (int n1 = 0; n1 < 16; ++n1) {
-      const int x = 24 * n1 + n2;
+      const int x = N2 * n1 + h;
       v[n1] = (n1 < 8 && x < nx) ? __ldg(b + (size_t)x * xs + c) : make_float2(0.0f, 0.0f);
     }
     dft16_half_in<false>(v);
-    // X[m] of the DFT16 sits in v[4 (m mod 4) + m / 4]; out to row m 24 + n2
+    // X[m] of the DFT16 sits in v[4 (m mod 4) + m / 4]
 #pragma unroll
     for (int m = 0; m < 16; ++m) {
       float2 y = v[4 * (m & 3) + (m >> 2)];
-      if (m > 0) y = cmul(y, twb[n2 * m]);
-      xb[(m * 24 + n2) * 16 + c] = y;
+      if (m > 0) y = cmul(y, twb[h * m]);
+      xb[(m * N2 + h) * 16 + c] = y;
     }
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
   __syncthreads();   // exchange written, S^ landed
-  float2 z[24];
-  const int k1 = threadIdx.x >> 4;
+  float2 z[N2];
   if (threadIdx.x < 256) {
-    // forward stage 2, thread (c, k1): rows k1 24 + n2
-    float2 a[24];
+    // forward stage 2, thread (c, k1 = h); the product; inverse stage A
+    float2 a[N2];
 #pragma unroll
-    for (int n2 = 0; n2 < 24; ++n2) a[n2] = xb[(k1 * 24 + n2) * 16 + c];
-    dft24<false>(a, z);
+    for (int n2 = 0; n2 < N2; ++n2) a[n2] = xb[(h * N2 + n2) * 16 + c];
+    dft_n2<false, N2>(a, z);
     const float cs = P.g.conj ? -1.0f : 1.0f;
 #pragma unroll
-    for (int k2 = 0; k2 < 24; ++k2) {
-      const float2 sv = sb[(k1 + 16 * k2) * 16 + c];
+    for (int k2 = 0; k2 < N2; ++k2) {
+      const float2 sv = sb[(h + 16 * k2) * 16 + c];
       a[k2] = cmul(z[k2], make_float2(sv.x, cs * sv.y));
     }
-    // inverse stage A: 24-point DFT over k2 -> n2
-    dft24<true>(a, z);
+    dft_n2<true, N2>(a, z);
   }
   __syncthreads();   // every read of the exchange done
   if (threadIdx.x < 256) {
 #pragma unroll
-    for (int n2 = 0; n2 < 24; ++n2) {
+    for (int n2 = 0; n2 < N2; ++n2) {
       float2 y = z[n2];
       if (n2 > 0) {
-        float2 w = twb[n2 * k1];
+        float2 w = twb[n2 * h];
         w.y = -w.y;
         y = cmul(y, w);
       }
-      xb[(n2 * 16 + k1) * 16 + c] = y;
+      xb[(n2 * 16 + h) * 16 + c] = y;
     }
   }
   __syncthreads();
-  {
-    // inverse stage B, thread (c, n2): 16-point DFT over k1 -> rows n2 + 24 n1
-    const int n2 = threadIdx.x >> 4;
+  if (threadIdx.x < 16 * N2) {
+    // inverse stage B, thread (c, n2 = h): rows n2 + N2 n1
     float2 v[16];
 #pragma unroll
-    for (int q = 0; q < 16; ++q) v[q] = xb[(n2 * 16 + q) * 16 + c];
+    for (int q = 0; q < 16; ++q) v[q] = xb[(h * 16 + q) * 16 + c];
     dft16<true>(v);
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
-      const int x = n2 + 24 * m;
+      const int x = h + N2 * m;
       if (x < nx) b[(size_t)x * xs + c] = v[4 * (m & 3) + (m >> 2)];
     }
   }
 }
 
-// The y passes at period 384 (grids of 129-192 voxels along y), 16 lines
-// (consecutive kz, 128-byte rows) per CTA, with the decomposition of the x
-// pass:
-//   forward (A rows y < ny <= 192 -> B, all 384 ky): stage 1, thread
-//     (c, n2): 16-point DFT over n1 of rows 24 n1 + n2 (n1 < 8), twiddled,
-//     out to shared memory; stage 2, thread (c, k1): 24-point DFT over n2,
-//     rows k1 + 16 k2 of B written;
-//   inverse (B -> A rows y < ny): stage A, thread (c, k1): 24-point DFT
-//     over k2 of rows k1 + 16 k2 of B, twiddled, out to shared memory;
-//     stage B, thread (c, n2): 16-point DFT over k1, rows n2 + 24 n1 < ny
-//     of A written.
-constexpr int Y384_SMEM = (384 * 16 + 384) * 8;   // exchange, twiddles
-template <bool INV>
-__global__ void __launch_bounds__(X384_THREADS, 2) spec_y384_kernel(SpecLaunch P) {
+template <bool INV, int N2>
+__global__ void __launch_bounds__(r16n_threads<N2>(), r16n_ctas<N2>()) spec_y16n_kernel(SpecLaunch P) {
+  constexpr int M = 16 * N2;
   extern __shared__ float2 spec_sm[];
   float2* const xb = spec_sm;                 // exchange, row r at 16 r
-  float2* const twb = spec_sm + 384 * 16;     // exp(-2 pi i k / 384)
+  float2* const twb = spec_sm + M * 16;       // exp(-2 pi i k / M)
   const SpecPair& pr = P.p[blockIdx.y];
   const int Mz = P.g.M[2], ny = P.g.n[1];
   const int nkb = Mz >> 4;
   const int x = blockIdx.x / nkb, kz0 = (blockIdx.x - x * nkb) << 4;
-  const float2* const src = (INV ? pr.b + (size_t)x * 384 * Mz : pr.a + (size_t)x * ny * Mz) + kz0;
-  float2* const dst = (INV ? pr.a + (size_t)x * ny * Mz : pr.b + (size_t)x * 384 * Mz) + kz0;
+  const float2* const src = (INV ? pr.b + (size_t)x * M * Mz : pr.a + (size_t)x * ny * Mz) + kz0;
+  float2* const dst = (INV ? pr.a + (size_t)x * ny * Mz : pr.b + (size_t)x * M * Mz) + kz0;
   const int c = threadIdx.x & 15, h = threadIdx.x >> 4;   // h: n2 (stages 1, B) or k1 (stages 2, A)
-  twb[threadIdx.x] = __ldg(P.g.tw[1] + threadIdx.x);
+  if (threadIdx.x < M) twb[threadIdx.x] = __ldg(P.g.tw[1] + threadIdx.x);
   __syncthreads();   // twiddle table
   if (!INV) {
-    // stage 1, thread (c, n2 = h)
-    float2 v[16];
+    if (threadIdx.x < 16 * N2) {
+      // stage 1, thread (c, n2 = h)
+      float2 v[16];
 #pragma unroll
-    for (int n1 = 0; n1 < 16; ++n1) {
-      const int y = 24 * n1 + h;
-      v[n1] = (n1 < 8 && y < ny) ? __ldg(src + (size_t)y * Mz + c) : make_float2(0.0f, 0.0f);
-    }
-    dft16_half_in<false>(v);
+      for (int n1 = 0; n1 < 16; ++n1) {
+        const int y = N2 * n1 + h;
+        v[n1] = (n1 < 8 && y < ny) ? __ldg(src + (size_t)y * Mz + c) : make_float2(0.0f, 0.0f);
+      }
+      dft16_half_in<false>(v);
 #pragma unroll
-    for (int m = 0; m < 16; ++m) {
-      float2 t = v[4 * (m & 3) + (m >> 2)];
-      if (m > 0) t = cmul(t, twb[h * m]);
-      xb[(m * 24 + h) * 16 + c] = t;
+      for (int m = 0; m < 16; ++m) {
+        float2 t = v[4 * (m & 3) + (m >> 2)];
+        if (m > 0) t = cmul(t, twb[h * m]);
+        xb[(m * N2 + h) * 16 + c] = t;
+      }
     }
     __syncthreads();
     if (threadIdx.x < 256) {
       // stage 2, thread (c, k1 = h)
-      float2 a[24], z[24];
+      float2 a[N2], z[N2];
 #pragma unroll
-      for (int n2 = 0; n2 < 24; ++n2) a[n2] = xb[(h * 24 + n2) * 16 + c];
-      dft24<false>(a, z);
+      for (int n2 = 0; n2 < N2; ++n2) a[n2] = xb[(h * N2 + n2) * 16 + c];
+      dft_n2<false, N2>(a, z);
 #pragma unroll
-      for (int k2 = 0; k2 < 24; ++k2) dst[(size_t)(h + 16 * k2) * Mz + c] = z[k2];
+      for (int k2 = 0; k2 < N2; ++k2) dst[(size_t)(h + 16 * k2) * Mz + c] = z[k2];
     }
   } else {
     if (threadIdx.x < 256) {
       // stage A, thread (c, k1 = h)
-      float2 a[24], z[24];
+      float2 a[N2], z[N2];
 #pragma unroll
-      for (int k2 = 0; k2 < 24; ++k2) a[k2] = __ldg(src + (size_t)(h + 16 * k2) * Mz + c);
-      dft24<true>(a, z);
+      for (int k2 = 0; k2 < N2; ++k2) a[k2] = __ldg(src + (size_t)(h + 16 * k2) * Mz + c);
+      dft_n2<true, N2>(a, z);
 #pragma unroll
-      for (int n2 = 0; n2 < 24; ++n2) {
+      for (int n2 = 0; n2 < N2; ++n2) {
         float2 t = z[n2];
         if (n2 > 0) {
           float2 w = twb[n2 * h];
@@ -903,15 +937,17 @@ __global__ void __launch_bounds__(X384_THREADS, 2) spec_y384_kernel(SpecLaunch P
       }
     }
     __syncthreads();
-    // stage B, thread (c, n2 = h)
-    float2 v[16];
+    if (threadIdx.x < 16 * N2) {
+      // stage B, thread (c, n2 = h)
+      float2 v[16];
 #pragma unroll
-    for (int q = 0; q < 16; ++q) v[q] = xb[(h * 16 + q) * 16 + c];
-    dft16<true>(v);
+      for (int q = 0; q < 16; ++q) v[q] = xb[(h * 16 + q) * 16 + c];
+      dft16<true>(v);
 #pragma unroll
-    for (int m = 0; m < 8; ++m) {
-      const int y = h + 24 * m;
-      if (y < ny) dst[(size_t)y * Mz + c] = v[4 * (m & 3) + (m >> 2)];
+      for (int m = 0; m < 8; ++m) {
+        const int y = h + N2 * m;
+        if (y < ny) dst[(size_t)y * Mz + c] = v[4 * (m & 3) + (m >> 2)];
+      }
     }
   }
 }
@@ -1450,12 +1486,12 @@ cudaError_t setup_spec_kernels() {
     e = cudaFuncSetAttribute(spec_z_inverse_plane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_ZPLANE_SMEM);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(spec_plane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPEC_PLANE_SMEM);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(spec_x384_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, X384_SMEM);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(spec_y384_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, Y384_SMEM);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(spec_y384_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, Y384_SMEM);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_x16n_kernel<24>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_smem<24>(true));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_x16n_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_smem<12>(true));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_y16n_kernel<false, 24>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_smem<24>(false));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_y16n_kernel<true, 24>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_smem<24>(false));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_y16n_kernel<false, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_smem<12>(false));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_y16n_kernel<true, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_smem<12>(false));
 #define SPEC_SET(mp, ll) \
   if (e == cudaSuccess) e = set_smem<mp, ll>();
   SPEC_FOR_PERIODS(SPEC_SET)
@@ -1493,18 +1529,19 @@ void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
   if (!x_done && g.M[0] == mp && g.logL[0] == ll) { spec_x_kernel<true, mp, ll><<<gx, SPEC_THREADS, (spec_smem<mp, ll>()), st>>>(L); x_done = true; }
   SPEC_FOR_PERIODS(SPEC_Z)
   if (!z_done) spec_z_forward_kernel<-1, -1><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
-  const bool y384 = g.M[1] == 384 && g.n[1] <= 192 && g.M[2] % 16 == 0;
-  const dim3 gy384(g.n[0] * (g.M[2] / 16), L.n_pairs);
-  if (y384) {
-    spec_y384_kernel<false><<<gy384, X384_THREADS, Y384_SMEM, st>>>(L);
-    y_done = true;
-  }
+  // periods 384 and 192 along y and x: the 16 x N2 kernels (16 lines per CTA)
+  const int ny2 = g.M[2] % 16 == 0 && 2 * g.n[1] <= g.M[1] ? (g.M[1] == 384 ? 24 : g.M[1] == 192 ? 12 : 0) : 0;
+  const int nx2 = g.M[2] % 16 == 0 && 2 * g.n[0] <= g.M[0] ? (g.M[0] == 384 ? 24 : g.M[0] == 192 ? 12 : 0) : 0;
+  const dim3 gy16(g.n[0] * (g.M[2] / 16), L.n_pairs);
+  const unsigned gx16 = g.M[1] * (g.M[2] / 16) * L.n_pairs;
+  if (ny2 == 24) spec_y16n_kernel<false, 24><<<gy16, r16n_threads<24>(), r16n_smem<24>(false), st>>>(L);
+  if (ny2 == 12) spec_y16n_kernel<false, 12><<<gy16, r16n_threads<12>(), r16n_smem<12>(false), st>>>(L);
+  y_done = ny2 != 0;
   SPEC_FOR_PERIODS(SPEC_Y)
   if (!y_done) spec_y_kernel<false, -1, -1><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L);
-  if (g.M[0] == 384 && g.n[0] <= 192 && g.M[2] % 16 == 0) {
-    spec_x384_kernel<<<g.M[1] * (g.M[2] / 16) * L.n_pairs, X384_THREADS, X384_SMEM, st>>>(L);
-    x_done = true;
-  }
+  if (nx2 == 24) spec_x16n_kernel<24><<<gx16, r16n_threads<24>(), r16n_smem<24>(true), st>>>(L);
+  if (nx2 == 12) spec_x16n_kernel<12><<<gx16, r16n_threads<12>(), r16n_smem<12>(true), st>>>(L);
+  x_done = nx2 != 0;
   SPEC_FOR_PERIODS(SPEC_X)
   if (!x_done) spec_x_kernel<true, -1, -1><<<gx, SPEC_THREADS, SPEC_SMEM, st>>>(L);
 #undef SPEC_Z
@@ -1515,10 +1552,9 @@ void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
   if (!y_done && g.M[1] == mp && g.logL[1] == ll) { spec_y_kernel<true, mp, ll><<<gy, SPEC_THREADS, (spec_smem<mp, ll>()), st>>>(L); y_done = true; }
 #define SPEC_ZI(mp, ll) \
   if (!z_done && g.M[2] == mp && g.logL[2] == ll) { spec_z_inverse_kernel<mp, ll><<<gz, SPEC_THREADS, (spec_smem<mp, ll>()), st>>>(L); z_done = true; }
-  if (y384) {
-    spec_y384_kernel<true><<<gy384, X384_THREADS, Y384_SMEM, st>>>(L);
-    y_done = true;
-  }
+  if (ny2 == 24) spec_y16n_kernel<true, 24><<<gy16, r16n_threads<24>(), r16n_smem<24>(false), st>>>(L);
+  if (ny2 == 12) spec_y16n_kernel<true, 12><<<gy16, r16n_threads<12>(), r16n_smem<12>(false), st>>>(L);
+  y_done = ny2 != 0;
   SPEC_FOR_PERIODS(SPEC_YI)
   if (!y_done) spec_y_kernel<true, -1, -1><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L);
   SPEC_FOR_PERIODS(SPEC_ZI)

@@ -114,59 +114,61 @@ def test_period_256_schedule_and_layouts():
                 assert len(set(w.tolist())) == 16 and len(set(rd.tolist())) == 16
 
 
-def test_period_384_schedule():
-    """Period 384 as 16 x 24 (spec_x384_kernel, spec_y384_kernel): forward
-    with n = 24 n1 + n2 -- thread (line, n2) takes a 16-point DFT over n1 of
-    rows 24 n1 + n2 with only n1 < 8 non-zero (rows < 192, the padded input),
-    twiddled by exp(-2 pi i n2 k1 / 384) into exchange row 24 k1 + n2; thread
-    (line, k1) takes a 24-point DFT over n2 of rows 24 k1 + n2 and holds
-    X[k1 + 16 k2].  Times S^ there, then the inverse with n = n2 + 24 n1 in
-    the same thread (24-point DFT over k2, twiddled by exp(+2 pi i n2 k1 /
-    384), into exchange row 16 n2 + k1) and thread (line, n2) takes the
-    16-point DFT over k1 of rows 16 n2 + k1 into rows n2 + 24 n1, n1 < 8.
-    The 24-point DFT is three DFT8s over n8 of rows 3 n8 + n3, twiddles
-    exp(-+2 pi i n3 k8 / 24), eight DFT3s into k8 + 8 k3.  Both exchange maps
-    fill the 384 rows once."""
-    rng = np.random.default_rng(384)
-    nx = 177
-    x = np.zeros((16, 384), complex)
+@pytest.mark.parametrize("n2", [12, 24])
+def test_period_16xn2_schedule(n2):
+    """Periods 16 N2 = 192 and 384 as 16 x N2 (spec_x16n_kernel,
+    spec_y16n_kernel): forward with n = N2 n1 + n2 -- thread (line, n2) takes
+    a 16-point DFT over n1 of rows N2 n1 + n2 with only n1 < 8 non-zero (the
+    padded input), twiddled by exp(-2 pi i n2 k1 / M) into exchange row
+    N2 k1 + n2; thread (line, k1) takes an N2-point DFT over n2 of rows
+    N2 k1 + n2 and holds X[k1 + 16 k2].  Times S^ there, then the inverse
+    with n = n2 + N2 n1 in the same thread (N2-point DFT over k2, twiddled by
+    exp(+2 pi i n2 k1 / M), into exchange row 16 n2 + k1) and thread
+    (line, n2) takes the 16-point DFT over k1 of rows 16 n2 + k1 into rows
+    n2 + N2 n1, n1 < 8.  The N2-point DFT is three DFT(N2/3)s over the rows
+    3 m + n3, twiddles exp(-+2 pi i n3 k / N2), DFT3s into k + (N2/3) k3.
+    Both exchange maps fill the M rows once."""
+    M = 16 * n2
+    rng = np.random.default_rng(M)
+    nx = M // 2 - 15
+    x = np.zeros((16, M), complex)
     x[:, :nx] = rng.standard_normal((16, nx)) + 1j * rng.standard_normal((16, nx))
-    s = rng.standard_normal((16, 384)) + 1j * rng.standard_normal((16, 384))
-    tw = np.exp(-2j * np.pi * np.arange(384) / 384)
+    s = rng.standard_normal((16, M)) + 1j * rng.standard_normal((16, M))
+    tw = np.exp(-2j * np.pi * np.arange(M) / M)
     k1 = np.arange(16)
-    n2 = np.arange(24)
+    j2 = np.arange(n2)
     n1 = np.arange(16)
+    q = n2 // 3
 
-    def dft24(a, inv):
-        # a[..., 24] along the last axis, the kernel's 3 x 8 split
+    def dftn(a, inv):
+        # a[..., N2] along the last axis, the kernels' 3 x (N2 / 3) split
         sign = 1 if inv else -1
-        b = np.stack([np.fft.ifft(a[..., n3::3], axis=-1) * 8 if inv else np.fft.fft(a[..., n3::3], axis=-1)
-                      for n3 in range(3)], axis=-2)                        # [..., n3, k8]
-        k8 = np.arange(8)
-        b = b * np.exp(sign * 2j * np.pi * np.arange(3)[:, None] * k8[None, :] / 24)
-        y = np.fft.ifft(b, axis=-2) * 3 if inv else np.fft.fft(b, axis=-2)  # [..., k3, k8]
-        return y.reshape(*a.shape[:-1], 24)                                 # index k8 + 8 k3
+        b = np.stack([np.fft.ifft(a[..., n3::3], axis=-1) * q if inv else np.fft.fft(a[..., n3::3], axis=-1)
+                      for n3 in range(3)], axis=-2)                        # [..., n3, k]
+        b = b * np.exp(sign * 2j * np.pi * np.arange(3)[:, None] * np.arange(q)[None, :] / n2)
+        y = np.fft.ifft(b, axis=-2) * 3 if inv else np.fft.fft(b, axis=-2)  # [..., k3, k]
+        return y.reshape(*a.shape[:-1], n2)                                 # index k + q k3
 
-    # forward stage 1 into the exchange (rows 24 k1 + n2)
-    assert not x[:, 24 * n1[8:, None] + n2[None, :]].any()
-    y1 = np.fft.fft(x[:, 24 * n1[:, None] + n2[None, :]], axis=1)              # [line][k1][n2]
-    y1 = y1 * tw[(k1[:, None] * n2[None, :]) % 384]
-    rows = np.full((16, 384), np.nan + 0j)
-    rows[:, (24 * k1[:, None] + n2[None, :]).ravel()] = y1.reshape(16, -1)
+    # forward stage 1 into the exchange (rows N2 k1 + n2)
+    assert not x[:, n2 * n1[8:, None] + j2[None, :]].any()
+    y1 = np.fft.fft(x[:, n2 * n1[:, None] + j2[None, :]], axis=1)             # [line][k1][n2]
+    y1 = y1 * tw[(k1[:, None] * j2[None, :]) % M]
+    rows = np.full((16, M), np.nan + 0j)
+    rows[:, (n2 * k1[:, None] + j2[None, :]).ravel()] = y1.reshape(16, -1)
     assert not np.isnan(rows).any()
     # forward stage 2: X[k1 + 16 k2] per thread (line, k1)
-    z = dft24(rows[:, 24 * k1[:, None] + n2[None, :]], False)                # [line][k1][k2]
+    z = dftn(rows[:, n2 * k1[:, None] + j2[None, :]], False)                 # [line][k1][k2]
     X = np.fft.fft(x, axis=1)
-    assert np.abs(z - X[:, k1[:, None] + 16 * n2[None, :]]).max() <= 1e-12 * np.abs(X).max()
+    assert np.abs(z - X[:, k1[:, None] + 16 * j2[None, :]]).max() <= 1e-12 * np.abs(X).max()
     # product, inverse stage A into the exchange (rows 16 n2 + k1)
-    u = z * s[:, k1[:, None] + 16 * n2[None, :]]
-    v = dft24(u, True) * np.conj(tw[(k1[:, None] * n2[None, :]) % 384])      # [line][k1][n2]
-    rows = np.full((16, 384), np.nan + 0j)
-    rows[:, (16 * n2[None, :] + k1[:, None]).ravel()] = v.reshape(16, -1)
+    u = z * s[:, k1[:, None] + 16 * j2[None, :]]
+    v = dftn(u, True) * np.conj(tw[(k1[:, None] * j2[None, :]) % M])        # [line][k1][n2]
+    rows = np.full((16, M), np.nan + 0j)
+    rows[:, (16 * j2[None, :] + k1[:, None]).ravel()] = v.reshape(16, -1)
     assert not np.isnan(rows).any()
-    # inverse stage B: rows n2 + 24 n1
-    out = np.fft.ifft(rows[:, 16 * n2[:, None] + k1[None, :]], axis=2) * 16   # [line][n2][n1]
-    got = np.empty((16, 384), complex)
-    got[:, (n2[:, None] + 24 * n1[None, :]).ravel()] = out.reshape(16, -1)
-    ref = np.fft.ifft(X * s, axis=1) * 384
+    # inverse stage B: rows n2 + N2 n1
+    out = np.fft.ifft(rows[:, 16 * j2[:, None] + k1[None, :]], axis=2) * 16  # [line][n2][n1]
+    got = np.empty((16, M), complex)
+    got[:, (j2[:, None] + n2 * n1[None, :]).ravel()] = out.reshape(16, -1)
+    ref = np.fft.ifft(X * s, axis=1) * M
     assert np.abs(got[:, :nx] - ref[:, :nx]).max() <= 1e-11 * np.abs(ref).max()
