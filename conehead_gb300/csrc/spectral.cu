@@ -952,6 +952,139 @@ __global__ void __launch_bounds__(r16n_threads<N2>(), r16n_ctas<N2>()) spec_y16n
   }
 }
 
+// The z passes at periods 16 N2 = 384 and 192, 16 lines (x, y) per CTA.
+// Lines along z are contiguous, so lanes run along z: thread (n2, line)
+// with n2 fastest in the 16-point stages (consecutive z: the TERMA reads and
+// dose writes are coalesced), thread (k1, line) with k1 fastest in the
+// N2-point stages (consecutive k: 128-byte runs of A).  The exchange holds
+// each line's M rows with one slot of padding after every 16 (line c, row r
+// at c (M + M/16) + r + r/16), and both transforms use rows 16 n2 + k1, so
+// that 16 lanes at consecutive k1 (one row step) and at consecutive n2 (17
+// slots apart) fall in 16 different banks.
+//   forward: stage 1, thread (n2, c): 16-point DFT over n1 of z = N2 n1 + n2
+//     (n1 < 8), twiddled by exp(-2 pi i n2 k1 / M), into rows 16 n2 + k1;
+//     stage 2, thread (k1, c): N2-point DFT over n2 -> A[k1 + 16 k2];
+//   inverse: stage A, thread (k1, c): N2-point DFT over k2 of A[k1 + 16 k2],
+//     twiddled by exp(+2 pi i n2 k1 / M), into rows 16 n2 + k1; stage B,
+//     thread (n2, c): 16-point DFT over k1 -> z = n2 + N2 n1 < nz.
+template <int N2>
+constexpr int r16n_zsmem() { return (16 * (16 * N2 + N2) + 16 * N2) * 8; }
+template <int N2>
+__device__ __forceinline__ int zslot(int r, int c) { return c * (17 * N2) + r + (r >> 4); }
+
+template <int N2>
+__global__ void __launch_bounds__(r16n_threads<N2>(), r16n_ctas<N2>()) spec_z16n_forward_kernel(SpecLaunch P) {
+  constexpr int M = 16 * N2, T = r16n_threads<N2>();
+  extern __shared__ float2 spec_sm[];
+  float2* const xb = spec_sm;
+  float2* const twb = spec_sm + 16 * 17 * N2;
+  const SpecPair& pr = P.p[blockIdx.y];
+  const int nl = P.g.n[0] * P.g.n[1], nz = P.g.n[2];
+  const int l0 = blockIdx.x * 16;
+  __shared__ unsigned char zf[2][16];
+  bool mine = false;
+  if (threadIdx.x < 16) {
+    const int c = threadIdx.x, l = l0 + c, lc = l < nl ? l : nl - 1;
+    const unsigned a1 = pr.l1 ? (unsigned)__ldg(pr.l1 + lc) : 1u;
+    const unsigned a2 = (pr.t2 && pr.l2) ? (unsigned)__ldg(pr.l2 + lc) : 1u;
+    zf[0][c] = l < nl && a1 != 0u;
+    zf[1][c] = l < nl && pr.t2 && a2 != 0u;
+    mine = zf[0][c] || zf[1][c];
+  }
+  if (threadIdx.x < M) twb[threadIdx.x] = __ldg(P.g.tw[2] + threadIdx.x);
+  if (!__syncthreads_or(mine)) {
+    // no TERMA on these lines: zeros, two values per 16-byte store
+    const int lines = min(16, nl - l0);
+    float4* a4 = reinterpret_cast<float4*>(pr.a + (size_t)l0 * M);
+    for (int e = threadIdx.x; e < lines * M / 2; e += T) a4[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    return;
+  }
+  if (threadIdx.x < 16 * N2) {
+    const int n2 = threadIdx.x % N2, c = threadIdx.x / N2, l = l0 + c;
+    const bool f1 = zf[0][c], f2 = zf[1][c];
+    const size_t o = (size_t)(l < nl ? l : 0) * P.g.zp;
+    float2 v[16];
+#pragma unroll
+    for (int n1 = 0; n1 < 16; ++n1) {
+      const int z = N2 * n1 + n2;
+      v[n1] = make_float2(0.0f, 0.0f);
+      if (n1 < 8 && z < nz) {
+        if (f1) v[n1].x = __ldg(pr.t1 + o + z);
+        if (f2) v[n1].y = __ldg(pr.t2 + o + z);
+      }
+    }
+    dft16_half_in<false>(v);
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      float2 y = v[4 * (m & 3) + (m >> 2)];
+      if (m > 0) y = cmul(y, twb[n2 * m]);
+      xb[zslot<N2>(16 * n2 + m, c)] = y;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 256) {
+    const int k1 = threadIdx.x & 15, c = threadIdx.x >> 4, l = l0 + c;
+    float2 a[N2], z[N2];
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) a[n2] = xb[zslot<N2>(16 * n2 + k1, c)];
+    dft_n2<false, N2>(a, z);
+    if (l < nl) {
+#pragma unroll
+      for (int k2 = 0; k2 < N2; ++k2) pr.a[(size_t)l * M + k1 + 16 * k2] = z[k2];
+    }
+  }
+}
+
+template <int N2>
+__global__ void __launch_bounds__(r16n_threads<N2>(), r16n_ctas<N2>()) spec_z16n_inverse_kernel(SpecLaunch P) {
+  constexpr int M = 16 * N2;
+  extern __shared__ float2 spec_sm[];
+  float2* const xb = spec_sm;
+  float2* const twb = spec_sm + 16 * 17 * N2;
+  const SpecPair& pr = P.p[blockIdx.y];
+  const int nl = P.g.n[0] * P.g.n[1], nz = P.g.n[2];
+  const int l0 = blockIdx.x * 16;
+  if (threadIdx.x < M) twb[threadIdx.x] = __ldg(P.g.tw[2] + threadIdx.x);
+  __syncthreads();   // twiddle table
+  if (threadIdx.x < 256) {
+    const int k1 = threadIdx.x & 15, c = threadIdx.x >> 4, l = l0 + c;
+    const float2* al = pr.a + (size_t)(l < nl ? l : 0) * M;
+    float2 a[N2], z[N2];
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) a[k2] = l < nl ? __ldg(al + k1 + 16 * k2) : make_float2(0.0f, 0.0f);
+    dft_n2<true, N2>(a, z);
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) {
+      float2 y = z[n2];
+      if (n2 > 0) {
+        float2 w = twb[n2 * k1];
+        w.y = -w.y;
+        y = cmul(y, w);
+      }
+      xb[zslot<N2>(16 * n2 + k1, c)] = y;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 16 * N2) {
+    const int n2 = threadIdx.x % N2, c = threadIdx.x / N2, l = l0 + c;
+    float2 v[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = xb[zslot<N2>(16 * n2 + q, c)];
+    dft16<true>(v);
+    if (l < nl) {
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        const int z = n2 + N2 * m;
+        if (z < nz) {
+          const float2 d = v[4 * (m & 3) + (m >> 2)];
+          pr.d1[(size_t)l * nz + z] = d.x;
+          if (pr.d2) pr.d2[(size_t)l * nz + z] = d.y;
+        }
+      }
+    }
+  }
+}
+
 // z inverse: lines (x, y), A in, dose pair out (real part, imaginary part).
 template <int MP, int LL>
 __global__ void __launch_bounds__(SPEC_THREADS, spec_ctas<MP, LL>()) spec_z_inverse_kernel(SpecLaunch P) {
@@ -1492,6 +1625,10 @@ cudaError_t setup_spec_kernels() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_y16n_kernel<true, 24>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_smem<24>(false));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_y16n_kernel<false, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_smem<12>(false));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_y16n_kernel<true, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_smem<12>(false));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_z16n_forward_kernel<24>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_zsmem<24>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_z16n_forward_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_zsmem<12>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_z16n_inverse_kernel<24>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_zsmem<24>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_z16n_inverse_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_zsmem<12>());
 #define SPEC_SET(mp, ll) \
   if (e == cudaSuccess) e = set_smem<mp, ll>();
   SPEC_FOR_PERIODS(SPEC_SET)
@@ -1527,6 +1664,12 @@ void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
   if (!y_done && g.M[1] == mp && g.logL[1] == ll) { spec_y_kernel<false, mp, ll><<<gy, SPEC_THREADS, (spec_smem<mp, ll>()), st>>>(L); y_done = true; }
 #define SPEC_X(mp, ll) \
   if (!x_done && g.M[0] == mp && g.logL[0] == ll) { spec_x_kernel<true, mp, ll><<<gx, SPEC_THREADS, (spec_smem<mp, ll>()), st>>>(L); x_done = true; }
+  // periods 384 and 192 along z: the 16 x N2 kernels
+  const int nz2 = 2 * g.n[2] <= g.M[2] ? (g.M[2] == 384 ? 24 : g.M[2] == 192 ? 12 : 0) : 0;
+  const dim3 gz16((nl + 15) / 16, L.n_pairs);
+  if (nz2 == 24) spec_z16n_forward_kernel<24><<<gz16, r16n_threads<24>(), r16n_zsmem<24>(), st>>>(L);
+  if (nz2 == 12) spec_z16n_forward_kernel<12><<<gz16, r16n_threads<12>(), r16n_zsmem<12>(), st>>>(L);
+  z_done = nz2 != 0;
   SPEC_FOR_PERIODS(SPEC_Z)
   if (!z_done) spec_z_forward_kernel<-1, -1><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
   // periods 384 and 192 along y and x: the 16 x N2 kernels (16 lines per CTA)
@@ -1557,6 +1700,9 @@ void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
   y_done = ny2 != 0;
   SPEC_FOR_PERIODS(SPEC_YI)
   if (!y_done) spec_y_kernel<true, -1, -1><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L);
+  if (nz2 == 24) spec_z16n_inverse_kernel<24><<<gz16, r16n_threads<24>(), r16n_zsmem<24>(), st>>>(L);
+  if (nz2 == 12) spec_z16n_inverse_kernel<12><<<gz16, r16n_threads<12>(), r16n_zsmem<12>(), st>>>(L);
+  z_done = nz2 != 0;
   SPEC_FOR_PERIODS(SPEC_ZI)
   if (!z_done) spec_z_inverse_kernel<-1, -1><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
 #undef SPEC_YI
