@@ -172,3 +172,27 @@ def test_period_16xn2_schedule(n2):
     got[:, (j2[:, None] + n2 * n1[None, :]).ravel()] = out.reshape(16, -1)
     ref = np.fft.ifft(X * s, axis=1) * M
     assert np.abs(got[:, :nx] - ref[:, :nx]).max() <= 1e-11 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("n2", [12, 24])
+def test_period_16xn2_z_exchange_layout(n2):
+    """The z passes' exchange (spec_z16n_*_kernel): line c, row r at
+    c (M + M/16) + r + r/16.  The slots of the 16 lines are distinct and
+    inside the buffer, and the four access patterns -- 16 lanes at
+    consecutive k1 of one line (rows 16 n2 + k1) and 16 lanes at consecutive
+    n2 running on into the next line (rows 16 n2 + q) -- fall in 16
+    different banks of 8 bytes."""
+    M = 16 * n2
+    slot = lambda r, c: c * (17 * n2) + r + (r >> 4)
+    slots = [slot(r, c) for c in range(16) for r in range(M)]
+    assert len(set(slots)) == len(slots) and max(slots) < 16 * 17 * n2
+    for q in range(16):
+        # lanes along n2 (thread t -> n2 = t mod N2, line t / N2), one warp half at a time
+        for h0 in range(0, 16 * n2, 16):
+            banks = {slot(16 * (t % n2) + q, t // n2) % 16 for t in range(h0, h0 + 16)}
+            assert len(banks) == 16
+    for r2 in range(n2):
+        # lanes along k1 (thread t -> k1 = t mod 16, line t / 16)
+        for c in range(16):
+            banks = {slot(16 * r2 + k1, c) % 16 for k1 in range(16)}
+            assert len(banks) == 16
