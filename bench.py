@@ -75,6 +75,28 @@ SETTINGS = {
 }
 
 
+def host_link_rate(dev_bufs, host_bufs, stream, reps=3):
+    """GB/s of the machine's host link on the e2e loop's own buffers (one step's
+    doses and their pinned host copies), measured after the timed region:
+    device -> host and host -> device, one copy per buffer, CUDA events on
+    the copy stream."""
+    import torch
+    nbytes = sum(t.numel() * t.element_size() for t in dev_bufs)
+    out = {}
+    for name, pairs in (("d2h_gbs", list(zip(host_bufs, dev_bufs))), ("h2d_gbs", list(zip(dev_bufs, host_bufs)))):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(reps):
+                for dst, src in pairs:
+                    dst.copy_(src, non_blocking=True)
+            e1.record(stream)
+        e1.synchronize()
+        out[name] = reps * nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    out["bytes"] = nbytes
+    return out
+
+
 @contextlib.contextmanager
 def quiet_gc():
     """Collect once, then keep Python's cyclic collector out of a timed loop
@@ -751,7 +773,8 @@ def run_ours(args):
     e2e = {"value": world * args.steps * B / e2e_s, "unit": "beams/s",
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(B * N * 4),
            "pipelined": "two buffer sets, copy-in / compute / copy-out streams: step s+1's inputs and "
-                        "step s-1's doses move while step s computes; each set's job descriptors built once"}
+                        "step s-1's doses move while step s computes; each set's job descriptors built once",
+           "host_link": host_link_rate(d_doses[0], h_doses[0], out_st)}
 
     # ---- reference-equivalent voxel·direction updates/s (untimed, a few beams)
     updates_line = None
