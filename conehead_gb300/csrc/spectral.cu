@@ -750,14 +750,21 @@ __device__ __forceinline__ void dft12(const float2 (&a)[12], float2 (&x)[12]) {
 
 template <bool INV, int N2>
 __device__ __forceinline__ void dft_n2(const float2 (&a)[N2], float2 (&x)[N2]) {
-  if constexpr (N2 == 24)
+  if constexpr (N2 == 24) {
     dft24<INV>(a, x);
-  else
+  } else if constexpr (N2 == 12) {
     dft12<INV>(a, x);
+  } else {
+    static_assert(N2 == 8, "16 x N2 periods: 128, 192, 384");
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x[i] = a[i];
+    dft8<INV>(x);
+  }
 }
 
 // The x and y passes at periods 16 N2 = 384 (N2 = 24, grids of 129-192
-// voxels along the axis) and 192 (N2 = 12, 65-96 voxels), 16 lines
+// voxels along the axis), 192 (N2 = 12, 65-96 voxels) and 128 (N2 = 8,
+// 49-64 voxels), 16 lines
 // (consecutive kz, 128-byte rows) per CTA:
 //   forward, n = N2 n1 + n2, k = k1 + 16 k2:
 //     stage 1, thread (c, n2): 16-point DFT over n1 (n1 < 8 nonzero: the
@@ -952,7 +959,7 @@ __global__ void __launch_bounds__(r16n_threads<N2>(), r16n_ctas<N2>()) spec_y16n
   }
 }
 
-// The z passes at periods 16 N2 = 384 and 192, 16 lines (x, y) per CTA.
+// The z passes at periods 16 N2 = 384, 192 and 128, 16 lines (x, y) per CTA.
 // Lines along z are contiguous, so lanes run along z: thread (n2, line)
 // with n2 fastest in the 16-point stages (consecutive z: the TERMA reads and
 // dose writes are coalesced), thread (k1, line) with k1 fastest in the
@@ -1629,6 +1636,11 @@ cudaError_t setup_spec_kernels() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_z16n_forward_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_zsmem<12>());
   if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_z16n_inverse_kernel<24>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_zsmem<24>());
   if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_z16n_inverse_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_zsmem<12>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_x16n_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_smem<8>(true));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_y16n_kernel<false, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_smem<8>(false));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_y16n_kernel<true, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_smem<8>(false));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_z16n_forward_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_zsmem<8>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(spec_z16n_inverse_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, r16n_zsmem<8>());
 #define SPEC_SET(mp, ll) \
   if (e == cudaSuccess) e = set_smem<mp, ll>();
   SPEC_FOR_PERIODS(SPEC_SET)
@@ -1665,25 +1677,28 @@ void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
 #define SPEC_X(mp, ll) \
   if (!x_done && g.M[0] == mp && g.logL[0] == ll) { spec_x_kernel<true, mp, ll><<<gx, SPEC_THREADS, (spec_smem<mp, ll>()), st>>>(L); x_done = true; }
   // periods 384 and 192 along z: the 16 x N2 kernels
-  const int nz2 = 2 * g.n[2] <= g.M[2] ? (g.M[2] == 384 ? 24 : g.M[2] == 192 ? 12 : 0) : 0;
+  const int nz2 = 2 * g.n[2] <= g.M[2] ? (g.M[2] == 384 ? 24 : g.M[2] == 192 ? 12 : g.M[2] == 128 ? 8 : 0) : 0;
   const dim3 gz16((nl + 15) / 16, L.n_pairs);
   if (nz2 == 24) spec_z16n_forward_kernel<24><<<gz16, r16n_threads<24>(), r16n_zsmem<24>(), st>>>(L);
   if (nz2 == 12) spec_z16n_forward_kernel<12><<<gz16, r16n_threads<12>(), r16n_zsmem<12>(), st>>>(L);
+  if (nz2 == 8) spec_z16n_forward_kernel<8><<<gz16, r16n_threads<8>(), r16n_zsmem<8>(), st>>>(L);
   z_done = nz2 != 0;
   SPEC_FOR_PERIODS(SPEC_Z)
   if (!z_done) spec_z_forward_kernel<-1, -1><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);
   // periods 384 and 192 along y and x: the 16 x N2 kernels (16 lines per CTA)
-  const int ny2 = g.M[2] % 16 == 0 && 2 * g.n[1] <= g.M[1] ? (g.M[1] == 384 ? 24 : g.M[1] == 192 ? 12 : 0) : 0;
-  const int nx2 = g.M[2] % 16 == 0 && 2 * g.n[0] <= g.M[0] ? (g.M[0] == 384 ? 24 : g.M[0] == 192 ? 12 : 0) : 0;
+  const int ny2 = g.M[2] % 16 == 0 && 2 * g.n[1] <= g.M[1] ? (g.M[1] == 384 ? 24 : g.M[1] == 192 ? 12 : g.M[1] == 128 ? 8 : 0) : 0;
+  const int nx2 = g.M[2] % 16 == 0 && 2 * g.n[0] <= g.M[0] ? (g.M[0] == 384 ? 24 : g.M[0] == 192 ? 12 : g.M[0] == 128 ? 8 : 0) : 0;
   const dim3 gy16(g.n[0] * (g.M[2] / 16), L.n_pairs);
   const unsigned gx16 = g.M[1] * (g.M[2] / 16) * L.n_pairs;
   if (ny2 == 24) spec_y16n_kernel<false, 24><<<gy16, r16n_threads<24>(), r16n_smem<24>(false), st>>>(L);
   if (ny2 == 12) spec_y16n_kernel<false, 12><<<gy16, r16n_threads<12>(), r16n_smem<12>(false), st>>>(L);
+  if (ny2 == 8) spec_y16n_kernel<false, 8><<<gy16, r16n_threads<8>(), r16n_smem<8>(false), st>>>(L);
   y_done = ny2 != 0;
   SPEC_FOR_PERIODS(SPEC_Y)
   if (!y_done) spec_y_kernel<false, -1, -1><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L);
   if (nx2 == 24) spec_x16n_kernel<24><<<gx16, r16n_threads<24>(), r16n_smem<24>(true), st>>>(L);
   if (nx2 == 12) spec_x16n_kernel<12><<<gx16, r16n_threads<12>(), r16n_smem<12>(true), st>>>(L);
+  if (nx2 == 8) spec_x16n_kernel<8><<<gx16, r16n_threads<8>(), r16n_smem<8>(true), st>>>(L);
   x_done = nx2 != 0;
   SPEC_FOR_PERIODS(SPEC_X)
   if (!x_done) spec_x_kernel<true, -1, -1><<<gx, SPEC_THREADS, SPEC_SMEM, st>>>(L);
@@ -1697,11 +1712,13 @@ void launch_spec_pairs(const SpecLaunch& L, cudaStream_t st) {
   if (!z_done && g.M[2] == mp && g.logL[2] == ll) { spec_z_inverse_kernel<mp, ll><<<gz, SPEC_THREADS, (spec_smem<mp, ll>()), st>>>(L); z_done = true; }
   if (ny2 == 24) spec_y16n_kernel<true, 24><<<gy16, r16n_threads<24>(), r16n_smem<24>(false), st>>>(L);
   if (ny2 == 12) spec_y16n_kernel<true, 12><<<gy16, r16n_threads<12>(), r16n_smem<12>(false), st>>>(L);
+  if (ny2 == 8) spec_y16n_kernel<true, 8><<<gy16, r16n_threads<8>(), r16n_smem<8>(false), st>>>(L);
   y_done = ny2 != 0;
   SPEC_FOR_PERIODS(SPEC_YI)
   if (!y_done) spec_y_kernel<true, -1, -1><<<gy, SPEC_THREADS, SPEC_SMEM, st>>>(L);
   if (nz2 == 24) spec_z16n_inverse_kernel<24><<<gz16, r16n_threads<24>(), r16n_zsmem<24>(), st>>>(L);
   if (nz2 == 12) spec_z16n_inverse_kernel<12><<<gz16, r16n_threads<12>(), r16n_zsmem<12>(), st>>>(L);
+  if (nz2 == 8) spec_z16n_inverse_kernel<8><<<gz16, r16n_threads<8>(), r16n_zsmem<8>(), st>>>(L);
   z_done = nz2 != 0;
   SPEC_FOR_PERIODS(SPEC_ZI)
   if (!z_done) spec_z_inverse_kernel<-1, -1><<<gz, SPEC_THREADS, SPEC_SMEM, st>>>(L);

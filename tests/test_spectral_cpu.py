@@ -114,9 +114,9 @@ def test_period_256_schedule_and_layouts():
                 assert len(set(w.tolist())) == 16 and len(set(rd.tolist())) == 16
 
 
-@pytest.mark.parametrize("n2", [12, 24])
+@pytest.mark.parametrize("n2", [8, 12, 24])
 def test_period_16xn2_schedule(n2):
-    """Periods 16 N2 = 192 and 384 as 16 x N2 (spec_x16n_kernel,
+    """Periods 16 N2 = 128, 192 and 384 as 16 x N2 (spec_x16n_kernel,
     spec_y16n_kernel): forward with n = N2 n1 + n2 -- thread (line, n2) takes
     a 16-point DFT over n1 of rows N2 n1 + n2 with only n1 < 8 non-zero (the
     padded input), twiddled by exp(-2 pi i n2 k1 / M) into exchange row
@@ -126,7 +126,8 @@ def test_period_16xn2_schedule(n2):
     exp(+2 pi i n2 k1 / M), into exchange row 16 n2 + k1) and thread
     (line, n2) takes the 16-point DFT over k1 of rows 16 n2 + k1 into rows
     n2 + N2 n1, n1 < 8.  The N2-point DFT is three DFT(N2/3)s over the rows
-    3 m + n3, twiddles exp(-+2 pi i n3 k / N2), DFT3s into k + (N2/3) k3.
+    3 m + n3, twiddles exp(-+2 pi i n3 k / N2), DFT3s into k + (N2/3) k3
+    (N2 = 12, 24), or one DFT8.
     Both exchange maps fill the M rows once."""
     M = 16 * n2
     rng = np.random.default_rng(M)
@@ -142,6 +143,9 @@ def test_period_16xn2_schedule(n2):
 
     def dftn(a, inv):
         # a[..., N2] along the last axis, the kernels' 3 x (N2 / 3) split
+        # (N2 = 8: one DFT8)
+        if n2 % 3:
+            return np.fft.ifft(a, axis=-1) * n2 if inv else np.fft.fft(a, axis=-1)
         sign = 1 if inv else -1
         b = np.stack([np.fft.ifft(a[..., n3::3], axis=-1) * q if inv else np.fft.fft(a[..., n3::3], axis=-1)
                       for n3 in range(3)], axis=-2)                        # [..., n3, k]
@@ -174,7 +178,7 @@ def test_period_16xn2_schedule(n2):
     assert np.abs(got[:, :nx] - ref[:, :nx]).max() <= 1e-11 * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("n2", [12, 24])
+@pytest.mark.parametrize("n2", [8, 12, 24])
 def test_period_16xn2_z_exchange_layout(n2):
     """The z passes' exchange (spec_z16n_*_kernel): line c, row r at
     c (M + M/16) + r + r/16.  The slots of the 16 lines are distinct and
