@@ -5,7 +5,8 @@
   pair of a launch holds one beam) and batches of more than 32 beams (more
   than one launch per grid shape, reusing one work arena).
 * Axes of 97-128 voxels (period 256, the passes with one butterfly per thread
-  and stage) agree with the gather on every axis and on odd sizes.
+  and stage) agree with the gather on every axis and on odd sizes; so do
+  axes at periods 384, 192 and 128 (the 16 x N2 kernels), mixed per grid.
 * The cone operator C and its transpose agree between the two methods on a
   random sparse input, also with two axes at period 256.
 * The stencil spectrum of a grid shape is built by ch_plan_prepare, counted
@@ -119,6 +120,31 @@ def test_spectral_period_256_axes(eng, settings):
         assert b.max() > 0
         worst = max(worst, np.abs(a - b).max() / b.max())
     print(f"spectral vs gather, 5 beams on 99x101x120 / 128x36x97: {worst:.2e} of Dmax")
+    assert worst <= TOL
+
+
+def test_spectral_16xn2_periods_per_axis(eng, settings):
+    """Axes at FFT periods 384, 192 and 128 take the 16 x N2 pass kernels
+    (N2 = 24, 12, 8), chosen per axis: 150 x 70 x 50 (x at 384, y at 192,
+    z at 128) and 66 x 180 x 90 (x at 192, y at 384, z at 192), three beams
+    each (the last pair of a shape holds one), against the gather."""
+    from conehead_gb300.phantoms import random_beam
+    rng = np.random.default_rng(74)
+    sp = (0.25, 0.25, 0.25)
+    phs = [_grid_phantom((150, 70, 50), sp, 7), _grid_phantom((66, 180, 90), sp, 8)]
+    rhos = [eng.upload_densities(p.densities) for p in phs]
+    jobs = []
+    for i in range(6):
+        k = i % 2
+        src, blk = random_beam(rng, rect=(2.0, 8.0), collimator=True)
+        jobs.append(eng.job(phs[k], rhos[k], src, eng.block_for(blk), settings))
+    spec = _doses(eng, jobs, 0)
+    gath = _doses(eng, jobs, 1)
+    worst = 0.0
+    for a, b in zip(spec, gath):
+        assert b.max() > 0
+        worst = max(worst, np.abs(a - b).max() / b.max())
+    print(f"spectral vs gather, 6 beams on 150x70x50 / 66x180x90: {worst:.2e} of Dmax")
     assert worst <= TOL
 
 
