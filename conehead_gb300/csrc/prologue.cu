@@ -415,27 +415,28 @@ __device__ float radiological_depth(const float* __restrict__ rho, const GridDev
 // the line can pass the per-voxel test below; 0.01 cm on top of the margin
 // covers the float32 rounding of both tests (about 1e-5 cm here).
 __device__ __forceinline__ bool line_outside(const GridDev& g, const BeamDev& b, float px, float py) {
-  float xlo = INFINITY, xhi = -INFINITY, zlo = INFINITY, zhi = -INFINITY, inv_max = 0.0f, lat_max = 0.0f;
+  // every lane of the warp tests the same line: even lanes project its first
+  // voxel, odd lanes its last, and one shuffle step combines the two
+  const unsigned full = 0xffffffffu;
+  const int e = threadIdx.x & 1;
   const float kk = fabsf(b.a_K);
-#pragma unroll
-  for (int e = 0; e < 2; ++e) {
-    const float pz = voxel_centre(g.origin[2], g.spacing[2], e ? g.n[2] - 1 : 0);
-    const float np_ = b.vyf[0] * px + b.vyf[1] * py + b.vyf[2] * pz;
-    const float m0p = b.m0f[0] * px + b.m0f[1] * py + b.m0f[2] * pz;
-    const float m2p = b.m2f[0] * px + b.m2f[1] * py + b.m2f[2] * pz;
-    const float depth = np_ - b.a_nS;
-    if (!(depth > 0.2f * kk)) return false;   // near or behind the source plane: test per voxel
-    const float inv = 1.0f / depth;
-    const float si = -b.a_K * inv;
-    const float xb = b.a_c0 + si * (b.a_m0S - m0p);
-    const float zb = b.a_c2 + si * (b.a_m2S - m2p);
-    xlo = fminf(xlo, xb);
-    xhi = fmaxf(xhi, xb);
-    zlo = fminf(zlo, zb);
-    zhi = fmaxf(zhi, zb);
-    inv_max = fmaxf(inv_max, inv);
-    lat_max = fmaxf(lat_max, fmaxf(fabsf(b.a_m0S - m0p), fabsf(b.a_m2S - m2p)) * inv);
-  }
+  const float pz = voxel_centre(g.origin[2], g.spacing[2], e ? g.n[2] - 1 : 0);
+  const float np_ = b.vyf[0] * px + b.vyf[1] * py + b.vyf[2] * pz;
+  const float m0p = b.m0f[0] * px + b.m0f[1] * py + b.m0f[2] * pz;
+  const float m2p = b.m2f[0] * px + b.m2f[1] * py + b.m2f[2] * pz;
+  const float depth = np_ - b.a_nS;
+  const bool ok = depth > 0.2f * kk;
+  // near or behind the source plane at either end: test per voxel
+  if (!(ok && __shfl_xor_sync(full, (int)ok, 1))) return false;
+  const float inv = 1.0f / depth;
+  const float si = -b.a_K * inv;
+  const float xb = b.a_c0 + si * (b.a_m0S - m0p);
+  const float zb = b.a_c2 + si * (b.a_m2S - m2p);
+  const float lat = fmaxf(fabsf(b.a_m0S - m0p), fabsf(b.a_m2S - m2p)) * inv;
+  const float xb2 = __shfl_xor_sync(full, xb, 1), zb2 = __shfl_xor_sync(full, zb, 1);
+  const float inv_max = fmaxf(inv, __shfl_xor_sync(full, inv, 1));
+  const float lat_max = fmaxf(lat, __shfl_xor_sync(full, lat, 1));
+  const float xlo = fminf(xb, xb2), xhi = fmaxf(xb, xb2), zlo = fminf(zb, zb2), zhi = fmaxf(zb, zb2);
   const float M = b.cull_margin_k * kk * inv_max * (1.0f + lat_max) + 0.02f;
   return xhi < b.cx_lo - M || xlo > b.cx_hi + M || zhi < b.cz_lo - M || zlo > b.cz_hi + M;
 }
