@@ -222,7 +222,7 @@ def test_autograd_matches_backward_and_descends(eng, settings):
     target = torch.from_numpy(sphere_target(ph, (0.0, 0.0, 0.0), 3.0, value=1.0)).cuda()
     w = torch.full(bl.shape, 0.5, device="cuda", requires_grad=True)
     dose = beamlet_dose(w, op)
-    scale = float(target.max() / dose.max())
+    scale = float(target.max() / dose.detach().max())
     loss = ((dose * scale - target) ** 2).sum()
     loss.backward()
     direct = op.backward(2 * scale * (dose.detach() * scale - target), weights=w.detach())
