@@ -34,8 +34,11 @@ def weights_cho(E):
 def weights_ali(E):
     c1, c2, c3, e_e = 1.222, 5.147, -1.186, 5.76
     ratio = E / e_e
-    thin = (1 + c3 * ratio + np.power(ratio, 2)) * \
-        (np.log(e_e * (e_e - E) / E + 1.65) - 0.5)
+    # above the endpoint energy the logarithm's argument is negative: NaN,
+    # and those weights are zero below
+    with np.errstate(invalid="ignore"):
+        thin = (1 + c3 * ratio + np.power(ratio, 2)) * \
+            (np.log(e_e * (e_e - E) / E + 1.65) - 0.5)
     psi = thin * np.exp(-mu_W(E) * np.power(c1, 2) - mu_Al(E) * np.power(c2, 2))
     if isinstance(psi, np.ndarray) and psi.ndim > 0:
         psi[psi < 0] = 0
