@@ -998,7 +998,9 @@ __global__ void __launch_bounds__(r16n_threads<N2>(), r16n_ctas<N2>()) spec_z16n
     zf[1][c] = l < nl && pr.t2 && a2 != 0u;
     mine = zf[0][c] || zf[1][c];
   }
-  if (threadIdx.x < M) twb[threadIdx.x] = __ldg(P.g.tw[2] + threadIdx.x);
+  // stage-1 twiddles exp(-2 pi i n2 m / M) at m N2 + n2: lanes at consecutive
+  // n2 read consecutive slots
+  for (int i = threadIdx.x; i < M; i += T) twb[i] = __ldg(P.g.tw[2] + (i % N2) * (i / N2));
   if (!__syncthreads_or(mine)) {
     // no TERMA on these lines: zeros, two values per 16-byte store
     const int lines = min(16, nl - l0);
@@ -1024,7 +1026,7 @@ __global__ void __launch_bounds__(r16n_threads<N2>(), r16n_ctas<N2>()) spec_z16n
 #pragma unroll
     for (int m = 0; m < 16; ++m) {
       float2 y = v[4 * (m & 3) + (m >> 2)];
-      if (m > 0) y = cmul(y, twb[n2 * m]);
+      if (m > 0) y = cmul(y, twb[m * N2 + n2]);
       xb[zslot<N2>(16 * n2 + m, c)] = y;
     }
   }
@@ -1051,7 +1053,9 @@ __global__ void __launch_bounds__(r16n_threads<N2>(), r16n_ctas<N2>()) spec_z16n
   const SpecPair& pr = P.p[blockIdx.y];
   const int nl = P.g.n[0] * P.g.n[1], nz = P.g.n[2];
   const int l0 = blockIdx.x * 16;
-  if (threadIdx.x < M) twb[threadIdx.x] = __ldg(P.g.tw[2] + threadIdx.x);
+  // stage-A twiddles exp(-2 pi i n2 k1 / M) at 16 n2 + k1: lanes at
+  // consecutive k1 read consecutive slots
+  for (int i = threadIdx.x; i < M; i += r16n_threads<N2>()) twb[i] = __ldg(P.g.tw[2] + (i >> 4) * (i & 15));
   __syncthreads();   // twiddle table
   if (threadIdx.x < 256) {
     const int k1 = threadIdx.x & 15, c = threadIdx.x >> 4, l = l0 + c;
@@ -1064,7 +1068,7 @@ __global__ void __launch_bounds__(r16n_threads<N2>(), r16n_ctas<N2>()) spec_z16n
     for (int n2 = 0; n2 < N2; ++n2) {
       float2 y = z[n2];
       if (n2 > 0) {
-        float2 w = twb[n2 * k1];
+        float2 w = twb[16 * n2 + k1];
         w.y = -w.y;
         y = cmul(y, w);
       }
