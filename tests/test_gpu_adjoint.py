@@ -232,4 +232,4 @@ def test_autograd_matches_backward_and_descends(eng, settings):
         step = 1e-3 / float(w.grad.abs().max())
         w2 = (w - step * w.grad).clamp(min=0)
         loss2 = ((op.forward(w2) * scale - target) ** 2).sum()
-    assert float(loss2) < float(loss)
+    assert float(loss2) < float(loss.detach())
