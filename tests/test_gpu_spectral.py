@@ -8,7 +8,8 @@
   and stage) agree with the gather on every axis and on odd sizes; so do
   axes at periods 384, 192 and 128 (the 16 x N2 kernels), mixed per grid.
 * The cone operator C and its transpose agree between the two methods on a
-  random sparse input, also with two axes at period 256.
+  random sparse input, also with two axes at period 256 and with the 16 x N2
+  kernels on every axis (50 x 150 x 66: periods 128, 384, 192).
 * The stencil spectrum of a grid shape is built by ch_plan_prepare, counted
   in ch_plan_memory's tables, reused by the next call and dropped when the
   kernel changes.
@@ -148,7 +149,7 @@ def test_spectral_16xn2_periods_per_axis(eng, settings):
     assert worst <= TOL
 
 
-@pytest.mark.parametrize("size", [(29, 36, 31), (100, 36, 110)])
+@pytest.mark.parametrize("size", [(29, 36, 31), (100, 36, 110), (50, 150, 66)])
 def test_spectral_operator_and_transpose(eng, settings, size):
     import torch
     from conehead_gb300.adjoint import cone
