@@ -413,13 +413,13 @@ __device__ __forceinline__ void store_lines(const float2* res, float2* __restric
 // consecutive kz, so L also divides Mz.
 // z forward: lines (x, y), TERMA pair in, A out.  One CTA per L lines and pair.
 // Shared memory of a five-pass kernel: two buffers of its CTA's lines.  A
-// compile-time period and line count take only what they use, so periods
-// 96, 192 and 384 (3072 values per CTA, 48 KB) run four CTAs per SM, the
-// others (4096 values, 64 KB) three.
+// compile-time period and line count take only what they use, so period 96
+// (3072 values per CTA, 48 KB) runs four CTAs per SM, the others (4096
+// values, 64 KB) three.
 template <int MP, int LL>
 constexpr int spec_elems() {
-  static_assert(MP <= 0 || (MP << LL) <= SPEC_ELEMS, "lines of a CTA");
-  return MP > 0 ? (MP << LL) : SPEC_ELEMS;
+  static_assert(MP <= 0 || (MP << (LL > 0 ? LL : 0)) <= SPEC_ELEMS, "lines of a CTA");
+  return MP > 0 ? (MP << (LL > 0 ? LL : 0)) : SPEC_ELEMS;
 }
 template <int MP, int LL>
 constexpr int spec_smem() { return 2 * spec_elems<MP, LL>() * 8; }
@@ -484,34 +484,34 @@ __global__ void __launch_bounds__(SPEC_THREADS, spec_ctas<MP, LL>()) spec_z_forw
 #pragma unroll
         for (int k2 = 0; k2 < 4; ++k2) pr.a[(size_t)l * Mz + j + 16 * (k1 + 4 * k2)] = v[4 * k1 + k2];
     }
-    return;
-  }
-  {
-    // every load of the thread first, then the shared-memory stores
-    float2 v[SPEC_ELEMS / SPEC_THREADS];
+  } else {
+    {
+      // every load of the thread first, then the shared-memory stores
+      float2 v[SPEC_ELEMS / SPEC_THREADS];
 #pragma unroll
-    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
-      const int e = threadIdx.x + q * SPEC_THREADS;
-      const int c = e / Mz, i = e - c * Mz, l = l0 + c;
-      v[q] = make_float2(0.0f, 0.0f);
-      if (c < L && l < nl && i < nz) {
-        const size_t o = (size_t)l * P.g.zp + i;
-        if (zf[0][c]) v[q].x = __ldg(pr.t1 + o);
-        if (zf[1][c]) v[q].y = __ldg(pr.t2 + o);
+      for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
+        const int e = threadIdx.x + q * SPEC_THREADS;
+        const int c = e / Mz, i = e - c * Mz, l = l0 + c;
+        v[q] = make_float2(0.0f, 0.0f);
+        if (c < L && l < nl && i < nz) {
+          const size_t o = (size_t)l * P.g.zp + i;
+          if (zf[0][c]) v[q].x = __ldg(pr.t1 + o);
+          if (zf[1][c]) v[q].y = __ldg(pr.t2 + o);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
+        const int e = threadIdx.x + q * SPEC_THREADS;
+        const int c = e / Mz, i = e - c * Mz;
+        if (c < L) sm[swz(i, c, L)] = v[q];
       }
     }
-#pragma unroll
-    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
-      const int e = threadIdx.x + q * SPEC_THREADS;
-      const int c = e / Mz, i = e - c * Mz;
-      if (c < L) sm[swz(i, c, L)] = v[q];
+    __syncthreads();
+    const float2* res = fft_block<false, MP, LL>(sm, sm2, Mz, logL, P.g.tw[2], 2 * nz <= Mz, false);
+    for (int e = threadIdx.x; e < L * Mz; e += SPEC_THREADS) {
+      const int c = e / Mz, i = e - c * Mz, l = l0 + c;
+      if (l < nl) pr.a[(size_t)l * Mz + i] = res[swz(i, c, L)];
     }
-  }
-  __syncthreads();
-  const float2* res = fft_block<false, MP, LL>(sm, sm2, Mz, logL, P.g.tw[2], 2 * nz <= Mz, false);
-  for (int e = threadIdx.x; e < L * Mz; e += SPEC_THREADS) {
-    const int c = e / Mz, i = e - c * Mz, l = l0 + c;
-    if (l < nl) pr.a[(size_t)l * Mz + i] = res[swz(i, c, L)];
   }
 }
 
@@ -1130,31 +1130,31 @@ __global__ void __launch_bounds__(SPEC_THREADS, spec_ctas<MP, LL>()) spec_z_inve
           }
         }
     }
-    return;
-  }
-  {
-    float2 v[SPEC_ELEMS / SPEC_THREADS];
+  } else {
+    {
+      float2 v[SPEC_ELEMS / SPEC_THREADS];
 #pragma unroll
-    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
-      const int e = threadIdx.x + q * SPEC_THREADS;
+      for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
+        const int e = threadIdx.x + q * SPEC_THREADS;
+        const int c = e / Mz, i = e - c * Mz, l = l0 + c;
+        v[q] = (c < L && l < nl) ? pr.a[(size_t)l * Mz + i] : make_float2(0.0f, 0.0f);
+      }
+#pragma unroll
+      for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
+        const int e = threadIdx.x + q * SPEC_THREADS;
+        const int c = e / Mz, i = e - c * Mz;
+        if (c < L) sm[swz(i, c, L)] = v[q];
+      }
+    }
+    __syncthreads();
+    const float2* res = fft_block<true, MP, LL>(sm, sm2, Mz, logL, P.g.tw[2], false, 2 * nz <= Mz);
+    for (int e = threadIdx.x; e < L * Mz; e += SPEC_THREADS) {
       const int c = e / Mz, i = e - c * Mz, l = l0 + c;
-      v[q] = (c < L && l < nl) ? pr.a[(size_t)l * Mz + i] : make_float2(0.0f, 0.0f);
-    }
-#pragma unroll
-    for (int q = 0; q < SPEC_ELEMS / SPEC_THREADS; ++q) {
-      const int e = threadIdx.x + q * SPEC_THREADS;
-      const int c = e / Mz, i = e - c * Mz;
-      if (c < L) sm[swz(i, c, L)] = v[q];
-    }
-  }
-  __syncthreads();
-  const float2* res = fft_block<true, MP, LL>(sm, sm2, Mz, logL, P.g.tw[2], false, 2 * nz <= Mz);
-  for (int e = threadIdx.x; e < L * Mz; e += SPEC_THREADS) {
-    const int c = e / Mz, i = e - c * Mz, l = l0 + c;
-    if (l < nl && i < nz) {
-      const float2 v = res[swz(i, c, L)];
-      pr.d1[(size_t)l * nz + i] = v.x;
-      if (pr.d2) pr.d2[(size_t)l * nz + i] = v.y;
+      if (l < nl && i < nz) {
+        const float2 v = res[swz(i, c, L)];
+        pr.d1[(size_t)l * nz + i] = v.x;
+        if (pr.d2) pr.d2[(size_t)l * nz + i] = v.y;
+      }
     }
   }
 }
@@ -1610,7 +1610,8 @@ int spec_pass_lines_log2(int M, int Mz) {
 
 // Compile-time periods for the common shapes (grids of 17 to 256 voxels per
 // axis): a pass is specialised when its lines per CTA are the natural ones.
-#define SPEC_FOR_PERIODS(X) X(64, 6) X(96, 5) X(128, 5) X(192, 4) X(256, 4) X(384, 3) X(512, 3)
+// (periods 128, 192 and 384 take the 16 x N2 kernels on every axis)
+#define SPEC_FOR_PERIODS(X) X(64, 6) X(96, 5) X(256, 4) X(512, 3)
 
 template <int MP, int LL>
 cudaError_t set_smem() {
